@@ -1,0 +1,334 @@
+"""Benchmark of the CVT hot path (plain Lloyd, the reference's gCVT loop).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: 4096 x 4096 float32 density (1 + 32 seeded Gaussians, 0 outside the
+disk of radius 0.48), 262,144 seeded sites uniform in the disk, no fixed
+sites.  One step = the gCVT computation on it: load the inputs, 100 Lloyd
+iterations with the reference's omega schedule (no early stop), the final
+labelling pass.  Every step is a full Lloyd run from the same initial sites;
+the density (64 MB) and site grid (64 MB) exceed no cache individually but the
+loop's working set fits in L2 between iterations, so the L2 is flushed before
+each step (config.l2).
+
+Metric: Gpix-pass/s = n^2 x labelling passes / second, 101 passes per step
+(100 Lloyd iterations + the final labelling), whole job over all GPUs.
+  value : inputs resident in HBM (device-to-device load), CUDA events on the
+          launching stream, max over ranks.
+  e2e   : the same through the C ABI with pinned host buffers: host->device
+          copies of sites, density and mask and the device->host copy of the
+          label grid inside every timed step.
+  roofline: the dominant kernel (fused label + moment row pass): algorithmic
+          bytes per launch / its mean launch duration (CUDA events on the
+          launching stream over the same workload) against the measured HBM
+          copy bandwidth.
+--impl reference runs the reference's algorithm on the host cores (the
+oracle's OpenMP restatement of gcvt.cu, all threads) on a bounded sample of
+the same workload, in the same unit.
+Multi-GPU: independent replicas, one per rank (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "surface-remesher_gb300")
+for _p in (os.path.join(PKG, "python"), PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+CONFIG = "plain_4096"
+SEED = 1
+ITERS = 100
+PASSES = ITERS + 1
+METRIC = "Gpix-pass/s, plain Lloyd CVT (gCVT loop), 4096^2 grid, 262,144 sites, 100 iterations"
+UNIT = "Gpix-pass/s"
+# Algorithmic bytes of one fused row-pass launch per pixel and per site:
+# density 4 B/px + site bitmap 1/8 B/px + column summaries 1/16 B/px, and the
+# per-site moment accumulators (hi + lo float4) 32 B/site.
+ALG_BYTES_PER_PX = 4.0 + 0.125 + 0.0625
+ALG_BYTES_PER_SITE = 32.0
+# dram__bytes_read.sum + dram__bytes_write.sum of one row-pass launch on this
+# workload, from the ncu capture summarised in profiles/ (None until captured).
+NCU_TRAFFIC_BYTES = None
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline_sample(sites, rho, mask, target_s=10.0):
+    """The oracle's OpenMP restatement of the reference's Lloyd loop (faithful
+    FP32 mode, all host threads) on a bounded sample: as many iterations of
+    the 4096^2 workload as fit in about target_s seconds."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    n = sites.shape[0]
+    t = time.perf_counter()
+    orc.gcvt(sites, rho, mask, 1, 1, mode=orc.FAITHFUL, fixed_iters=1)
+    t1 = time.perf_counter() - t
+    k = int(max(1, min(ITERS, target_s / max(t1, 1e-3))))
+    t = time.perf_counter()
+    orc.gcvt(sites, rho, mask, 1, k, mode=orc.FAITHFUL, fixed_iters=k)
+    dt = time.perf_counter() - t
+    # k iterations + the final labelling pass
+    value = n * n * (k + 1) / dt / 1e9
+    return {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d Lloyd iterations + final labelling of the 4096^2 / 262,144-site "
+                      "workload, faithful FP32 restatement of gcvt.cu, %.1f s" % (k, dt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from workloads import config_inputs
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    n = sites.shape[0]
+    iters_per_step = 2
+    for _ in range(args.warmup):
+        orc.gcvt(sites, rho, mask, 1, iters_per_step, mode=orc.FAITHFUL, fixed_iters=iters_per_step)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        orc.gcvt(sites, rho, mask, 1, iters_per_step, mode=orc.FAITHFUL, fixed_iters=iters_per_step)
+    dt = time.perf_counter() - t
+    value = n * n * (iters_per_step + 1) * args.steps / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int16",
+        "data": "synthetic (seeded Gaussian density on a disk, uniform sites)",
+        "config": {"workload": CONFIG, "n": n, "sites": int((sites[..., 0] != -32768).sum()),
+                   "sample_iterations_per_step": iters_per_step},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d Lloyd iterations + final labelling per step, faithful "
+                                   "FP32 OpenMP restatement of gcvt.cu" % iters_per_step},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import gcvt_gb300 as G
+    from workloads import config_inputs
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    sites, rho, mask, iters = config_inputs(CONFIG, seed=SEED)
+    assert iters == ITERS
+    n = sites.shape[0]
+    nsites = int((sites[..., 0] != -32768).sum())
+    stream = torch.cuda.Stream(device=dev)
+    d_sites = torch.from_numpy(sites).to(dev)
+    d_rho = torch.from_numpy(rho).to(dev)
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_out = torch.empty_like(d_sites)
+    h_sites = torch.from_numpy(sites).pin_memory()
+    h_rho = torch.from_numpy(rho).pin_memory()
+    h_mask = torch.from_numpy(mask).pin_memory()
+    h_out = torch.empty(d_sites.shape, dtype=torch.int16).pin_memory()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > L2
+    ctx = G.Context(n)
+    ctx.set_stream(stream.cuda_stream)
+
+    def step_device():
+        ctx.load(d_sites, d_rho, d_mask)
+        ctx.iterate(ITERS)
+        ctx.label(d_out)
+
+    def step_host():
+        ctx.load(h_sites, h_rho, h_mask)
+        ctx.iterate(ITERS)
+        ctx.label(h_out)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def timed(step_fn, steps):
+        total = 0.0
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_fn()
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        barrier()
+        return total / 1e3
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_device()
+        with ClockSampler(local) as clk:
+            t_dev = timed(step_device, args.steps)
+        for _ in range(max(1, args.warmup // 2)):
+            step_host()
+        t_e2e = timed(step_host, args.steps)
+        # dominant kernel: per-launch durations on the launching stream
+        ctx.load(d_sites, d_rho, d_mask)
+        kms = ctx.time_kernels(20)
+        torch.cuda.synchronize(dev)
+        info = ctx.info()
+    if ws > 1:
+        t = torch.tensor([t_dev, t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev, t_e2e = t.tolist()
+    passes = n * n * PASSES * args.steps * ws
+    value = passes / t_dev / 1e9
+    e2e = passes / t_e2e / 1e9
+    peak, peak_kind = measured_peak()
+    alg = n * n * ALG_BYTES_PER_PX + nsites * ALG_BYTES_PER_SITE
+    rows_s = kms[1] / 1e3
+    achieved = alg / rows_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+int16",
+        "data": "synthetic (seeded Gaussian density on a disk, uniform sites)",
+        "config": {"workload": CONFIG, "n": n, "sites": nsites, "iterations": ITERS,
+                   "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
+                   "parallelism": "replicas x%d" % ws},
+        "iter_per_s": ITERS * args.steps * ws / t_dev,
+        "kernel_ms": {"column_summary": kms[0], "row_pass": kms[1], "update": kms[2]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
+                     "peak_source": peak_kind, "kernel": "k_rows<1> (fused label + moments)",
+                     "algorithmic_bytes": alg},
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": int(h_sites.numel() * 2 + h_rho.numel() * 4 + h_mask.numel()),
+                "d2h_bytes_per_step": int(h_out.numel() * 2),
+                "ms_per_step": t_e2e / args.steps * 1e3},
+        "gpu_launches": args.steps * (1 + 3 * ITERS + 2),
+        "clocks": clk.summary(),
+        "final_energy": info["energy"],
+    }
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask)
+        if args.reference_gpu:
+            line["reference_gpu"] = reference_gpu(sites, rho, mask)
+        print(json.dumps(line))
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def reference_gpu(sites, rho, mask):
+    """The reference's own kernels (compiled from its sources into
+    oracle/_ref/gcvt_ref.cubin) under gcvt.cu's loop on the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    if not orc.ref_available():
+        return {"unavailable": "reference cubin not built"}
+    n = sites.shape[0]
+    orc.ref_gcvt(sites, rho, mask, 1, 10, fixed_iters=10)
+    _, info = orc.ref_gcvt(sites, rho, mask, 1, ITERS, fixed_iters=ITERS)
+    return {"value": n * n * PASSES / (info["loop_ms"] / 1e3) / 1e9, "unit": UNIT,
+            "loop_ms": info["loop_ms"], "total_ms": info["total_ms"],
+            "what": "gcvt.cu kernels on this GPU, 100 iterations + final labelling; loop_ms "
+                    "excludes its per-call allocation and copies, total_ms includes them"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-gpu", action="store_true",
+                    help="also time the reference's own kernels on this GPU")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,139 @@
+/*
+ * gcvt_gb300.h -- C ABI of libgcvt_gb300.so, the GB300 (sm_103a) engine for
+ * the centroidal Voronoi tessellation (CVT) hot path of Surface-Remesher.
+ *
+ * Conventions shared with the reference (source/gcvt.h:26-27):
+ *   - a grid of size n holds pixel (x, y) at index y*n + x;
+ *   - a site / label grid holds two int16 per pixel, x then y (the memory
+ *     layout of CUDA's short2); MARKER (-32768) marks "no site";
+ *   - density is float32, 0 outside the domain; the mask is one byte per
+ *     pixel, nonzero = fixed (constraint) site.
+ *
+ * Every function returns GCVT_OK (0) or a GCVT_ERR_* status; none exits the
+ * process.  The only exception is the reference's own C++ entry point gCVT()
+ * declared at the end, which keeps the reference's void signature and exits
+ * with a message on failure as the reference does (gcvt.cu:41-47).
+ *
+ * Pointers tagged `mem` are host pointers when mem == GCVT_MEM_HOST and
+ * device pointers (on the context's device) when mem == GCVT_MEM_DEVICE.
+ */
+#ifndef GCVT_GB300_H
+#define GCVT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCVT_MARKER (-32768)
+
+enum gcvt_status {
+    GCVT_OK = 0,
+    GCVT_ERR_ARGUMENT = 1, /* null pointer or invalid enum value              */
+    GCVT_ERR_SIZE = 2,     /* grid size outside the supported set             */
+    GCVT_ERR_CUDA = 3,     /* a CUDA runtime call failed                      */
+    GCVT_ERR_INPUT = 4,    /* a site pixel does not hold its own coordinates  */
+    GCVT_ERR_STATE = 5,    /* call order: no problem loaded                   */
+    GCVT_ERR_ALLOC = 6     /* device or host allocation failed                */
+};
+
+enum gcvt_mem { GCVT_MEM_HOST = 0, GCVT_MEM_DEVICE = 1 };
+
+typedef struct gcvt_ctx gcvt_ctx;
+
+typedef struct {
+    int iterations;        /* Lloyd iterations run so far (gcvtIterations)    */
+    int levels;            /* resolution levels run by the last gcvt_ctx_run  */
+    float omega;           /* current over-relaxation factor (pbaOmega)       */
+    double energy;         /* CVT energy of the most recent iteration         */
+    double sampled_energy; /* energy sampled by the schedule (iter % 10 == 0) */
+} gcvt_run_info;
+
+/* Human-readable text of a status code. */
+const char *gcvt_status_string(int status);
+
+/* Library version as 10000*major + 100*minor + patch. */
+int gcvt_version(void);
+
+/* ---- context API ------------------------------------------------------- */
+
+/* Create a context on the current CUDA device for grids up to n_max (a
+ * multiple of 256 in [256, 8192]).  Device buffers live in the context;
+ * nothing is allocated per call afterwards.  Replaces the per-call
+ * allocation of gcvtInitialization (gcvt.cu:840-875). */
+int gcvt_ctx_create(int n_max, gcvt_ctx **out);
+
+/* Free the context and its device buffers (pbaCVDDeinitialization,
+ * gcvt.cu:878-903). */
+int gcvt_ctx_destroy(gcvt_ctx *ctx);
+
+/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the
+ * context's own stream. */
+int gcvt_ctx_set_stream(gcvt_ctx *ctx, void *stream);
+
+/* Load a problem of size n: site grid (2*n*n int16), density (n*n float),
+ * mask (n*n bytes, may be NULL for "no fixed sites").  Replaces
+ * pba2DInitializeInput + the site upload (gcvt.cu:906-914, 1102).  The grid is
+ * checked where it is used: calls that work at full resolution return
+ * GCVT_ERR_INPUT when a non-MARKER pixel does not hold its own (x, y), and
+ * gcvt_ctx_run checks the coarse grid that depth > 1 reads from the first
+ * (n >> (depth-1))^2 entries (gcvt.cu:1099-1103). */
+int gcvt_ctx_load(gcvt_ctx *ctx, int n, const int16_t *voronoi, const float *density,
+                  const uint8_t *mask, int mem);
+
+/* Label every pixel with its nearest current site (2*n*n int16), bit-
+ * identical to pba2DCompute (gcvt.cu:967-978). */
+int gcvt_ctx_label(gcvt_ctx *ctx, int16_t *labels, int mem);
+
+/* Run `iterations` plain Lloyd iterations (label, centroid, update;
+ * gcvt.cu:1114-1123) with the reference's omega schedule and no stop rule. */
+int gcvt_ctx_iterate(gcvt_ctx *ctx, int iterations);
+
+/* Full gCVT schedule from the loaded site grid (restarting from it, with a
+ * fresh schedule): `depth` pyramid levels, the energy stop rule and the
+ * maxIter cap (gcvt.cu:1087-1147).  Follow with gcvt_ctx_label for the final
+ * label grid (gcvt.cu:1149-1152).  The loaded size must be a power of two. */
+int gcvt_ctx_run(gcvt_ctx *ctx, int depth, int max_iter, gcvt_run_info *info);
+
+/* Current site grid (2*n*n int16; sites hold their coordinates, MARKER
+ * elsewhere) -- the state kernelUpdateSites leaves (gcvt.cu:1030-1033). */
+int gcvt_ctx_sites(gcvt_ctx *ctx, int16_t *voronoi, int mem);
+
+/* Per-site moments of the current sites without moving them: four n*n
+ * double planes W, X, Y, E (density sum, x- and y-weighted sums, energy sum
+ * rho*|site-p|^2) at each site pixel, 0 elsewhere.  The reference keeps the
+ * same sums in pbaTotalW/X/Y after kernelScan_Y (gcvt.cu:1008-1023). */
+int gcvt_ctx_moments(gcvt_ctx *ctx, double *out4, int mem);
+
+/* Run `iterations` plain Lloyd iterations as separate launches and return
+ * the mean duration (ms) of each of the iteration's three kernels -- column
+ * summaries, fused label + moment row pass, site update -- timed with CUDA
+ * events on the context's stream.  The sites advance as in
+ * gcvt_ctx_iterate.  No reference counterpart: the reference times nothing
+ * (gcvt.cu:27 includes a timer header it never uses). */
+int gcvt_ctx_time_kernels(gcvt_ctx *ctx, int iterations, float *ms3);
+
+/* Schedule state (iterations, omega, energies). */
+int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
+
+/* ---- one-call forms ---------------------------------------------------- */
+
+/* gCVT with a status code: host buffers in, label grid out in `voronoi`
+ * (gcvt.cu:1087-1156).  size is a power of two in [256, 8192]. */
+int gcvt_compute(int16_t *voronoi, const float *density, const uint8_t *mask, int size,
+                 int depth, int max_iter);
+
+/* Label a site grid once (pba2DCompute on a given grid). */
+int gcvt_label_grid(const int16_t *sites, int16_t *labels, int n, int mem);
+
+#ifdef __cplusplus
+} /* extern "C" */
+
+/* The reference's entry point, same signature and C++ symbol (gcvt.h:29,
+ * gcvt.cu:1087), so source/main.cpp links against this library unchanged. */
+extern void gCVT(short *Voronoi, float *density_d, bool *mask, int size, int depth,
+                 int maxIter);
+#endif
+
+#endif /* GCVT_GB300_H */

@@ -1,0 +1,224 @@
+"""ctypes binding of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/liboracle.so (the C restatement of gcvt.cu's algorithm)
+and, where present, oracle/_build/librefh.so with the reference's kernels
+from oracle/_ref/*.cubin.  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline / reference legs use this module.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+MARKER = -32768
+P, I = ctypes.c_void_p, ctypes.c_int
+
+FAITHFUL, EXACT = 0, 1
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("levels", ctypes.c_int),
+                ("last_energy", ctypes.c_double), ("omega", ctypes.c_float)]
+
+
+_lib = None
+_refh = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(BUILD, "liboracle.so")
+        if not os.path.exists(path):
+            from build_oracle import build_oracle  # noqa: local build on demand
+            build_oracle()
+        L = ctypes.CDLL(path)
+        for f in ("orc_pba_label", "orc_spec_label", "orc_brute_label"):
+            getattr(L, f).argtypes = [P, P, I]
+            getattr(L, f).restype = I
+        L.orc_gcvt.argtypes = [P, P, P, I, I, I, I, I, I, ctypes.POINTER(OrcStats)]
+        L.orc_gcvt.restype = I
+        L.orc_lloyd_step.argtypes = [P, P, P, I, ctypes.c_float, P, P, P, P]
+        L.orc_lloyd_step.restype = I
+        L.orc_faithful_step.argtypes = [P, P, P, I, ctypes.c_float, P, P, P]
+        L.orc_faithful_step.restype = I
+        L.orc_faithful_energy.argtypes = [P, P, I, I]
+        L.orc_faithful_energy.restype = ctypes.c_float
+        L.orc_rasterize.argtypes = [P, P, I, P, I, P, ctypes.c_double, I, I]
+        L.orc_rasterize.restype = I
+        L.orc_seed_sites.argtypes = [P, P, P, I, I, ctypes.c_longlong]
+        L.orc_seed_sites.restype = I
+        _lib = L
+    return _lib
+
+
+def _chk(rc, name):
+    if rc < 0:
+        raise RuntimeError("%s failed: %d" % (name, rc))
+    return rc
+
+
+def pba_label(sites):
+    n = sites.shape[0]
+    out = np.empty_like(sites)
+    _chk(lib().orc_pba_label(sites.ctypes.data, out.ctypes.data, n), "orc_pba_label")
+    return out
+
+
+def spec_label(sites):
+    n = sites.shape[0]
+    out = np.empty_like(sites)
+    _chk(lib().orc_spec_label(sites.ctypes.data, out.ctypes.data, n), "orc_spec_label")
+    return out
+
+
+def brute_label(sites):
+    n = sites.shape[0]
+    out = np.empty_like(sites)
+    _chk(lib().orc_brute_label(sites.ctypes.data, out.ctypes.data, n), "orc_brute_label")
+    return out
+
+
+def gcvt(voronoi, density, mask, depth=1, max_iter=1000, mode=EXACT, fixed_iters=0, threads=0):
+    """Restated gCVT; returns (labels, stats dict).  voronoi is not modified."""
+    v = np.ascontiguousarray(voronoi).copy()
+    n = v.shape[0]
+    st = OrcStats()
+    _chk(lib().orc_gcvt(v.ctypes.data, np.ascontiguousarray(density, np.float32).ctypes.data,
+                        np.ascontiguousarray(mask, np.uint8).ctypes.data, n, depth, max_iter,
+                        mode, fixed_iters, threads, ctypes.byref(st)), "orc_gcvt")
+    return v, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def lloyd_step(sites, density, mask, omega):
+    """One exact-mode Lloyd step: (labels, moments[3,n,n], energy, new_sites)."""
+    n = sites.shape[0]
+    labels = np.empty_like(sites)
+    mom = np.empty((3, n, n), np.float64)
+    e = ctypes.c_double()
+    out = np.empty_like(sites)
+    _chk(lib().orc_lloyd_step(sites.ctypes.data, density.ctypes.data,
+                              np.ascontiguousarray(mask, np.uint8).ctypes.data, n,
+                              ctypes.c_float(omega), labels.ctypes.data, mom.ctypes.data,
+                              ctypes.byref(e), out.ctypes.data), "orc_lloyd_step")
+    return labels, mom, e.value, out
+
+
+def faithful_step(sites, density, mask, omega):
+    """One faithful Lloyd step: (labels, totals[3,n,n] float32, new_sites)."""
+    n = sites.shape[0]
+    labels = np.empty_like(sites)
+    tot = np.empty((3, n, n), np.float32)
+    out = np.empty_like(sites)
+    _chk(lib().orc_faithful_step(sites.ctypes.data, density.ctypes.data,
+                                 np.ascontiguousarray(mask, np.uint8).ctypes.data, n,
+                                 ctypes.c_float(omega), labels.ctypes.data, tot.ctypes.data,
+                                 out.ctypes.data), "orc_faithful_step")
+    return labels, tot, out
+
+
+def faithful_energy(labels, density, level=0):
+    return float(lib().orc_faithful_energy(labels.ctypes.data, density.ctypes.data,
+                                           labels.shape[0], level))
+
+
+def rasterize(points, weight, triangles, scale, n, threads=0):
+    out = np.empty((n, n), np.float32)
+    _chk(lib().orc_rasterize(points.ctypes.data, weight.ctypes.data, len(weight),
+                             triangles.ctypes.data, len(triangles), out.ctypes.data,
+                             ctypes.c_double(scale), n, threads), "orc_rasterize")
+    return out
+
+
+def seed_sites(density, mask, num, seed=-1):
+    n = density.shape[0]
+    v = np.empty((n, n, 2), np.int16)
+    _chk(lib().orc_seed_sites(v.ctypes.data, density.ctypes.data,
+                              np.ascontiguousarray(mask, np.uint8).ctypes.data, num, n, seed),
+         "orc_seed_sites")
+    return v
+
+
+# ---- the reference's own kernels -------------------------------------------
+
+def ref_available():
+    return (os.path.exists(os.path.join(REF, "gcvt_ref.cubin")) and
+            os.path.exists(os.path.join(BUILD, "librefh.so")))
+
+
+def refh():
+    """The reference-kernel harness; needs a GPU and the cubins."""
+    global _refh
+    if _refh is None:
+        path = os.path.join(BUILD, "librefh.so")
+        if not os.path.exists(path):
+            from build_oracle import build_harness
+            build_harness()
+        R = ctypes.CDLL(path)
+        R.refh_init.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        R.refh_pba_label.argtypes = [P, P, I]
+        R.refh_energy.argtypes = [P, P, I, ctypes.POINTER(ctypes.c_float)]
+        R.refh_lloyd_step.argtypes = [P, P, P, I, ctypes.c_float, P, P, P]
+        R.refh_gcvt.argtypes = [P, P, P, I, I, I, I, P, I, P, P]
+        R.refh_rasterize.argtypes = [P, P, I, P, I, P, ctypes.c_double, I, P]
+        raster = os.path.join(REF, "raster_ref.cubin")
+        rc = R.refh_init(os.path.join(REF, "gcvt_ref.cubin").encode(),
+                         raster.encode() if os.path.exists(raster) else None)
+        if rc != 0:
+            raise RuntimeError("refh_init failed: %d" % rc)
+        _refh = R
+    return _refh
+
+
+def ref_pba_label(sites):
+    n = sites.shape[0]
+    out = np.empty_like(sites)
+    _chk(refh().refh_pba_label(sites.ctypes.data, out.ctypes.data, n), "refh_pba_label")
+    return out
+
+
+def ref_energy(labels, density):
+    e = ctypes.c_float()
+    _chk(refh().refh_energy(labels.ctypes.data, density.ctypes.data, labels.shape[0],
+                            ctypes.byref(e)), "refh_energy")
+    return e.value
+
+
+def ref_lloyd_step(sites, density, mask, omega):
+    n = sites.shape[0]
+    labels = np.empty_like(sites)
+    tot = np.empty((3, n, n), np.float32)
+    out = np.empty_like(sites)
+    _chk(refh().refh_lloyd_step(sites.ctypes.data, density.ctypes.data,
+                                np.ascontiguousarray(mask, np.uint8).ctypes.data, n,
+                                ctypes.c_float(omega), labels.ctypes.data, tot.ctypes.data,
+                                out.ctypes.data), "refh_lloyd_step")
+    return labels, tot, out
+
+
+def ref_gcvt(voronoi, density, mask, depth=1, max_iter=1000, fixed_iters=0):
+    """The reference's kernels under gCVT's loop; returns (labels, info)."""
+    v = np.ascontiguousarray(voronoi).copy()
+    n = v.shape[0]
+    energies = np.zeros(4096, np.float32)
+    stats = np.zeros(2, np.int32)
+    times = np.zeros(2, np.float32)
+    _chk(refh().refh_gcvt(v.ctypes.data, np.ascontiguousarray(density, np.float32).ctypes.data,
+                          np.ascontiguousarray(mask, np.uint8).ctypes.data, n, depth, max_iter,
+                          fixed_iters, energies.ctypes.data, len(energies), stats.ctypes.data,
+                          times.ctypes.data), "refh_gcvt")
+    ne = int(stats[1])
+    return v, {"iterations": int(stats[0]), "energies": energies[:min(ne, 4096)].tolist(),
+               "total_ms": float(times[0]), "loop_ms": float(times[1])}
+
+
+def ref_rasterize(points, weight, triangles, scale, n):
+    out = np.empty((n, n), np.float32)
+    t = ctypes.c_float()
+    _chk(refh().refh_rasterize(points.ctypes.data, weight.ctypes.data, len(weight),
+                               triangles.ctypes.data, len(triangles), out.ctypes.data,
+                               ctypes.c_double(scale), n, ctypes.byref(t)), "refh_rasterize")
+    return out, t.value

@@ -1,0 +1,230 @@
+"""ctypes binding of libgcvt_gb300.so (include/gcvt_gb300.h).
+
+The Python mirror of the reference's CVT interface (source/gcvt.h):
+  * ``gcvt(voronoi, density, mask, depth, max_iter)`` -- gCVT (gcvt.h:29):
+    site grid in, label grid out, in place on ``voronoi``;
+  * ``label_grid(sites)`` -- one exact labelling pass (pba2DCompute);
+  * ``Context`` -- the context API: load once, label / iterate / run / read
+    back, with host (numpy) or device (objects exposing ``data_ptr()``, e.g.
+    torch CUDA tensors) buffers.
+
+Grids follow the reference: a site/label grid is an int16 array of shape
+(n, n, 2) holding (x, y) per pixel, MARKER = -32768 where there is no site.
+There is no fallback: every call runs the CUDA library, and loading fails
+loudly when the library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+MARKER = -32768
+MEM_HOST, MEM_DEVICE = 0, 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libgcvt_gb300.so"))
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported grid size", 3: "CUDA runtime error",
+          4: "site grid pixel does not hold its own coordinates", 5: "no problem loaded",
+          6: "allocation failed"}
+
+
+class GcvtError(RuntimeError):
+    def __init__(self, code, where):
+        super().__init__("%s: %s (status %d)" % (where, STATUS.get(code, "unknown"), code))
+        self.code = code
+
+
+class RunInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("levels", ctypes.c_int),
+                ("omega", ctypes.c_float), ("energy", ctypes.c_double),
+                ("sampled_energy", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# Every symbol the header declares, with its ctypes signature.
+P, I = ctypes.c_void_p, ctypes.c_int
+SIGNATURES = {
+    "gcvt_status_string": ([I], ctypes.c_char_p),
+    "gcvt_version": ([], I),
+    "gcvt_ctx_create": ([I, ctypes.POINTER(P)], I),
+    "gcvt_ctx_destroy": ([P], I),
+    "gcvt_ctx_set_stream": ([P, P], I),
+    "gcvt_ctx_load": ([P, I, P, P, P, I], I),
+    "gcvt_ctx_label": ([P, P, I], I),
+    "gcvt_ctx_iterate": ([P, I], I),
+    "gcvt_ctx_run": ([P, I, I, ctypes.POINTER(RunInfo)], I),
+    "gcvt_ctx_sites": ([P, P, I], I),
+    "gcvt_ctx_moments": ([P, P, I], I),
+    "gcvt_ctx_info": ([P, ctypes.POINTER(RunInfo)], I),
+    "gcvt_ctx_time_kernels": ([P, I, P], I),
+    "gcvt_compute": ([P, P, P, I, I, I], I),
+    "gcvt_label_grid": ([P, P, I, I], I),
+}
+CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii"}
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libgcvt_gb300.so (raises OSError when it is not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    lib = ctypes.CDLL(path or LIB_PATH)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(code, where):
+    if code != 0:
+        raise GcvtError(code, where)
+
+
+def _host_ptr(a, dtype, shape=None):
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous %s numpy array" % np.dtype(dtype))
+    if shape is not None and a.shape != shape:
+        raise ValueError("expected shape %s, got %s" % (shape, a.shape))
+    return a.ctypes.data
+
+
+def _ptr_mem(a, dtype, shape):
+    """(address, GCVT_MEM_*) of a numpy array or a torch tensor (CUDA tensors
+    are device memory, CPU tensors -- e.g. pinned ones -- host memory)."""
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr(), (MEM_DEVICE if getattr(a, "is_cuda", False) else MEM_HOST)
+    return _host_ptr(a, dtype, shape), MEM_HOST
+
+
+class Context:
+    """A device context for grids up to n_max (gcvt_ctx_*)."""
+
+    def __init__(self, n_max):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib.gcvt_ctx_create(int(n_max), ctypes.byref(h)), "gcvt_ctx_create")
+        self.h = h
+        self.n_max = int(n_max)
+        self.n = None
+
+    def close(self):
+        if self.h:
+            self.lib.gcvt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        _check(self.lib.gcvt_ctx_set_stream(self.h, stream_handle), "gcvt_ctx_set_stream")
+
+    def load(self, sites, density, mask=None):
+        if hasattr(sites, "data_ptr"):
+            n = int(sites.shape[0])
+            mp = mask.data_ptr() if mask is not None else None
+            mem = MEM_DEVICE if getattr(sites, "is_cuda", False) else MEM_HOST
+            _check(self.lib.gcvt_ctx_load(self.h, n, sites.data_ptr(), density.data_ptr(), mp,
+                                          mem), "gcvt_ctx_load")
+        else:
+            n = int(sites.shape[0])
+            sp = _host_ptr(sites, np.int16, (n, n, 2))
+            dp = _host_ptr(density, np.float32, (n, n))
+            mp = _host_ptr(mask, np.uint8, (n, n)) if mask is not None else None
+            _check(self.lib.gcvt_ctx_load(self.h, n, sp, dp, mp, MEM_HOST), "gcvt_ctx_load")
+        self.n = n
+
+    def label(self, out=None):
+        n = self.n
+        if out is None:
+            out = np.empty((n, n, 2), np.int16)
+        p, mem = _ptr_mem(out, np.int16, (n, n, 2))
+        _check(self.lib.gcvt_ctx_label(self.h, p, mem), "gcvt_ctx_label")
+        return out
+
+    def iterate(self, iterations):
+        _check(self.lib.gcvt_ctx_iterate(self.h, int(iterations)), "gcvt_ctx_iterate")
+
+    def run(self, depth=1, max_iter=1000):
+        info = RunInfo()
+        _check(self.lib.gcvt_ctx_run(self.h, int(depth), int(max_iter), ctypes.byref(info)),
+               "gcvt_ctx_run")
+        return info.as_dict()
+
+    def sites(self, out=None):
+        n = self.n
+        if out is None:
+            out = np.empty((n, n, 2), np.int16)
+        p, mem = _ptr_mem(out, np.int16, (n, n, 2))
+        _check(self.lib.gcvt_ctx_sites(self.h, p, mem), "gcvt_ctx_sites")
+        return out
+
+    def moments(self):
+        """(W, X, Y, E) planes of shape (n, n) at the current site pixels."""
+        n = self.n
+        out = np.empty((4, n, n), np.float64)
+        _check(self.lib.gcvt_ctx_moments(self.h, out.ctypes.data, MEM_HOST), "gcvt_ctx_moments")
+        return out
+
+    def time_kernels(self, iterations):
+        """Mean ms of (summary, row pass, update) over `iterations` iterations."""
+        ms = (ctypes.c_float * 3)()
+        _check(self.lib.gcvt_ctx_time_kernels(self.h, int(iterations), ms), "gcvt_ctx_time_kernels")
+        return list(ms)
+
+    def info(self):
+        info = RunInfo()
+        _check(self.lib.gcvt_ctx_info(self.h, ctypes.byref(info)), "gcvt_ctx_info")
+        return info.as_dict()
+
+
+def gcvt(voronoi, density, mask, depth=1, max_iter=1000):
+    """gCVT: runs the Lloyd loop from the site grid ``voronoi`` and overwrites
+    it with the final label grid (gcvt.cu:1087-1156)."""
+    lib = load_library()
+    n = int(voronoi.shape[0])
+    _check(lib.gcvt_compute(_host_ptr(voronoi, np.int16, (n, n, 2)),
+                            _host_ptr(density, np.float32, (n, n)),
+                            _host_ptr(mask, np.uint8, (n, n)), n, int(depth), int(max_iter)),
+           "gcvt_compute")
+    return voronoi
+
+
+def label_grid(sites):
+    """Labels of a site grid (one exact pass, bit-identical to pba2DCompute)."""
+    lib = load_library()
+    n = int(sites.shape[0])
+    if hasattr(sites, "data_ptr"):
+        import torch  # device path: output on the same device
+        out = torch.empty_like(sites)
+        _check(lib.gcvt_label_grid(sites.data_ptr(), out.data_ptr(), n, MEM_DEVICE),
+               "gcvt_label_grid")
+        return out
+    out = np.empty_like(sites)
+    _check(lib.gcvt_label_grid(_host_ptr(sites, np.int16, (n, n, 2)), out.ctypes.data, n,
+                               MEM_HOST), "gcvt_label_grid")
+    return out
+
+
+def sites_from_points(n, xs, ys):
+    """Site grid with a site at each (x, y)."""
+    g = np.full((n, n, 2), MARKER, np.int16)
+    g[ys, xs, 0] = xs
+    g[ys, xs, 1] = ys
+    return g

@@ -1,0 +1,126 @@
+"""GPU Lloyd parity against the FP64 oracle (exact mode).
+
+Contract (per iteration, same sites in): labels bit-exact; per-site moments
+W, X, Y and the energy within 1e-5 relative of FP64 (compensated FP32 with
+FP64 only in the final division); the integer site update identical except
+for sites whose FP64 pre-rounding coordinate lies within 1e-6 of a rounding
+boundary.  Trajectories are then compared over many iterations."""
+import numpy as np
+import pytest
+
+from workloads import MARKER, config_inputs, small_case
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def site_list(g):
+    ys, xs = np.nonzero(g[..., 0] != MARKER)
+    return set(zip(xs.tolist(), ys.tolist()))
+
+
+@pytest.mark.parametrize("case", [(256, 300, 1), (512, 2000, 2), (1024, 4096, 3)])
+def test_moments_match_fp64(gcvt_lib, oracle, cuda_device, case):
+    n, m, seed = case
+    sites, rho, mask = small_case(n, m, seed)
+    labels, mom, energy, _ = oracle.lloyd_step(sites, rho, mask, 2.0)
+    ctx = gcvt_lib.Context(n)
+    ctx.load(sites, rho, mask)
+    assert np.array_equal(ctx.label(), labels)
+    got = ctx.moments()
+    ys, xs = np.nonzero(sites[..., 0] != MARKER)
+    for k in range(3):
+        want = mom[k][ys, xs]
+        have = got[k][ys, xs]
+        err = np.abs(have - want) / np.maximum(np.abs(want), 1e-30)
+        assert err.max() < REL, (k, err.max())
+    e_gpu = got[3][ys, xs].sum() / (n * n)
+    assert abs(e_gpu - energy) / energy < REL
+    ctx.close()
+
+
+def _boundary_distance(mom, xs, ys, omega):
+    W = mom[0][ys, xs]
+    out = []
+    for plane, base in ((mom[1][ys, xs], xs), (mom[2][ys, xs], ys)):
+        c = (plane / W).astype(np.float32)
+        f = np.float32(base) + (c - np.float32(base)) * np.float32(omega) + np.float32(0.5)
+        out.append(np.abs(f - np.round(f)) if False else np.abs(f - np.floor(f)))
+    return np.minimum(np.minimum(out[0], 1 - out[0]), np.minimum(out[1], 1 - out[1]))
+
+
+@pytest.mark.parametrize("omega_case", [(256, 400, 5), (1024, 4096, 6)])
+def test_one_update_matches_oracle(gcvt_lib, oracle, cuda_device, omega_case):
+    n, m, seed = omega_case
+    sites, rho, mask = small_case(n, m, seed)
+    _, mom, _, want = oracle.lloyd_step(sites, rho, mask, 2.0)
+    ctx = gcvt_lib.Context(n)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(1)
+    got = ctx.sites()
+    a, b = site_list(got), site_list(want)
+    diff = a ^ b
+    if diff:
+        ys, xs = np.nonzero(sites[..., 0] != MARKER)
+        d = _boundary_distance(mom, xs, ys, 2.0)
+        assert len(diff) <= 4 and d.min() < 1e-4, (len(diff), d.min())
+    ctx.close()
+
+
+def test_trajectory_matches_oracle(gcvt_lib, oracle, cuda_device):
+    sites, rho, mask = small_case(512, 1500, seed=9)
+    iters = 40
+    want, st = oracle.gcvt(sites, rho, mask, 1, iters, mode=oracle.EXACT, fixed_iters=iters)
+    ctx = gcvt_lib.Context(512)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(iters)
+    got = ctx.label()
+    info = ctx.info()
+    assert info["iterations"] == iters
+    same = (got == want).all(-1).mean()
+    assert same > 0.999, same
+    ctx.close()
+
+
+def test_gcvt_schedule_matches_oracle(gcvt_lib, oracle, cuda_device):
+    sites, rho, mask = small_case(256, 300, seed=12)
+    want, st = oracle.gcvt(sites, rho, mask, 1, 1000, mode=oracle.EXACT)
+    got = gcvt_lib.gcvt(sites.copy(), rho, mask, 1, 1000)
+    ctx = gcvt_lib.Context(256)
+    ctx.load(sites, rho, mask)
+    info = ctx.run(1, 1000)
+    assert info["iterations"] == st["iterations"]
+    assert abs(info["omega"] - st["omega"]) < 1e-6
+    assert (got == want).all(-1).mean() > 0.999
+    ctx.close()
+
+
+def test_fixed_sites_stay(gcvt_lib, cuda_device):
+    sites, rho, mask = small_case(256, 200, seed=13)
+    mask = np.zeros_like(mask)
+    ys, xs = np.nonzero(sites[..., 0] != MARKER)
+    mask[ys[:20], xs[:20]] = 1
+    ctx = gcvt_lib.Context(256)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(25)
+    out = ctx.sites()
+    for x, y in zip(xs[:20], ys[:20]):
+        assert tuple(out[y, x]) == (x, y)
+    ctx.close()
+
+
+def test_multilevel_depth2_matches_oracle(gcvt_lib, oracle, cuda_device):
+    sites, rho, mask = small_case(512, 800, seed=14)
+    # depth 2: the first 256*256 entries of the array are the coarse grid
+    coarse = np.full((512, 512, 2), MARKER, np.int16)
+    c_sites, _, _ = small_case(256, 200, seed=15)
+    coarse.reshape(-1, 2)[: 256 * 256] = c_sites.reshape(-1, 2)
+    want, st = oracle.gcvt(coarse, rho, mask, 2, 60, mode=oracle.EXACT)
+    ctx = gcvt_lib.Context(512)
+    ctx.load(coarse, rho, mask)
+    info = ctx.run(2, 60)
+    got = ctx.label()
+    assert info["iterations"] == st["iterations"]
+    assert (got == want).all(-1).mean() > 0.99
+    ctx.close()
