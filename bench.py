@@ -281,7 +281,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(h_sites.numel() * 2 + h_rho.numel() * 4 + h_mask.numel()),
                 "d2h_bytes_per_step": int(h_out.numel() * 2),
                 "ms_per_step": t_e2e / args.steps * 1e3},
-        "gpu_launches": args.steps * (1 + 3 * ITERS + 2),
+        "gpu_launches": args.steps * (3 + 4 * ITERS + 3),
         "clocks": clk.summary(),
         "final_energy": info["energy"],
     }
@@ -313,6 +313,22 @@ def reference_gpu(sites, rho, mask):
                     "excludes its per-call allocation and copies, total_ms includes them"}
 
 
+def run_profile_case(iterations):
+    """The bench workload for ncu captures: load once, then `iterations` Lloyd
+    iterations as plain (non-graph) launches."""
+    import torch
+    import gcvt_gb300 as G
+    from workloads import config_inputs
+    sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    ctx = G.Context(sites.shape[0])
+    ctx.load(sites, rho, mask)
+    ms = ctx.time_kernels(iterations)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": CONFIG, "iterations": iterations, "kernel_ms": ms}))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,7 +338,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-gpu", action="store_true",
                     help="also time the reference's own kernels on this GPU")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="ITERS",
+                    help="only run ITERS Lloyd iterations of the workload (for ncu)")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -34,10 +34,13 @@ struct gcvt_ctx {
   uint32_t *grid = nullptr;   // staging: labels and site dumps
   uint64_t *bits[2] = {};
   int16_t *prev = nullptr, *next = nullptr;
+  uint64_t *fixed_bits[8] = {};   // per level
+  int *word_rank = nullptr, *group_count = nullptr, *group_offset = nullptr;
   float4 *mhi = nullptr, *mlo = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned mirror
-  double *blk_energy = nullptr;
+  float *blk_energy = nullptr;    // 2 floats per update block
+  int2 *support[8] = {};          // per level: row support of the density
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
   int *err = nullptr;
   int last_levels = 0;
@@ -69,11 +72,16 @@ LevelBufs level_bufs(gcvt_ctx *c, int n, int level) {
   b.next = c->next;
   b.density = c->density[level];
   b.fixed = c->mask;
+  b.fixed_bits = c->fixed_bits[level];
+  b.word_rank = c->word_rank;
+  b.group_count = c->group_count;
+  b.group_offset = c->group_offset;
   b.mhi = c->mhi;
   b.mlo = c->mlo;
   b.labels = c->grid;
   b.st = c->st;
   b.blk_energy = c->blk_energy;
+  b.support = c->support[level];
   return b;
 }
 
@@ -251,11 +259,18 @@ int gcvt_ctx_create(int n_max, gcvt_ctx **out) {
   ok = ok && dal((void **)&c->bits[0], words * sizeof(uint64_t));
   ok = ok && dal((void **)&c->bits[1], words * sizeof(uint64_t));
   ok = ok && dal((void **)&c->prev, words * sizeof(int16_t));
+  ok = ok && dal((void **)&c->word_rank, words * sizeof(int));
+  ok = ok && dal((void **)&c->group_count, (size_t)(n_max / 32) * sizeof(int));
+  ok = ok && dal((void **)&c->group_offset, (size_t)(n_max / 32) * sizeof(int));
+  for (int l = 0; l < c->dens_levels && ok; ++l)
+    ok &= dal((void **)&c->fixed_bits[l], (size_t)((n_max >> l) / kBand) * (n_max >> l) * sizeof(uint64_t));
   ok = ok && dal((void **)&c->next, words * sizeof(int16_t));
   ok = ok && dal((void **)&c->mhi, nn * sizeof(float4));
   ok = ok && dal((void **)&c->mlo, nn * sizeof(float4));
   ok = ok && dal((void **)&c->st, sizeof(DevState));
-  ok = ok && dal((void **)&c->blk_energy, (size_t)update_blocks(n_max) * sizeof(double));
+  ok = ok && dal((void **)&c->blk_energy, (size_t)update_blocks(n_max) * 2 * sizeof(float));
+  for (int l = 0; l < c->dens_levels && ok; ++l)
+    ok &= dal((void **)&c->support[l], (size_t)(n_max >> l) * sizeof(int2));
   ok = ok && dal((void **)&c->err, sizeof(int));
   if (!ok) return fail(GCVT_ERR_ALLOC);
   if (cudaMallocHost((void **)&c->st_host, sizeof(DevState)) != cudaSuccess)
@@ -282,11 +297,16 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->bits[0]);
   cudaFree(c->bits[1]);
   cudaFree(c->prev);
+  cudaFree(c->word_rank);
+  cudaFree(c->group_count);
+  cudaFree(c->group_offset);
+  for (int l = 0; l < 8; ++l) cudaFree(c->fixed_bits[l]);
   cudaFree(c->next);
   cudaFree(c->mhi);
   cudaFree(c->mlo);
   cudaFree(c->st);
   cudaFree(c->blk_energy);
+  for (int l = 0; l < 8; ++l) cudaFree(c->support[l]);
   cudaFree(c->moments);
   cudaFree(c->err);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -338,11 +358,13 @@ int gcvt_ctx_load(gcvt_ctx *c, int n, const int16_t *voronoi, const float *densi
   int rc;
   c->loaded = 0;
   if ((rc = copy_in(c->density[0], density, nn * sizeof(float), mem, c->stream))) return rc;
+  CK(launch_row_support(c->density[0], n, c->support[0], c->stream));
   if (mask) {
     if ((rc = copy_in(c->mask, mask, nn, mem, c->stream))) return rc;
   } else {
     CK(cudaMemsetAsync(c->mask, 0, nn, c->stream));
   }
+  CK(launch_fixed_bits(c->mask, n, c->fixed_bits[0], c->stream));
   return load_sites(c, n, voronoi, mem);
 }
 
@@ -376,8 +398,11 @@ int gcvt_ctx_run(gcvt_ctx *c, int depth, int max_iter, gcvt_run_info *info) {
     if ((size >> i) < 256) { depth = i; break; }
   int rc;
   // density pyramid (gcvt.cu:985-993)
-  for (int l = 1; l < depth; ++l)
+  for (int l = 1; l < depth; ++l) {
     CK(launch_density_halve(c->density[l - 1], c->density[l], size >> l, c->stream));
+    CK(launch_row_support(c->density[l], size >> l, c->support[l], c->stream));
+    CK(launch_fixed_bits(c->mask, size >> l, c->fixed_bits[l], c->stream));
+  }
   // the coarsest grid is the first (size >> (depth-1))^2 entries of the loaded
   // array (gcvt.cu:1099-1103)
   const int n0 = size >> (depth - 1);

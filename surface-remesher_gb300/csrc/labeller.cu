@@ -84,53 +84,115 @@ cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cud
 }
 
 // ---------------------------------------------------------------------------
-// Column summaries: prev[b][x] = last site row in bands < b, next[b][x] =
-// first site row in bands > b (kNoneAbove / kNoneBelow when there is none).
-// Block = 32 columns x 32 band groups; each thread owns ceil(nb/32) bands.
+// Column summaries and site slots, one block per 32-column group (32 columns x
+// 32 band groups; each thread owns ceil(nb/32) consecutive bands):
+//   prev[b][x] = last site row in bands < b, next[b][x] = first site row in
+//   bands > b (kNoneAbove / kNoneBelow when there is none);
+//   word_rank[b][x] = sites of the group in earlier words (band-major, then
+//   column), group_count[g] = sites of the group.  A second one-block kernel
+//   turns group_count into group_offset, which completes the site slots used
+//   by the moment accumulators (see site_slot).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_summary(LevelBufs a, int respect_stop) {
   if (respect_stop && a.st->stopped) return;
   __shared__ int sLast[32][33];
   __shared__ int sFirst[32][33];
+  __shared__ int sCnt[32];    // sites in each warp's bands (all 32 columns)
   const int n = a.n, nb = n / kBand;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = blockIdx.x * 32 + tx;
   const uint64_t *bits = (a.st->parity ? a.bits[1] : a.bits[0]);
   const int G = (nb + 31) / 32;
-  const int b0 = ty * G, b1 = min(nb, b0 + G);
-  int myLast = kNoneAbove, myFirst = kNoneBelow;
-  if (x < n) {
-    for (int b = b0; b < b1; ++b) {
-      uint64_t w = bits[(size_t)b * n + x];
-      if (w) {
-        if (myFirst == kNoneBelow) myFirst = b * kBand + __ffsll((long long)w) - 1;
-        myLast = b * kBand + 63 - __clzll((long long)w);
-      }
+  const int b0 = min(nb, ty * G), b1 = min(nb, b0 + G);
+  int myLast = kNoneAbove, myFirst = kNoneBelow, myCnt = 0;
+  for (int b = b0; b < b1; ++b) {
+    uint64_t w = bits[(size_t)b * n + x];
+    if (w) {
+      if (myFirst == kNoneBelow) myFirst = b * kBand + __ffsll((long long)w) - 1;
+      myLast = b * kBand + 63 - __clzll((long long)w);
+      myCnt += __popcll(w);
     }
   }
   sLast[ty][tx] = myLast;
   sFirst[ty][tx] = myFirst;
+  int wsum = myCnt;
+  for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+  if (tx == 0) sCnt[ty] = wsum;
   __syncthreads();
-  if (x >= n || b0 >= nb) return;
   int pv = kNoneAbove;
   for (int k = 0; k < ty; ++k) pv = max(pv, sLast[k][tx]);
   int nx = kNoneBelow;
   for (int k = ty + 1; k < 32; ++k) nx = min(nx, sFirst[k][tx]);
+  int rank = 0;  // sites of the group in bands before b0
+  for (int k = 0; k < ty; ++k) rank += sCnt[k];
   for (int b = b0; b < b1; ++b) {
-    a.prev[(size_t)b * n + x] = (int16_t)pv;
-    uint64_t w = bits[(size_t)b * n + x];
+    const size_t wi = (size_t)b * n + x;
+    a.prev[wi] = (int16_t)pv;
+    const uint64_t w = bits[wi];
     if (w) pv = b * kBand + 63 - __clzll((long long)w);
+    // rank of this word: earlier bands + earlier columns of this band
+    const int c = __popcll(w);
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tx >= o) incl += t;
+    }
+    a.word_rank[wi] = rank + incl - c;
+    rank += __shfl_sync(0xffffffffu, incl, 31);
   }
   for (int b = b1 - 1; b >= b0; --b) {
     a.next[(size_t)b * n + x] = (int16_t)nx;
     uint64_t w = bits[(size_t)b * n + x];
     if (w) nx = b * kBand + __ffsll((long long)w) - 1;
   }
+  if (tx == 0 && ty == 31) {
+    int tot = 0;
+    for (int k = 0; k < 32; ++k) tot += sCnt[k];
+    a.group_count[blockIdx.x] = tot;
+  }
+}
+
+// Exclusive scan of the per-group site counts (n/32 <= 256 groups).
+__global__ void __launch_bounds__(256) k_group_offsets(LevelBufs a, int respect_stop) {
+  if (respect_stop && a.st->stopped) return;
+  __shared__ int s[256];
+  const int ng = a.n / 32, t = threadIdx.x;
+  int v = t < ng ? a.group_count[t] : 0;
+  s[t] = v;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    int add = t >= o ? s[t - o] : 0;
+    __syncthreads();
+    s[t] += add;
+    __syncthreads();
+  }
+  if (t < ng) a.group_offset[t] = s[t] - v;
 }
 
 cudaError_t launch_summary(const LevelBufs &b, int respect_stop, cudaStream_t s) {
-  dim3 blk(32, 32), grd((b.n + 31) / 32);
+  dim3 blk(32, 32), grd(b.n / 32);
   k_summary<<<grd, blk, 0, s>>>(b, respect_stop);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_group_offsets<<<1, 256, 0, s>>>(b, respect_stop);
+  return cudaGetLastError();
+}
+
+// Fixed-site bitmap of a level from the mask.  The reference indexes the full-
+// resolution mask with the level's own pitch (gcvt.cu:777); so does this.
+__global__ void k_fixed_bits(const uint8_t *__restrict__ mask, int n, uint64_t *fb) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int b = blockIdx.y;
+  if (x >= n) return;
+  uint64_t w = 0;
+  for (int i = 0; i < kBand; ++i)
+    if (mask[(size_t)(b * kBand + i) * n + x]) w |= 1ull << i;
+  fb[(size_t)b * n + x] = w;
+}
+
+cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, cudaStream_t s) {
+  dim3 blk(128), grd((n + 127) / 128, n / kBand);
+  k_fixed_bits<<<grd, blk, 0, s>>>(mask, n, fixed_bits);
   return cudaGetLastError();
 }
 
@@ -145,20 +207,28 @@ __device__ __forceinline__ int ent_B(int e) {
   int x = ent_x(e), g = ent_g(e);
   return x * x + g * g;
 }
+__device__ __forceinline__ int pack_ent(int x, int g) { return (x << 16) | (g & 0xffff); }
+constexpr int kNoEnt = -1;  // x = 0xffff never occurs (n <= 8192)
 
-// 1 if pixel p lies at or after the first pixel that entry e2 (successor of
-// e1 on the envelope) owns: e2 starts at floor((B2-B1) / (2(x2-x1))) + 1,
-// ties at an integer breakpoint staying with the smaller column.
-__device__ __forceinline__ bool past_start(int e1, int e2, int p) {
-  int num = ent_B(e2) - ent_B(e1);
-  int den = 2 * (ent_x(e2) - ent_x(e1));
-  return num < p * den;
+// 1 when b lies strictly below the segment a-c on the points (x, B), i.e. b
+// survives a chord test.  Exact in 64-bit integers.
+__device__ __forceinline__ bool below_chord(int a, int b, int c) {
+  const int ax = ent_x(a), bx = ent_x(b), cx = ent_x(c);
+  const int aB = ent_B(a), bB = ent_B(b), cB = ent_B(c);
+  return (long long)(bx - ax) * (long long)(cB - aB) - (long long)(bB - aB) * (long long)(cx - ax) > 0;
 }
 
-// Orientation of (o, a, b) on points (x, B); > 0 when a lies strictly below
-// the segment o-b, i.e. a stays on the lower hull.
-__device__ __forceinline__ long long hull_cross(int ox, int oB, int ax, int aB, int bx, int bB) {
-  return (long long)(ax - ox) * (long long)(bB - oB) - (long long)(aB - oB) * (long long)(bx - ox);
+// First pixel owned by entry e2 when e1 precedes it on the envelope:
+// floor((B2 - B1) / (2 (x2 - x1))) + 1; an integer tie stays with e1 (the
+// smaller column), as kernelColor's '>' break does (gcvt.cu:457).
+__device__ __forceinline__ int start_pixel(int e1, int e2) {
+  const int num = ent_B(e2) - ent_B(e1);
+  const int den = 2 * (ent_x(e2) - ent_x(e1));
+  int q = (int)floorf(__fdividef((float)num, (float)den));
+  // exact fix-up: q = floor(num / den)
+  while (q * den > num) --q;
+  while ((q + 1) * den <= num) ++q;
+  return q + 1;
 }
 
 // Column candidate: the vertically nearest site row of one column for row r,
@@ -174,281 +244,245 @@ __device__ __forceinline__ int column_candidate(uint64_t w, int pv, int nx, uint
   return da < db ? a : (db < da ? b : (be ? b : a));
 }
 
-struct RowSmem {
-  int *base;  // 32 lanes x SP stack slots, then lo[32], hi[32]
-  int SP;
-  __device__ __forceinline__ int *stk(int lane) const { return base + lane * SP; }
-  __device__ __forceinline__ int *lo() const { return base + 32 * SP; }
-  __device__ __forceinline__ int *hi() const { return base + 32 * SP + 32; }
-  __device__ __forceinline__ int at(int lane, int k) const { return base[lane * SP + k]; }
-};
-
-// Join the hulls of lanes [L0, M) and [M, L1) along their lower bridge.  Run
-// by one lane; every loop advances a finger monotonically, so it ends.
-__device__ void bridge_merge(const RowSmem &sm, int L0, int M, int L1) {
-  int *lo = sm.lo(), *hi = sm.hi();
-  int iL = -1, kL = -1;
-  for (int j = M - 1; j >= L0; --j)
-    if (hi[j] > lo[j]) { iL = j; break; }
-  for (int j = M; j < L1; ++j)
-    if (hi[j] > lo[j]) { kL = j; break; }
-  if (iL < 0 || kL < 0) return;
-  int ik = hi[iL] - 1, kk = lo[kL];
-  int I = sm.at(iL, ik), K = sm.at(kL, kk);
-  bool changed = true;
-  while (changed) {
-    changed = false;
-    for (;;) {  // drop left-hull points on or above the line pred(i) -> k
-      int pL = iL, pk = ik - 1;
-      if (pk < lo[pL]) {
-        pL = -1;
-        for (int j = iL - 1; j >= L0; --j)
-          if (hi[j] > lo[j]) { pL = j; pk = hi[j] - 1; break; }
-        if (pL < 0) break;
-      }
-      int P = sm.at(pL, pk);
-      if (hull_cross(ent_x(P), ent_B(P), ent_x(I), ent_B(I), ent_x(K), ent_B(K)) <= 0) {
-        iL = pL; ik = pk; I = P; changed = true;
-      } else {
-        break;
-      }
-    }
-    for (;;) {  // drop right-hull points on or above the line i -> succ(k)
-      int sL = kL, sk = kk + 1;
-      if (sk >= hi[sL]) {
-        sL = -1;
-        for (int j = kL + 1; j < L1; ++j)
-          if (hi[j] > lo[j]) { sL = j; sk = lo[j]; break; }
-        if (sL < 0) break;
-      }
-      int Q = sm.at(sL, sk);
-      if (hull_cross(ent_x(I), ent_B(I), ent_x(K), ent_B(K), ent_x(Q), ent_B(Q)) <= 0) {
-        kL = sL; kk = sk; K = Q; changed = true;
-      } else {
-        break;
-      }
-    }
-  }
-  hi[iL] = ik + 1;
-  for (int j = iL + 1; j < M; ++j) hi[j] = lo[j];
-  lo[kL] = kk;
-  for (int j = M; j < kL; ++j) lo[j] = hi[j];
+// Two-float helpers (error-free transformations).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bp = __fsub_rn(s, a);
+  float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
 }
 
-// Compensated accumulation of v into the per-site (hi, lo) pair: the vector
-// atomic returns the old hi, the rounding error of old + v (round to nearest,
-// as the atomic unit computes it) is recovered exactly by TwoSum and added to
-// lo.
-__device__ __forceinline__ void atomic_add_comp(float4 *hi, float4 *lo, float4 v) {
+// Compensated accumulation of the two-float value (vh, vl) into the per-site
+// (hi, lo) pair: the vector atomic returns the old hi; the rounding error of
+// old + vh (the atomic rounds to nearest) is recovered exactly by TwoSum and
+// added to lo together with vl.
+__device__ __forceinline__ float4 atom_add_v4(float4 *p, float4 v) {
   float4 o;
   asm volatile("atom.global.add.v4.f32 {%0,%1,%2,%3}, [%4], {%5,%6,%7,%8};"
                : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w)
-               : "l"(hi), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
                : "memory");
-  float4 e;
-#define TWO_SUM_ERR(A, B, E)                 \
-  {                                          \
-    float s_ = __fadd_rn(A, B);              \
-    float bp_ = __fsub_rn(s_, A);            \
-    float ap_ = __fsub_rn(s_, bp_);          \
-    E = __fadd_rn(__fsub_rn(A, ap_), __fsub_rn(B, bp_)); \
-  }
-  TWO_SUM_ERR(o.x, v.x, e.x);
-  TWO_SUM_ERR(o.y, v.y, e.y);
-  TWO_SUM_ERR(o.z, v.z, e.z);
-  TWO_SUM_ERR(o.w, v.w, e.w);
-#undef TWO_SUM_ERR
-  if (e.x != 0.f || e.y != 0.f || e.z != 0.f || e.w != 0.f)
-    asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(lo), "f"(e.x), "f"(e.y),
-                 "f"(e.z), "f"(e.w)
-                 : "memory");
+  return o;
+}
+__device__ __forceinline__ void red_add_v4(float4 *p, float4 v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
 }
 
+// Lower envelope of the row's column candidates, left in C[0, K).
+// Candidates are generated 32 columns at a time (lane = column, coalesced
+// loads) and the first round of chord removal is applied on the fly; further
+// rounds remove, all at once, every point strictly above the chord of its
+// current neighbours, until a round removes nothing -- the surviving chain is
+// then convex, i.e. the lower hull (each removed point lies above a chord of
+// points on or above the hull).  After kMaxRounds the remaining points go
+// through one sequential monotone-chain pass, so any input ends exactly.
+constexpr int kMaxRounds = 24;
+
+__device__ int row_hull(const LevelBufs &a, int r, int *C) {
+  const int n = a.n;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int band = r >> 6, bi = r & 63;
+  const uint64_t le = (bi == 63) ? ~0ull : ((2ull << bi) - 1ull);
+  const int base = band * kBand;
+  const uint64_t *wrow = (a.st->parity ? a.bits[1] : a.bits[0]) + (size_t)band * n;
+  const int16_t *prow = a.prev + (size_t)band * n;
+  const int16_t *nrow = a.next + (size_t)band * n;
+
+  auto cand = [&](int c) -> int {  // packed candidate of column 32c+lane or kNoEnt
+    const int x = c * 32 + lane;
+    const int cr = column_candidate(__ldg(wrow + x), __ldg(prow + x), __ldg(nrow + x), le, base, r);
+    return cr == kNoneAbove ? kNoEnt : pack_ent(x, cr - r);
+  };
+
+  // ---- phase 1: candidates + fused first chord round ----------------------
+  const int nchunks = n >> 5;
+  int K = 0;
+  int carry = kNoEnt;        // last valid candidate of earlier chunks
+  int cur = cand(0);
+  for (int c = 0; c < nchunks; ++c) {
+    const int nxt = (c + 1 < nchunks) ? cand(c + 1) : kNoEnt;
+    const unsigned vcur = __ballot_sync(0xffffffffu, cur != kNoEnt);
+    const unsigned vnxt = __ballot_sync(0xffffffffu, nxt != kNoEnt);
+    // left neighbour: previous valid lane of this chunk, else the carry
+    const unsigned lower = vcur & lt;
+    const int lsrc = lower ? 31 - __clz(lower) : 0;
+    int left = __shfl_sync(0xffffffffu, cur, lsrc);
+    if (!lower) left = carry;
+    // right neighbour: next valid lane of this chunk, else next chunk's first
+    const unsigned upper = vcur & ~lt & ~(1u << lane);
+    const int rsrc = upper ? __ffs(upper) - 1 : (vnxt ? __ffs(vnxt) - 1 : 0);
+    const int r_in = __shfl_sync(0xffffffffu, cur, rsrc);
+    const int r_nx = __shfl_sync(0xffffffffu, nxt, rsrc);
+    int right = upper ? r_in : (vnxt ? r_nx : kNoEnt);  // unknown: keep (always safe)
+    bool keep = cur != kNoEnt &&
+                (left == kNoEnt || right == kNoEnt || below_chord(left, cur, right));
+    const unsigned km = __ballot_sync(0xffffffffu, keep);
+    if (keep) C[K + __popc(km & lt)] = cur;
+    K += __popc(km);
+    if (vcur) carry = __shfl_sync(0xffffffffu, cur, 31 - __clz(vcur));
+    cur = nxt;
+  }
+  __syncwarp();
+
+  // ---- further rounds of simultaneous chord removal ------------------------
+  int round = 0;
+  for (; round < kMaxRounds; ++round) {
+    int w = 0;
+    int prevv = kNoEnt;  // last (original) value of the previous chunk
+    bool changed = false;
+    for (int c = 0; c < K; c += 32) {
+      const int idx = c + lane;
+      const int v = idx < K ? C[idx] : kNoEnt;
+      const int look = (lane == 31 && c + 32 < K) ? C[c + 32] : kNoEnt;
+      __syncwarp();
+      int left = __shfl_up_sync(0xffffffffu, v, 1);
+      if (lane == 0) left = prevv;
+      int right = __shfl_down_sync(0xffffffffu, v, 1);
+      if (lane == 31) right = look;
+      if (idx + 1 >= K) right = kNoEnt;
+      const bool keep = v != kNoEnt && (left == kNoEnt || right == kNoEnt || below_chord(left, v, right));
+      const unsigned km = __ballot_sync(0xffffffffu, keep);
+      const unsigned vm = __ballot_sync(0xffffffffu, v != kNoEnt);
+      changed |= (km != vm);
+      if (keep) C[w + __popc(km & lt)] = v;
+      w += __popc(km);
+      prevv = __shfl_sync(0xffffffffu, v, 31);
+      __syncwarp();
+    }
+    K = w;
+    if (!changed) break;
+  }
+  if (round == kMaxRounds) {  // not converged: one exact sequential pass
+    int sp = 0;
+    if (lane == 0) {
+      for (int i = 0; i < K; ++i) {
+        const int P = C[i];
+        while (sp >= 2 && !below_chord(C[sp - 2], C[sp - 1], P)) --sp;
+        C[sp++] = P;
+      }
+    }
+    K = __shfl_sync(0xffffffffu, sp, 0);
+    __syncwarp();
+  }
+  return K;
+}
+
+// Row support: [s0, s1) holds every pixel of the row with density != 0.
 template <int MODE>  // 0: write labels; 1: accumulate Lloyd moments
 __global__ void __launch_bounds__(kRowsPerBlock * 32) k_rows(LevelBufs a, int respect_stop) {
   extern __shared__ __align__(16) int smem[];
   if (respect_stop && a.st->stopped) return;
   const int n = a.n;
-  const int S = n >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = blockIdx.x * kRowsPerBlock + warp;
   if (r >= n) return;
-  RowSmem sm;
-  sm.SP = S + 1;
-  sm.base = smem + warp * (32 * sm.SP + 64);
-  int *stk = sm.stk(lane);
+  int *C = smem + warp * n;
+  const int K = row_hull(a, r, C);
 
-  // ---- local lower hull of this lane's columns ----------------------------
-  const int band = r >> 6, bi = r & 63;
-  const uint64_t le = (bi == 63) ? ~0ull : ((2ull << bi) - 1ull);
-  const int base = band * kBand;
-  const int xbeg = lane * S;
-  const uint64_t *wrow = (a.st->parity ? a.bits[1] : a.bits[0]) + (size_t)band * n + xbeg;
-  const int16_t *prow = a.prev + (size_t)band * n + xbeg;
-  const int16_t *nrow = a.next + (size_t)band * n + xbeg;
-  int sp = 0;
-  int t0x = 0, t0B = 0, t1x = 0, t1B = 0;  // second and top of the stack
-  for (int k0 = 0; k0 < S; k0 += 8) {
-    ulonglong2 w01 = *reinterpret_cast<const ulonglong2 *>(wrow + k0);
-    ulonglong2 w23 = *reinterpret_cast<const ulonglong2 *>(wrow + k0 + 2);
-    ulonglong2 w45 = *reinterpret_cast<const ulonglong2 *>(wrow + k0 + 4);
-    ulonglong2 w67 = *reinterpret_cast<const ulonglong2 *>(wrow + k0 + 6);
-    uint4 pv4 = *reinterpret_cast<const uint4 *>(prow + k0);
-    uint4 nx4 = *reinterpret_cast<const uint4 *>(nrow + k0);
-    uint64_t ws[8] = {w01.x, w01.y, w23.x, w23.y, w45.x, w45.y, w67.x, w67.y};
-    unsigned pvs[4] = {pv4.x, pv4.y, pv4.z, pv4.w};
-    unsigned nxs[4] = {nx4.x, nx4.y, nx4.z, nx4.w};
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      int pv = (int)(int16_t)((pvs[q >> 1] >> ((q & 1) * 16)) & 0xffffu);
-      int nx = (int)(int16_t)((nxs[q >> 1] >> ((q & 1) * 16)) & 0xffffu);
-      int c = column_candidate(ws[q], pv, nx, le, base, r);
-      if (c == kNoneAbove) continue;
-      const int x = xbeg + k0 + q;
-      const int g = c - r;
-      const int B = x * x + g * g;
-      while (sp >= 2) {
-        if (hull_cross(t0x, t0B, t1x, t1B, x, B) > 0) break;
-        --sp;
-        t1x = t0x; t1B = t0B;
-        if (sp >= 2) {
-          int e = stk[sp - 2];
-          t0x = ent_x(e); t0B = ent_B(e);
-        }
-      }
-      stk[sp++] = (x << 16) | (g & 0xffff);
-      t0x = t1x; t0B = t1B; t1x = x; t1B = B;
+  if (MODE == 0) {
+    uint32_t *out = a.labels + (size_t)r * n;
+    if (K == 0) {  // no site anywhere
+      for (int p = lane; p < n; p += 32) out[p] = kMarkerWord;
+      return;
     }
-  }
-  sm.lo()[lane] = 0;
-  sm.hi()[lane] = sp;
-  __syncwarp();
-
-  // ---- five levels of bridge merges ----------------------------------------
-#pragma unroll 1
-  for (int G = 1; G < 32; G <<= 1) {
-    if ((lane & (2 * G - 1)) == 0) bridge_merge(sm, lane, lane + G, lane + 2 * G);
-    __syncwarp();
-  }
-
-  // ---- locate the envelope entry covering this lane's first pixel ---------
-  const int mylo = sm.lo()[lane], myhi = sm.hi()[lane];
-  const unsigned ne = __ballot_sync(0xffffffffu, myhi > mylo);
-  const int X0 = xbeg;
-  uint32_t *lab_out = (MODE == 0) ? a.labels + (size_t)r * n + X0 : nullptr;
-  if (ne == 0) {  // no site anywhere
-    if (MODE == 0)
-      for (int p = 0; p < S; p += 4)
-        *reinterpret_cast<uint4 *>(lab_out + p) =
-            make_uint4(kMarkerWord, kMarkerWord, kMarkerWord, kMarkerWord);
+    for (int k0 = 0; k0 < K; k0 += 32) {
+      const int k = k0 + lane;
+      int s0 = 0, s1 = 0;
+      uint32_t lab = 0;
+      if (k < K) {
+        const int e = C[k];
+        s0 = k == 0 ? 0 : max(0, start_pixel(C[k - 1], e));
+        s1 = k + 1 == K ? n : min(n, start_pixel(e, C[k + 1]));
+        lab = pack_xy(ent_x(e), ent_g(e) + r);
+        if (s1 - s0 <= 16)
+          for (int p = s0; p < s1; ++p) out[p] = lab;
+      }
+      // long ranges: written by the whole warp, coalesced
+      unsigned lm = __ballot_sync(0xffffffffu, s1 - s0 > 16);
+      while (lm) {
+        const int L = __ffs(lm) - 1;
+        lm &= lm - 1;
+        const int b0 = __shfl_sync(0xffffffffu, s0, L), b1 = __shfl_sync(0xffffffffu, s1, L);
+        const uint32_t lv = __shfl_sync(0xffffffffu, lab, L);
+        for (int p = b0 + lane; p < b1; p += 32) out[p] = lv;
+      }
+    }
     return;
   }
-  int fe = 0, pe = 0;
-  bool has_pred = false;
-  if (myhi > mylo) {
-    fe = stk[mylo];
-    unsigned lower = ne & ((1u << lane) - 1u);
-    if (lower) {
-      int pl = 31 - __clz(lower);
-      pe = sm.at(pl, sm.hi()[pl] - 1);
-      has_pred = true;
-    }
-  }
-  int ansL = 0;
-#pragma unroll 4
-  for (int q = 0; q < 32; ++q) {
-    bool ok = (myhi > mylo) && (!has_pred || past_start(pe, fe, q * S));
-    unsigned m = __ballot_sync(0xffffffffu, ok);
-    if (lane == q) ansL = 31 - __clz(m);
-  }
-  int cL = ansL, ck;
-  {
-    int k0 = sm.lo()[ansL], k1 = sm.hi()[ansL] - 1;
-    while (k0 < k1) {
-      int mid = (k0 + k1 + 1) >> 1;
-      if (past_start(sm.at(ansL, mid - 1), sm.at(ansL, mid), X0)) k0 = mid;
-      else k1 = mid - 1;
-    }
-    ck = k0;
-  }
-  int cur = sm.at(cL, ck);
-  // successor on the envelope
-  int sL = cL, sk = ck + 1, suc = 0;
-  bool has_suc = true;
-  if (sk >= sm.hi()[sL]) {
-    unsigned above = (cL == 31) ? 0u : (ne & ~((2u << cL) - 1u));
-    if (above) { sL = __ffs(above) - 1; sk = sm.lo()[sL]; }
-    else has_suc = false;
-  }
-  if (has_suc) suc = sm.at(sL, sk);
 
-  // ---- walk the envelope over pixels [X0, X0 + S) --------------------------
-  const int ry = r;
-  if (MODE == 0) {
-    for (int p0 = 0; p0 < S; p0 += 4) {
-      uint32_t out[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int p = X0 + p0 + q;
-        while (has_suc && past_start(cur, suc, p)) {
-          cur = suc; cL = sL; ck = sk;
-          sk = ck + 1;
-          if (sk >= sm.hi()[sL]) {
-            unsigned above = (cL == 31) ? 0u : (ne & ~((2u << cL) - 1u));
-            if (above) { sL = __ffs(above) - 1; sk = sm.lo()[sL]; }
-            else has_suc = false;
-          }
-          if (has_suc) suc = sm.at(sL, sk);
-        }
-        out[q] = pack_xy(ent_x(cur), ent_g(cur) + ry);
-      }
-      *reinterpret_cast<uint4 *>(lab_out + p0) = make_uint4(out[0], out[1], out[2], out[3]);
+  // MODE 1: per entry, two-float sums over its pixels inside the row's density
+  // support, then one converged compensated flush per entry.  The flush's
+  // atomic returns the old accumulator; its TwoSum correction is completed at
+  // the next flush, so the atomic's round trip overlaps the next entry's work.
+  if (K == 0) return;
+  const int2 sup = a.support[r];
+  const float *drow = a.density + (size_t)r * n;
+  const uint64_t *bits = (a.st->parity ? a.bits[1] : a.bits[0]);
+  float4 pend_o = make_float4(0.f, 0.f, 0.f, 0.f), pend_v = pend_o, pend_l = pend_o;
+  int pend_slot = -1;
+  auto complete = [&]() {
+    if (pend_slot >= 0) {
+      float4 lo;
+      float t;
+      two_sum(pend_o.x, pend_v.x, t, lo.x);
+      two_sum(pend_o.y, pend_v.y, t, lo.y);
+      two_sum(pend_o.z, pend_v.z, t, lo.z);
+      two_sum(pend_o.w, pend_v.w, t, lo.w);
+      lo.x = __fadd_rn(lo.x, pend_l.x);
+      lo.y = __fadd_rn(lo.y, pend_l.y);
+      lo.z = __fadd_rn(lo.z, pend_l.z);
+      red_add_v4(a.mlo + pend_slot, lo);
+      pend_slot = -1;
     }
-  } else {
-    const float *drow = a.density + (size_t)r * n + X0;
-    float W = 0.f, SX = 0.f, Q = 0.f;
-    auto flush = [&](int e) {
-      if (W != 0.f) {
-        const int ex = ent_x(e), eg = ent_g(e);
-        const float fg = (float)eg;
-        float4 v = make_float4(W, SX, __fmul_rn(-fg, W), __fmaf_rn((float)(eg * eg), W, Q));
-        size_t pid = (size_t)(eg + ry) * n + ex;
-        atomic_add_comp(a.mhi + pid, a.mlo + pid, v);
-      }
-      W = 0.f; SX = 0.f; Q = 0.f;
-    };
-    for (int p0 = 0; p0 < S; p0 += 4) {
-      float4 d4 = __ldg(reinterpret_cast<const float4 *>(drow + p0));
-      float ds[4] = {d4.x, d4.y, d4.z, d4.w};
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int p = X0 + p0 + q;
-        while (has_suc && past_start(cur, suc, p)) {
-          flush(cur);
-          cur = suc; cL = sL; ck = sk;
-          sk = ck + 1;
-          if (sk >= sm.hi()[sL]) {
-            unsigned above = (cL == 31) ? 0u : (ne & ~((2u << cL) - 1u));
-            if (above) { sL = __ffs(above) - 1; sk = sm.lo()[sL]; }
-            else has_suc = false;
-          }
-          if (has_suc) suc = sm.at(sL, sk);
-        }
-        const float rho = ds[q];
-        const float dx = (float)(p - ent_x(cur));
-        W = __fadd_rn(W, rho);
-        SX = __fmaf_rn(dx, rho, SX);
+  };
+  for (int k0 = 0; k0 < K; k0 += 32) {
+    const int k = k0 + lane;
+    float Wh = 0.f, Wl = 0.f, Xh = 0.f, Xl = 0.f, Q = 0.f;
+    int e = 0;
+    if (k < K) {
+      e = C[k];
+      const int s0 = max(sup.x, k == 0 ? 0 : start_pixel(C[k - 1], e));
+      const int s1 = min(sup.y, k + 1 == K ? n : start_pixel(e, C[k + 1]));
+      const int ex = ent_x(e);
+      for (int p = s0; p < s1; ++p) {
+        const float rho = __ldg(drow + p);
+        const float dx = (float)(p - ex);
+        float s, er;
+        two_sum(Wh, rho, s, er);
+        Wh = s;
+        Wl = __fadd_rn(Wl, er);
+        const float pr = __fmul_rn(dx, rho);
+        const float pe = __fmaf_rn(dx, rho, -pr);
+        two_sum(Xh, pr, s, er);
+        Xh = s;
+        Xl = __fadd_rn(Xl, __fadd_rn(er, pe));
         Q = __fmaf_rn(__fmul_rn(dx, dx), rho, Q);
       }
     }
-    flush(cur);
+    if (k < K && Wh != 0.f) {
+      const int eg = ent_g(e), ex = ent_x(e);
+      const float fg = (float)(-eg);
+      // SY = -g * W (two-float), E = Q + g^2 * W
+      const float yh = __fmul_rn(fg, Wh);
+      const float yl = __fmaf_rn(fg, Wh, -yh) + fg * Wl;
+      const float Ev = __fmaf_rn((float)(eg * eg), Wh, Q);
+      const int slot = site_slot(bits, a.word_rank, a.group_offset, n, ex, eg + r);
+      const float4 v = make_float4(Wh, Xh, yh, Ev);
+      const float4 o = atom_add_v4(a.mhi + slot, v);
+      complete();
+      pend_o = o;
+      pend_v = v;
+      pend_l = make_float4(Wl, Xl, yl, 0.f);
+      pend_slot = slot;
+    }
   }
+  complete();
 }
 
-size_t rows_smem_bytes(int n) {
-  int S = n >> 5;
-  return (size_t)kRowsPerBlock * (32 * (S + 1) + 64) * sizeof(int);
-}
+size_t rows_smem_bytes(int n) { return (size_t)kRowsPerBlock * n * sizeof(int); }
 
 cudaError_t rows_configure() {
   cudaError_t e = cudaFuncSetAttribute(k_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -463,6 +497,31 @@ cudaError_t launch_rows(const LevelBufs &b, int label_mode, int respect_stop, cu
   dim3 blk(kRowsPerBlock * 32), grd((b.n + kRowsPerBlock - 1) / kRowsPerBlock);
   if (label_mode) k_rows<0><<<grd, blk, smem, s>>>(b, respect_stop);
   else k_rows<1><<<grd, blk, smem, s>>>(b, respect_stop);
+  return cudaGetLastError();
+}
+
+// Row support of a density grid: [first, last + 1) of its nonzero pixels
+// (an empty row gets [0, 0)).  One warp per row.
+__global__ void k_row_support(const float *__restrict__ d, int n, int2 *sup) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  int lo = n, hi = -1;
+  for (int p = lane; p < n; p += 32) {
+    if (d[(size_t)r * n + p] != 0.0f) {
+      lo = min(lo, p);
+      hi = max(hi, p);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) sup[r] = hi < 0 ? make_int2(0, 0) : make_int2(lo, hi + 1);
+}
+
+cudaError_t launch_row_support(const float *density, int n, int2 *sup, cudaStream_t s) {
+  k_row_support<<<(n + 7) / 8, 256, 0, s>>>(density, n, sup);
   return cudaGetLastError();
 }
 

@@ -3,14 +3,16 @@
 // k_update restates kernelFillShort + kernelUpdateSites (gcvt.cu:65-71,
 // 753-781) over the site bitmap: one thread per 64-row word, one site per set
 // bit.  The centroid comes from the compensated moments the row pass
-// accumulated (FP64 only for the final division, as the reference's centroid
-// is a float): c = site + SX/W, rounded once to float, then
+// accumulated, divided in two-float arithmetic (GB300 runs FP64 at a small
+// fraction of FP32 rate, and this kernel was FP64-bound): c = site + SX/W,
+// rounded once to float, then
 //     new = trunc(fma(c - site, omega, site) + 0.5f), clamped to [0, n-1],
 // unchanged for fixed sites or when the density at the new pixel is 0.  New
 // positions are OR-ed into the other bitmap, so sites landing on one pixel
-// merge, as the reference's scatter does.  The energy total is summed in FP64
-// in a fixed order (threads, then blocks), and the last block runs the omega /
-// stop schedule of gcvt.cu:1105-1142 on the device.
+// merge, as the reference's scatter does.  The energy is summed in two-float
+// arithmetic in a fixed order (threads, then blocks), the global total is
+// formed in FP64 once, and the last block runs the omega / stop schedule of
+// gcvt.cu:1105-1142 on the device.
 #include "gcvt_internal.cuh"
 
 namespace cvtgb {
@@ -20,6 +22,37 @@ namespace cvtgb {
 __device__ __forceinline__ int update_coord(float v, int n) {
   int c = __float2int_rz(v);  // saturates to int32, NaN -> 0
   return min(max(c, 0), n - 1);
+}
+
+// Error-free sum of two floats (TwoSum).
+__device__ __forceinline__ void tsum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bp = __fsub_rn(s, a);
+  float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// (ah, al) + (bh, bl) in two-float arithmetic.
+__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
+  float s, e;
+  tsum(ah, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(al, bl));
+  ah = __fadd_rn(s, e);
+  al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
+// Centroid coordinate base + (Sh + Sl) / (Wh + Wl) rounded once to float.
+// The quotient is formed in two-float arithmetic (about 44 significant
+// bits): q = Sh / Wh, remainder r = (Sh - q Wh) + Sl - q Wl (the first term
+// exact by fma), q2 = r / Wh; then base + q + q2 is summed error-free and
+// rounded.  W = 0 gives NaN, as the reference's 0/0 does.
+__device__ __forceinline__ float centroid_coord(int base, float Sh, float Sl, float Wh, float Wl) {
+  const float q = __fdiv_rn(Sh, Wh);
+  const float rr = __fadd_rn(__fmaf_rn(-q, Wh, Sh), __fmaf_rn(-q, Wl, Sl));
+  const float q2 = __fdiv_rn(rr, Wh);
+  float s, e;
+  tsum((float)base, q, s, e);
+  return __fadd_rn(s, __fadd_rn(e, q2));
 }
 
 __global__ void __launch_bounds__(kUpdateThreads) k_update(LevelBufs a) {
@@ -32,63 +65,76 @@ __global__ void __launch_bounds__(kUpdateThreads) k_update(LevelBufs a) {
   uint64_t *cur = parity ? a.bits[1] : a.bits[0];
   uint64_t *nxt = parity ? a.bits[0] : a.bits[1];
   const float omega = st->omega;
-  double e = 0.0;
+  float eh = 0.f, el = 0.f;  // energy, two-float
   if (t < nwords) {
     uint64_t w = cur[t];
     if (w) cur[t] = 0ull;  // this buffer receives the iteration after next
-    const int b = (int)(t / n), x = (int)(t % n);
+    const int b = (int)(t / (unsigned)n), x = (int)(t % (unsigned)n);
+    const uint64_t fw = w ? a.fixed_bits[t] : 0ull;
+    int slot = w ? a.group_offset[x >> 5] + a.word_rank[t] : 0;
     while (w) {
       const int i = __ffsll((long long)w) - 1;
       w &= w - 1ull;
       const int y = b * kBand + i;
-      const size_t pid = (size_t)y * n + x;
-      const float4 h = a.mhi[pid], l = a.mlo[pid];
-      a.mhi[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
-      a.mlo[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
-      const double W = (double)h.x + (double)l.x;
-      const double SX = (double)h.y + (double)l.y;
-      const double SY = (double)h.z + (double)l.z;
-      e += (double)h.w + (double)l.w;
-      const float cx = (float)((double)x + SX / W);
-      const float cy = (float)((double)y + SY / W);
+      const float4 h = a.mhi[slot], l = a.mlo[slot];
+      a.mhi[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+      a.mlo[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+      ++slot;
+      df_add(eh, el, h.w, l.w);
+      const float cx = centroid_coord(x, h.y, l.y, h.x, l.x);
+      const float cy = centroid_coord(y, h.z, l.z, h.x, l.x);
       const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)x), omega, (float)x), 0.5f);
       const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)y), omega, (float)y), 0.5f);
       int nx = update_coord(fx, n), ny = update_coord(fy, n);
-      if (a.fixed[pid] || a.density[(size_t)ny * n + nx] == 0.0f) { nx = x; ny = y; }
+      if (((fw >> i) & 1ull) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = x; ny = y; }
       atomicOr(reinterpret_cast<unsigned long long *>(nxt + (size_t)(ny / kBand) * n + nx),
                1ull << (ny % kBand));
     }
   }
-  // fixed-order block reduction of the energy
-  __shared__ double sred[kUpdateThreads];
+  // fixed-order two-float block reduction of the energy
+  __shared__ float sh[kUpdateThreads], sl[kUpdateThreads];
   __shared__ bool is_last;
-  sred[threadIdx.x] = e;
+  sh[threadIdx.x] = eh;
+  sl[threadIdx.x] = el;
   __syncthreads();
   for (int s = kUpdateThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sred[threadIdx.x] += sred[threadIdx.x + s];
+    if (threadIdx.x < s) {
+      float ah = sh[threadIdx.x], al = sl[threadIdx.x];
+      df_add(ah, al, sh[threadIdx.x + s], sl[threadIdx.x + s]);
+      sh[threadIdx.x] = ah;
+      sl[threadIdx.x] = al;
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    a.blk_energy[blockIdx.x] = sred[0];
+    a.blk_energy[2 * blockIdx.x] = sh[0];
+    a.blk_energy[2 * blockIdx.x + 1] = sl[0];
     __threadfence();
     unsigned prev = atomicAdd(&st->done_blocks, 1u);
     is_last = (prev == gridDim.x - 1);
   }
   __syncthreads();
   if (!is_last) return;
-  // last block: total energy in block order, then the schedule
+  // last block: total energy in block order (two-float, then one FP64 total),
+  // then the schedule
   __threadfence();
-  double acc = 0.0;
-  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x)
-    acc += ((volatile double *)a.blk_energy)[k];
-  sred[threadIdx.x] = acc;
+  float ah = 0.f, al = 0.f;
+  const volatile float *be = a.blk_energy;
+  for (unsigned k = threadIdx.x; k < gridDim.x; k += blockDim.x) df_add(ah, al, be[2 * k], be[2 * k + 1]);
+  sh[threadIdx.x] = ah;
+  sl[threadIdx.x] = al;
   __syncthreads();
   for (int s = kUpdateThreads / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sred[threadIdx.x] += sred[threadIdx.x + s];
+    if (threadIdx.x < s) {
+      float xh = sh[threadIdx.x], xl = sl[threadIdx.x];
+      df_add(xh, xl, sh[threadIdx.x + s], sl[threadIdx.x + s]);
+      sh[threadIdx.x] = xh;
+      sl[threadIdx.x] = xl;
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double E = sred[0] * st->energy_scale;
+    const double E = ((double)sh[0] + (double)sl[0]) * st->energy_scale;
     st->energy = E;
     const int i = st->iter;
     if (i % 10 == 0) st->sampled = E;          // gcvt.cu:1116-1117
@@ -172,17 +218,19 @@ __global__ void k_read_moments(LevelBufs a, double *out) {
   size_t pid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= (size_t)n * n) return;
   const int x = (int)(pid % n), y = (int)(pid / n);
-  const uint64_t w = (a.st->parity ? a.bits[1] : a.bits[0])[(size_t)(y / kBand) * n + x];
+  const uint64_t *bits = a.st->parity ? a.bits[1] : a.bits[0];
+  const uint64_t w = bits[(size_t)(y / kBand) * n + x];
   double W = 0, X = 0, Y = 0, E = 0;
   if ((w >> (y % kBand)) & 1ull) {
-    const float4 h = a.mhi[pid], l = a.mlo[pid];
+    const int slot = site_slot(bits, a.word_rank, a.group_offset, n, x, y);
+    const float4 h = a.mhi[slot], l = a.mlo[slot];
     W = (double)h.x + (double)l.x;
     X = (double)x * W + ((double)h.y + (double)l.y);
     Y = (double)y * W + ((double)h.z + (double)l.z);
     E = (double)h.w + (double)l.w;
+    a.mhi[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.mlo[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  a.mhi[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
-  a.mlo[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
   const size_t nn = (size_t)n * n;
   out[pid] = W;
   out[nn + pid] = X;
