@@ -127,6 +127,18 @@ int gcvt_compute(int16_t *voronoi, const float *density, const uint8_t *mask, in
 /* Label a site grid once (pba2DCompute on a given grid). */
 int gcvt_label_grid(const int16_t *sites, int16_t *labels, int n, int mem);
 
+/* The same labelling for callers that cannot allocate device memory -- code
+ * handed pre-allocated buffers by a host that owns all device memory, or a
+ * loop that must not allocate after start-up.  No counterpart in the
+ * reference.  `sites` and `labels` are device pointers (2*n*n int16 each) on
+ * the current device; `stream` is a cudaStream_t (NULL: the legacy default
+ * stream).  Nothing is allocated: the scratch lives in one static device
+ * array sized for n <= 2048 (about 1 MB, held by every device that loads the
+ * library until exit); larger n returns GCVT_ERR_SIZE.  The first call on a
+ * device looks up that array's device address -- make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race. */
+int gcvt_label_grid_static(const int16_t *sites, int16_t *labels, int n, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 

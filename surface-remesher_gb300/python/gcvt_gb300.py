@@ -62,6 +62,7 @@ SIGNATURES = {
     "gcvt_ctx_time_kernels": ([P, I, P], I),
     "gcvt_compute": ([P, P, P, I, I, I], I),
     "gcvt_label_grid": ([P, P, I, I], I),
+    "gcvt_label_grid_static": ([P, P, I, P], I),
 }
 CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii"}
 
