@@ -127,6 +127,17 @@ int gcvt_compute(int16_t *voronoi, const float *density, const uint8_t *mask, in
 /* Label a site grid once (pba2DCompute on a given grid). */
 int gcvt_label_grid(const int16_t *sites, int16_t *labels, int n, int mem);
 
+/* Rasterise a triangle mesh into a density grid, pixel for pixel equal to
+ * kernelDiscretization (discretization.cu:57-85): pixel (tx, ty) samples
+ * (tx*scale, ty*scale); the first triangle (index order) whose three FP64
+ * barycentric weights are all >= 0 gives sum w_i * weight[v_i], else 0.
+ * points: 2*num_point doubles, weight: num_point doubles, triangle:
+ * 3*num_tri vertex indices, density: n*n floats; n a multiple of 16.
+ * Replaces discretization_d (discretization.cu:87-120). */
+int gcvt_rasterize(const double *points, const double *weight, int num_point,
+                   const int32_t *triangle, int num_tri, float *density, double scale, int n,
+                   int mem);
+
 /* The same labelling for callers that cannot allocate device memory -- code
  * handed pre-allocated buffers by a host that owns all device memory, or a
  * loop that must not allocate after start-up.  No counterpart in the
@@ -146,6 +157,11 @@ int gcvt_label_grid_static(const int16_t *sites, int16_t *labels, int n, void *s
  * gcvt.cu:1087), so source/main.cpp links against this library unchanged. */
 extern void gCVT(short *Voronoi, float *density_d, bool *mask, int size, int depth,
                  int maxIter);
+
+/* The reference's rasteriser entry point, same signature and C++ symbol
+ * (discretization.h:66, discretization.cu:87). */
+extern void discretization_d(double *points, double *weight, int num_point, int *triangle,
+                             int num_tri, float *density, double scale, int n);
 #endif
 
 #endif /* GCVT_GB300_H */

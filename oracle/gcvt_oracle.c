@@ -997,7 +997,8 @@ int orc_rasterize(const double *points, const double *weight, int num_point,
                 bary(points[p1 << 1], points[p1 << 1 | 1], points[p2 << 1], points[p2 << 1 | 1],
                      points[p3 << 1], points[p3 << 1 | 1], x, y, &w1, &w2, &w3);
                 if (w1 < 0 || w2 < 0 || w3 < 0) continue;
-                res = (float)fma(w3, weight[p3], fma(w2, weight[p2], w1 * weight[p1]));
+                /* w1*weight[p1] + w2*weight[p2] + w3*weight[p3] as nvcc contracts it */
+                res = (float)fma(w3, weight[p3], fma(w1, weight[p1], w2 * weight[p2]));
                 goto done;
             }
             res = 0.0f;

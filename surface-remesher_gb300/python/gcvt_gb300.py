@@ -63,8 +63,10 @@ SIGNATURES = {
     "gcvt_compute": ([P, P, P, I, I, I], I),
     "gcvt_label_grid": ([P, P, I, I], I),
     "gcvt_label_grid_static": ([P, P, I, P], I),
+    "gcvt_rasterize": ([P, P, I, P, I, P, ctypes.c_double, I, I], I),
 }
-CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii"}
+CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii",
+               "discretization_d": "_Z16discretization_dPdS_iPiiPfdi"}
 
 _lib = None
 
@@ -220,6 +222,17 @@ def label_grid(sites):
     out = np.empty_like(sites)
     _check(lib.gcvt_label_grid(_host_ptr(sites, np.int16, (n, n, 2)), out.ctypes.data, n,
                                MEM_HOST), "gcvt_label_grid")
+    return out
+
+
+def rasterize(points, weight, triangles, scale, n):
+    """Density grid (n, n) float32 of a mesh: points (V, 2) float64, weight (V,)
+    float64, triangles (T, 3) int32 (discretization_d's arguments)."""
+    lib = load_library()
+    out = np.empty((n, n), np.float32)
+    _check(lib.gcvt_rasterize(_host_ptr(points, np.float64), _host_ptr(weight, np.float64),
+                              len(weight), _host_ptr(triangles, np.int32), len(triangles),
+                              out.ctypes.data, float(scale), int(n), MEM_HOST), "gcvt_rasterize")
     return out
 
 

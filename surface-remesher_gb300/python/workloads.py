@@ -64,6 +64,15 @@ def disk_sites(n, m, seed, density=None, radius=0.48):
     return g
 
 
+def mesh_inputs(nv=256, n=2048, sites=65536, seed=2):
+    """Mesh-driven configuration: the rasterised area-ratio density of a
+    jittered disk mesh (see disk_mesh) and sites uniform over its support.
+    Returns (mesh tuple (points, weight, triangles, scale), sites, mask)."""
+    P, w, T = disk_mesh(nv, seed=seed)
+    Q, scale, _, _ = raster_inputs(P, n)
+    return (Q, w, T, scale), np.zeros((n, n), np.uint8)
+
+
 def config_inputs(name, seed=1):
     """(sites, density, mask, iterations) of a named configuration."""
     c = CONFIGS[name]
@@ -71,6 +80,67 @@ def config_inputs(name, seed=1):
     sites = disk_sites(c["n"], c["sites"], seed, rho)
     mask = np.zeros((c["n"], c["n"]), np.uint8)
     return sites, rho, mask, c["iters"]
+
+
+def disk_mesh(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
+    """Triangulated unit-disk parameterisation with a height field.
+
+    A regular nv x nv grid on [0,1]^2 (two triangles per cell) keeps the
+    triangles whose vertices all lie in the disk of centre (0.5, 0.5); vertices
+    get seeded Gaussian in-plane jitter of jitter x edge; the surface height is
+    z = 0.1 sum_j sin(f_j u + g_j v + phi_j), f, g ~ U(2, 20).  The per-vertex
+    density weight is the area ratio of weighting.h:79: sum of incident 3D face
+    areas / sum of incident UV face areas (ratios above 1e10 take the largest
+    finite ratio, weighting.h:80-92).
+    Returns (uv (V, 2) float64, weight (V,) float64, triangles (T, 3) int32)."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (nv - 1)
+    g = np.arange(nv) * h
+    X, Y = np.meshgrid(g, g)
+    P = np.stack([X.ravel(), Y.ravel()], 1)
+    inside = (P[:, 0] - 0.5) ** 2 + (P[:, 1] - 0.5) ** 2 <= radius * radius
+    P = P + rng.normal(0.0, jitter * h, P.shape)
+    idx = np.arange(nv * nv).reshape(nv, nv)
+    a, b, c, d = idx[:-1, :-1], idx[:-1, 1:], idx[1:, :-1], idx[1:, 1:]
+    tris = np.concatenate([np.stack([a, b, d], -1).reshape(-1, 3),
+                           np.stack([a, d, c], -1).reshape(-1, 3)])
+    tris = tris[inside[tris].all(1)]
+    used = np.unique(tris)
+    remap = -np.ones(nv * nv, np.int64)
+    remap[used] = np.arange(len(used))
+    P = P[used]
+    tris = remap[tris]
+    f = rng.uniform(2, 20, waves)
+    gg = rng.uniform(2, 20, waves)
+    phi = rng.uniform(0, 2 * np.pi, waves)
+    z = 0.1 * np.sin(np.outer(P[:, 0], f) + np.outer(P[:, 1], gg) + phi).sum(1)
+    P3 = np.concatenate([P, z[:, None]], 1)
+    e1 = P3[tris[:, 1]] - P3[tris[:, 0]]
+    e2 = P3[tris[:, 2]] - P3[tris[:, 0]]
+    a3 = 0.5 * np.linalg.norm(np.cross(e1, e2), axis=1)
+    u1, u2 = e1[:, :2], e2[:, :2]
+    a2 = 0.5 * np.abs(u1[:, 0] * u2[:, 1] - u2[:, 0] * u1[:, 1])
+    s3 = np.zeros(len(P))
+    s2 = np.zeros(len(P))
+    for k in range(3):
+        np.add.at(s3, tris[:, k], a3)
+        np.add.at(s2, tris[:, k], a2)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = s3 / s2
+    finite = np.isfinite(w) & (w <= 1e10)
+    w[~finite] = w[finite].max()
+    return P, w, tris.astype(np.int32)
+
+
+def raster_inputs(P, n):
+    """The host marshalling of discretization (discretization.h:89-118):
+    scale = longest bounding-box side / (n - 1), points shifted to the box's
+    lower-left corner.  Returns (shifted points, scale, left, lower)."""
+    l, b = P[:, 0].min(), P[:, 1].min()
+    r, u = P[:, 0].max(), P[:, 1].max()
+    scale = (u - b) / (n - 1) if (u - b) > (r - l) else (r - l) / (n - 1)
+    Q = np.ascontiguousarray(np.stack([P[:, 0] - l, P[:, 1] - b], 1))
+    return Q, scale, l, b
 
 
 def small_case(n, m, seed, k=6, a_max=4.0):

@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [os.path.join(ROOT, "oracle"), os.path.join(ROOT, "surface-remesher_gb300", "python")]
 
 import oracle as orc  # noqa: E402
-from workloads import MARKER, small_case  # noqa: E402
+from workloads import MARKER, disk_mesh, raster_inputs, small_case  # noqa: E402
 
 
 def pts_grid(n, xs, ys):
@@ -105,6 +105,19 @@ def main(outdir):
     d["run_iterations"] = np.int32(info["iterations"])
     d["run_energies"] = np.array(info["energies"], np.float32)
     np.savez_compressed(os.path.join(outdir, "ref_lloyd.npz"), **d)
+    # 3. rasteriser (discretization_d) on jittered disk meshes
+    d = {}
+    for i, (nv, n, seed, jit) in enumerate(((24, 256, 11, 0.3), (40, 256, 12, 0.45))):
+        P, w, T = disk_mesh(nv, jitter=jit, seed=seed)
+        Q, scale, _, _ = raster_inputs(P, n)
+        dens, _ = orc.ref_rasterize(Q, w, T, scale, n)
+        d["n%d" % i] = np.int32(n)
+        d["points%d" % i] = Q
+        d["weight%d" % i] = w
+        d["tris%d" % i] = T
+        d["scale%d" % i] = np.float64(scale)
+        d["density%d" % i] = dens
+    np.savez_compressed(os.path.join(outdir, "ref_raster.npz"), **d)
     print("wrote", sorted(os.listdir(outdir)))
 
 

@@ -77,3 +77,13 @@ def test_oracle_gcvt_run_close_to_reference(oracle, lloyd_npz):
     ref_iters = int(lloyd_npz["run_iterations"])
     assert abs(st["iterations"] - ref_iters) <= 20, (st["iterations"], ref_iters)
     assert (out == want).all(-1).mean() > 0.8
+
+
+def test_oracle_raster_equals_reference_kernel(oracle):
+    z = np.load(os.path.join(GOLD, "ref_raster.npz"))
+    for i in range(2):
+        n = int(z["n%d" % i])
+        got = oracle.rasterize(z["points%d" % i], z["weight%d" % i], z["tris%d" % i],
+                               float(z["scale%d" % i]), n)
+        want = z["density%d" % i]
+        assert np.array_equal(got.view(np.int32), want.view(np.int32)), i
