@@ -18,10 +18,10 @@ Metric: Gpix-pass/s = n^2 x labelling passes / second, 101 passes per step
   e2e   : the same through the C ABI with pinned host buffers: host->device
           copies of sites, density and mask and the device->host copy of the
           label grid inside every timed step.
-  roofline: the dominant kernel (fused label + moment row pass): algorithmic
-          bytes per launch / its mean launch duration (CUDA events on the
-          launching stream over the same workload) against the measured HBM
-          copy bandwidth.
+  roofline: the dominant kernel (k_cell<0>, one whole Lloyd iteration):
+          algorithmic bytes per launch / its mean launch duration (CUDA events
+          on the launching stream over the same workload) against the measured
+          HBM copy bandwidth.
 --impl reference runs the reference's algorithm on the host cores (the
 oracle's OpenMP restatement of gcvt.cu, all threads) on a bounded sample of
 the same workload, in the same unit.
@@ -49,14 +49,26 @@ ITERS = 100
 PASSES = ITERS + 1
 METRIC = "Gpix-pass/s, plain Lloyd CVT (gCVT loop), 4096^2 grid, 262,144 sites, 100 iterations"
 UNIT = "Gpix-pass/s"
-# Algorithmic bytes of one fused row-pass launch per pixel and per site:
-# density 4 B/px + site bitmap 1/8 B/px + column summaries 1/16 B/px, and the
-# per-site moment accumulators (hi + lo float4) 32 B/site.
-ALG_BYTES_PER_PX = 4.0 + 0.125 + 0.0625
-ALG_BYTES_PER_SITE = 32.0
-# dram__bytes_read.sum + dram__bytes_write.sum of one row-pass launch on this
+# Algorithmic bytes of one Lloyd-iteration launch (k_cell<0>): the density
+# once over its row support (4 B per support pixel: every such pixel belongs
+# to exactly one cell), the current site bitmap read and the bitmap two
+# iterations ahead cleared (1/8 B per pixel each), and per site its word of the
+# fixed-site bitmap read and its bit OR-ed into the next bitmap (8 + 8 B).
+ALG_BYTES_PER_SUPPORT_PX = 4.0
+ALG_BYTES_PER_PX = 0.125 + 0.125
+ALG_BYTES_PER_SITE = 16.0
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_cell<0> launch on this
 # workload, from the ncu capture summarised in profiles/ (None until captured).
 NCU_TRAFFIC_BYTES = None
+
+
+def support_pixels(rho):
+    """Pixels inside the per-row [first, last] span of nonzero density."""
+    nz = rho != 0
+    rows = nz.any(1)
+    first = np.argmax(nz, 1)
+    last = rho.shape[1] - 1 - np.argmax(nz[:, ::-1], 1)
+    return int(((last - first + 1) * rows).sum())
 
 
 def dist_env():
@@ -259,9 +271,10 @@ def run_ours(args):
     value = passes / t_dev / 1e9
     e2e = passes / t_e2e / 1e9
     peak, peak_kind = measured_peak()
-    alg = n * n * ALG_BYTES_PER_PX + nsites * ALG_BYTES_PER_SITE
-    rows_s = kms[1] / 1e3
-    achieved = alg / rows_s / 1e9
+    support_px = support_pixels(rho)
+    alg = (support_px * ALG_BYTES_PER_SUPPORT_PX + n * n * ALG_BYTES_PER_PX
+           + nsites * ALG_BYTES_PER_SITE)
+    achieved = alg / (kms[0] / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
@@ -272,16 +285,19 @@ def run_ours(args):
                    "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
                    "parallelism": "replicas x%d" % ws},
         "iter_per_s": ITERS * args.steps * ws / t_dev,
-        "kernel_ms": {"column_summary": kms[0], "row_pass": kms[1], "update": kms[2]},
+        "kernel_ms": {"lloyd_iteration": kms[0], "label_pass": kms[1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
-                     "peak_source": peak_kind, "kernel": "k_rows<1> (fused label + moments)",
+                     "peak_source": peak_kind, "kernel": "k_cell<0> (one Lloyd iteration)",
                      "algorithmic_bytes": alg},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(h_sites.numel() * 2 + h_rho.numel() * 4 + h_mask.numel()),
                 "d2h_bytes_per_step": int(h_out.numel() * 2),
                 "ms_per_step": t_e2e / args.steps * 1e3},
-        "gpu_launches": args.steps * (3 + 4 * ITERS + 3),
+        # per step: load (row support, fixed bitmap, site bitmap), covering
+        # bound (column summaries, rows, k_cover, k_cover_finish), one k_cell
+        # per iteration, final labelling (column summaries, rows)
+        "gpu_launches": args.steps * (3 + 4 + ITERS + 2),
         "clocks": clk.summary(),
         "final_energy": info["energy"],
     }
@@ -322,9 +338,10 @@ def run_profile_case(iterations):
     sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
     ctx = G.Context(sites.shape[0])
     ctx.load(sites, rho, mask)
-    ms = ctx.time_kernels(iterations)
+    per_iter = [ctx.time_kernels(1)[0] for _ in range(iterations)]
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": CONFIG, "iterations": iterations, "kernel_ms": ms}))
+    print(json.dumps({"profile_case": CONFIG, "iterations": iterations,
+                      "lloyd_ms_per_iteration": per_iter}))
     ctx.close()
     return 0
 

@@ -106,12 +106,13 @@ int gcvt_ctx_sites(gcvt_ctx *ctx, int16_t *voronoi, int mem);
  * same sums in pbaTotalW/X/Y after kernelScan_Y (gcvt.cu:1008-1023). */
 int gcvt_ctx_moments(gcvt_ctx *ctx, double *out4, int mem);
 
-/* Run `iterations` plain Lloyd iterations as separate launches and return
- * the mean duration (ms) of each of the iteration's three kernels -- column
- * summaries, fused label + moment row pass, site update -- timed with CUDA
- * events on the context's stream.  The sites advance as in
- * gcvt_ctx_iterate.  No reference counterpart: the reference times nothing
- * (gcvt.cu:27 includes a timer header it never uses). */
+/* Run `iterations` plain Lloyd iterations as separate launches, each
+ * followed by a labelling pass, and return in ms3 the mean duration (ms) of
+ * [0] one Lloyd iteration (one kernel), [1] one labelling pass (column
+ * summaries + rows), [2] 0 -- timed with CUDA events on the context's
+ * stream.  The sites advance as in gcvt_ctx_iterate.  No reference
+ * counterpart: the reference times nothing (gcvt.cu:27 includes a timer
+ * header it never uses). */
 int gcvt_ctx_time_kernels(gcvt_ctx *ctx, int iterations, float *ms3);
 
 /* Schedule state (iterations, omega, energies). */

@@ -2,11 +2,11 @@
 // allocated once), the Lloyd driver of gCVT (gcvt.cu:1087-1156) and the C ABI
 // declared in include/gcvt_gb300.h.
 //
-// One Lloyd iteration is three launches (column summaries, fused row pass,
-// update), all reading their buffer roles and the omega / stop state from
-// device memory, so ten iterations are captured once as a CUDA graph and
-// replayed.  The host reads the state back once per ten iterations, where the
-// reference's schedule can end a level (gcvt.cu:1125-1140).
+// One Lloyd iteration is two launches (cells.cu: site list, cells) that read
+// their buffer roles and the omega / stop state from device memory, so ten
+// iterations are captured once as a CUDA graph and replayed.  The host reads the state back once per
+// ten iterations, where the reference's schedule can end a level
+// (gcvt.cu:1125-1140).  Label grids come from the PBA+ passes (labeller.cu).
 #include "gcvt_internal.cuh"
 #include "../../include/gcvt_gb300.h"
 
@@ -25,27 +25,32 @@ struct gcvt_ctx {
   int loaded = 0;
   int input_err = 0;    // the loaded grid is malformed at full resolution
   int cur_n = 0;        // size of the level currently held in the bitmaps
+  int sites = 0;        // sites in the grid the bitmaps were built from
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
-  float *density[8] = {};  // pyramid, [0] = full resolution
-  int dens_levels = 0;
+  float *density[8] = {};      // pyramid, [0] = full resolution
+  int2 *support[8] = {};       // per level: [first, last+1) of nonzero density per row
+  int2 *sup_range[8] = {};     // per level: rows holding nonzero density
+  uint64_t *fixed_bits[8] = {};
+  unsigned long long *sup_pixels = nullptr;  // per level: pixels of nonzero density
   uint8_t *mask = nullptr;
   uint32_t *input = nullptr;  // the loaded site grid, kept for gcvt_ctx_run
   uint32_t *grid = nullptr;   // staging: labels and site dumps
-  uint64_t *bits[2] = {};
+  uint64_t *bits[3] = {};
   int16_t *prev = nullptr, *next = nullptr;
-  uint64_t *fixed_bits[8] = {};   // per level
-  int *word_rank = nullptr, *group_count = nullptr, *group_offset = nullptr;
-  float4 *mhi = nullptr, *mlo = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned mirror
-  float *blk_energy = nullptr;    // 2 floats per update block
-  int2 *support[8] = {};          // per level: row support of the density
+  uint32_t *list = nullptr;     // site list, n_max^2 entries
+  unsigned *counts[3] = {};     // per bitmap: sites per list block
+  uint8_t *hint = nullptr;      // per pixel window hints
+  float4 *gslot = nullptr, *sslot = nullptr;
+  unsigned *scnt = nullptr;
+  int cover_valid = 0;          // the covering bound, list counts and hints
+                                // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
-  int *err = nullptr;
+  int *err = nullptr;           // [0] malformed-grid flag, [1] site count
   int last_levels = 0;
-  // graph of kChunk iterations for one level size
-  cudaGraphExec_t chunk_exec = nullptr;
+  cudaGraphExec_t chunk_exec = nullptr;  // kChunk iterations of one level
   int chunk_n = 0;
   int chunk_level = -1;
 };
@@ -62,26 +67,26 @@ constexpr int kChunk = 10;  // iterations per graph; the schedule acts every 10
 
 bool valid_n(int n) { return n >= kMinN && n <= kMaxN && n % 256 == 0; }
 bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+size_t bits_words(int n) { return (size_t)(n / kBand) * n; }
 
 LevelBufs level_bufs(gcvt_ctx *c, int n, int level) {
-  LevelBufs b;
+  LevelBufs b = {};
   b.n = n;
-  b.bits[0] = c->bits[0];
-  b.bits[1] = c->bits[1];
+  for (int k = 0; k < 3; ++k) b.bits[k] = c->bits[k];
   b.prev = c->prev;
   b.next = c->next;
   b.density = c->density[level];
-  b.fixed = c->mask;
+  b.support = c->support[level];
+  b.sup_range = c->sup_range[level];
   b.fixed_bits = c->fixed_bits[level];
-  b.word_rank = c->word_rank;
-  b.group_count = c->group_count;
-  b.group_offset = c->group_offset;
-  b.mhi = c->mhi;
-  b.mlo = c->mlo;
   b.labels = c->grid;
   b.st = c->st;
-  b.blk_energy = c->blk_energy;
-  b.support = c->support[level];
+  b.list = c->list;
+  for (int k = 0; k < 3; ++k) b.counts[k] = c->counts[k];
+  b.hint = c->hint;
+  b.gslot = c->gslot;
+  b.sslot = c->sslot;
+  b.scnt = c->scnt;
   return b;
 }
 
@@ -96,41 +101,41 @@ int push_state(gcvt_ctx *c) {
   return GCVT_OK;
 }
 
-// Enqueue one Lloyd iteration at size n.
-int enqueue_iteration(gcvt_ctx *c, int n, int level) {
-  LevelBufs b = level_bufs(c, n, level);
-  CK(launch_summary(b, 1, c->stream));
-  CK(launch_rows(b, 0 /*lloyd*/, 1, c->stream));
-  CK(launch_update(b, c->stream));
-  return GCVT_OK;
-}
-
-// Enqueue kChunk iterations through a CUDA graph captured once per (size,
-// level); a stream that cannot be captured (the legacy default stream) gets
-// plain launches.
+// Enqueue kChunk Lloyd iterations through a CUDA graph captured once per
+// (size, level); a stream that cannot be captured (the legacy default stream)
+// gets plain launches.
 int enqueue_chunk(gcvt_ctx *c, int n, int level) {
   if (c->chunk_exec && (c->chunk_n != n || c->chunk_level != level)) {
     cudaGraphExecDestroy(c->chunk_exec);
     c->chunk_exec = nullptr;
   }
+  const LevelBufs b = level_bufs(c, n, level);
   if (!c->chunk_exec) {
-    cudaGraph_t g;
     if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       cudaGetLastError();
       for (int i = 0; i < kChunk; ++i) {
-        int rc = enqueue_iteration(c, n, level);
-        if (rc) return rc;
+        CK(launch_list(b, 1, c->stream));
+        CK(launch_cells(b, 0, nullptr, c->stream));
       }
       return GCVT_OK;
     }
-    int rc = GCVT_OK;
-    for (int i = 0; i < kChunk && rc == GCVT_OK; ++i) rc = enqueue_iteration(c, n, level);
-    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-    if (rc != GCVT_OK) return rc;
-    CK(ce);
-    ce = cudaGraphInstantiate(&c->chunk_exec, g, 0);
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < kChunk && le == cudaSuccess; ++i) {
+      le = launch_list(b, 1, c->stream);
+      if (le == cudaSuccess) le = launch_cells(b, 0, nullptr, c->stream);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return GCVT_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->chunk_exec, g, 0);
     cudaGraphDestroy(g);
-    CK(ce);
+    if (ie != cudaSuccess) {
+      c->chunk_exec = nullptr;
+      return GCVT_ERR_CUDA;
+    }
     c->chunk_n = n;
     c->chunk_level = level;
   }
@@ -138,24 +143,63 @@ int enqueue_chunk(gcvt_ctx *c, int n, int level) {
   return GCVT_OK;
 }
 
-// Bring the bitmaps to size n_new = 2 * cur_n (gcvt.cu:1036-1051).
+// Sites of level size n go to size 2n (gcvt.cu:1036-1051): zoom from the
+// current bitmap into the next one, clear the other two.
 int zoom_level(gcvt_ctx *c, int n) {
   int rc = pull_state(c);
   if (rc) return rc;
-  int p = c->st_host->parity;
-  size_t words2 = (size_t)(2 * n / kBand) * (2 * n);
-  CK(cudaMemsetAsync(c->bits[p ^ 1], 0, words2 * sizeof(uint64_t), c->stream));
-  CK(launch_zoom(c->bits[p], n, c->bits[p ^ 1], c->stream));
-  CK(cudaMemsetAsync(c->bits[p], 0, words2 * sizeof(uint64_t), c->stream));
-  c->st_host->parity = p ^ 1;
+  const int p = c->st_host->cur, q = (p + 1) % 3, r = (p + 2) % 3;
+  const size_t bytes2 = bits_words(2 * n) * sizeof(uint64_t);
+  CK(cudaMemsetAsync(c->bits[q], 0, bytes2, c->stream));
+  CK(launch_zoom(c->bits[p], n, c->bits[q], c->stream));
+  c->cover_valid = 0;
+  CK(cudaMemsetAsync(c->bits[p], 0, bytes2, c->stream));
+  CK(cudaMemsetAsync(c->bits[r], 0, bytes2, c->stream));
+  c->st_host->cur = q;
   return push_state(c);
+}
+
+// What the Lloyd kernel carries from one iteration to the next, set up for
+// the current sites of size n: the covering bound (label the sites, take the
+// largest pixel-to-owner distance over the density support), the site counts
+// of the current bitmap, zero counts for the next one, no window hints.
+int ensure_cover(gcvt_ctx *c, int n, int level) {
+  if (c->cover_valid) return GCVT_OK;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  const LevelBufs b = level_bufs(c, n, level);
+  CK(launch_summary(b, 0, c->stream));
+  CK(launch_rows(b, 0, c->stream));
+  CK(launch_cover(b, c->stream));
+  CK(launch_count(b, c->stream));
+  const size_t nlb = list_blocks(n);
+  CK(cudaMemsetAsync(c->counts[(c->st_host->cur + 1) % 3], 0, nlb * sizeof(unsigned), c->stream));
+  CK(cudaMemsetAsync(c->hint, 0, (size_t)n * n, c->stream));
+  c->cover_valid = 1;
+  return GCVT_OK;
+}
+
+// Initial half-size of the candidate window at a level: 2.5 mean cell radii
+// (mean cell area = density pixels / sites).  Only a starting guess: a cell
+// whose certificate fails grows its own window.
+int initial_window(gcvt_ctx *c, int level, int *w) {
+  unsigned long long pix = 0;
+  CK(cudaMemcpyAsync(&pix, c->sup_pixels + level, sizeof(pix), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const double per_site = c->sites > 0 ? (double)pix / c->sites : 64.0;
+  const int v = (int)std::ceil(2.5 * std::sqrt(per_site / 3.14159265358979));
+  *w = v < 2 ? 2 : (v > 1024 ? 1024 : v);
+  return GCVT_OK;
 }
 
 // Run one level until the device schedule stops it.  fixed > 0: exactly that
 // many iterations without the stop rule.
 int run_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter, int poll) {
-  int rc = pull_state(c);
+  int window = 0;
+  int rc = initial_window(c, level, &window);
   if (rc) return rc;
+  if ((rc = pull_state(c))) return rc;
   DevState &h = *c->st_host;
   h.level = level;
   h.stopped = 0;
@@ -163,23 +207,20 @@ int run_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter, int poll) 
   h.use_stop_rule = fixed > 0 ? 0 : 1;
   h.fixed_iters = fixed;
   h.max_iter = max_iter;
+  h.window = window;
   h.energy_scale = std::pow(4.0, level) / ((double)n * (double)n);
   h.done_blocks = 0;
-  rc = push_state(c);
-  if (rc) return rc;
+  if ((rc = push_state(c))) return rc;
   c->cur_n = n;
+  if ((rc = ensure_cover(c, n, level))) return rc;
   if (fixed > 0 && !poll) {
-    for (int done = 0; done < fixed; done += kChunk) {
-      rc = enqueue_chunk(c, n, level);
-      if (rc) return rc;
-    }
+    for (int done = 0; done < fixed; done += kChunk)
+      if ((rc = enqueue_chunk(c, n, level))) return rc;
     return GCVT_OK;
   }
   for (;;) {
-    rc = enqueue_chunk(c, n, level);
-    if (rc) return rc;
-    rc = pull_state(c);
-    if (rc) return rc;
+    if ((rc = enqueue_chunk(c, n, level))) return rc;
+    if ((rc = pull_state(c))) return rc;
     if (c->st_host->stopped) return GCVT_OK;
   }
 }
@@ -197,14 +238,64 @@ int copy_out(void *dst, const void *src, size_t bytes, int mem, cudaStream_t s) 
   return GCVT_OK;
 }
 
-int reset_schedule(gcvt_ctx *c, int parity) {
+int reset_schedule(gcvt_ctx *c) {
   DevState &h = *c->st_host;
   std::memset(&h, 0, sizeof(DevState));
-  h.parity = parity;
+  h.cur = 0;
   h.omega = 2.0f;           // gcvt.cu:1108
   h.last_energy = 1e18;     // gcvt.cu:1105
   h.max_iter = 0x7fffffff;
+  h.window = 8;
   return push_state(c);
+}
+
+// Density-side tables of one level: row support, row range and pixel count
+// of the nonzero density, fixed-site bitmap.
+int level_tables(gcvt_ctx *c, int n, int level) {
+  CK(launch_row_support(c->density[level], n, c->support[level], c->sup_range[level],
+                        c->sup_pixels + level, c->stream));
+  CK(launch_fixed_bits(c->mask, n, c->fixed_bits[level], c->stream));
+  return GCVT_OK;
+}
+
+// Build bitmap 0 from a device site grid of size n (pba2DInitializeInput's
+// site part), clear the other two, reset the schedule; reports whether the
+// grid is well formed and counts its sites.
+int build_sites(gcvt_ctx *c, const uint32_t *grid, int n, int *bad) {
+  const size_t bytes = bits_words(c->n_max) * sizeof(uint64_t);
+  for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(c->bits[k], 0, bytes, c->stream));
+  CK(cudaMemsetAsync(c->err, 0, 2 * sizeof(int), c->stream));
+  CK(launch_grid_to_bits(grid, n, c->bits[0], c->err, c->err + 1, c->stream));
+  int h[2] = {0, 0};
+  CK(cudaMemcpyAsync(h, c->err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  int rc = reset_schedule(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  c->cover_valid = 0;
+  *bad = h[0] != 0;
+  c->sites = h[1];
+  return GCVT_OK;
+}
+
+// Upload a site grid; a malformed grid is recorded and reported by the calls
+// that need the sites (gcvt_ctx_run validates its own coarse grid instead).
+int load_sites(gcvt_ctx *c, int n, const int16_t *voronoi, int mem) {
+  c->loaded = 0;
+  int rc = copy_in(c->input, voronoi, (size_t)n * n * sizeof(uint32_t), mem, c->stream);
+  if (rc) return rc;
+  int bad = 0;
+  if ((rc = build_sites(c, c->input, n, &bad))) return rc;
+  c->input_err = bad;
+  c->n = n;
+  c->cur_n = n;
+  c->loaded = 1;
+  return GCVT_OK;
+}
+
+int level_of(gcvt_ctx *c, int n) {
+  int level = 0;
+  while (level < 7 && (c->n >> level) != n) ++level;
+  return level;
 }
 
 }  // namespace
@@ -224,7 +315,7 @@ const char *gcvt_status_string(int status) {
   return "unknown status";
 }
 
-int gcvt_version(void) { return 10000; }
+int gcvt_version(void) { return 10100; }
 
 int gcvt_ctx_create(int n_max, gcvt_ctx **out) {
   if (!out) return GCVT_ERR_ARGUMENT;
@@ -238,49 +329,50 @@ int gcvt_ctx_create(int n_max, gcvt_ctx **out) {
   };
   if (cudaGetDevice(&c->device) != cudaSuccess) return fail(GCVT_ERR_CUDA);
   if (rows_configure() != cudaSuccess) return fail(GCVT_ERR_CUDA);
+  if (cells_configure() != cudaSuccess) return fail(GCVT_ERR_CUDA);
   c->n_max = n_max;
   const size_t nn = (size_t)n_max * n_max;
-  const size_t words = (size_t)(n_max / kBand) * n_max;
+  const size_t words = bits_words(n_max);
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(GCVT_ERR_CUDA);
   c->stream = c->own_stream;
-  auto dal = [&](void **p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
+  auto dal = [](void *p, size_t bytes) {
+    return cudaMalloc(reinterpret_cast<void **>(p), bytes) == cudaSuccess;
+  };
   bool ok = true;
-  c->dens_levels = 0;
   for (int l = 0; l < 8 && ok; ++l) {
-    int nl = n_max >> l;
+    const int nl = n_max >> l;
     if (nl < kMinN) break;
-    ok &= dal((void **)&c->density[l], (size_t)nl * nl * sizeof(float));
-    c->dens_levels = l + 1;
+    ok = ok && dal(&c->density[l], (size_t)nl * nl * sizeof(float));
+    ok = ok && dal(&c->support[l], (size_t)nl * sizeof(int2));
+    ok = ok && dal(&c->sup_range[l], sizeof(int2));
+    ok = ok && dal(&c->fixed_bits[l], bits_words(nl) * sizeof(uint64_t));
   }
-  ok = ok && dal((void **)&c->mask, nn);
-  ok = ok && dal((void **)&c->input, nn * sizeof(uint32_t));
-  ok = ok && dal((void **)&c->grid, nn * sizeof(uint32_t));
-  ok = ok && dal((void **)&c->bits[0], words * sizeof(uint64_t));
-  ok = ok && dal((void **)&c->bits[1], words * sizeof(uint64_t));
-  ok = ok && dal((void **)&c->prev, words * sizeof(int16_t));
-  ok = ok && dal((void **)&c->word_rank, words * sizeof(int));
-  ok = ok && dal((void **)&c->group_count, (size_t)(n_max / 32) * sizeof(int));
-  ok = ok && dal((void **)&c->group_offset, (size_t)(n_max / 32) * sizeof(int));
-  for (int l = 0; l < c->dens_levels && ok; ++l)
-    ok &= dal((void **)&c->fixed_bits[l], (size_t)((n_max >> l) / kBand) * (n_max >> l) * sizeof(uint64_t));
-  ok = ok && dal((void **)&c->next, words * sizeof(int16_t));
-  ok = ok && dal((void **)&c->mhi, nn * sizeof(float4));
-  ok = ok && dal((void **)&c->mlo, nn * sizeof(float4));
-  ok = ok && dal((void **)&c->st, sizeof(DevState));
-  ok = ok && dal((void **)&c->blk_energy, (size_t)update_blocks(n_max) * 2 * sizeof(float));
-  for (int l = 0; l < c->dens_levels && ok; ++l)
-    ok &= dal((void **)&c->support[l], (size_t)(n_max >> l) * sizeof(int2));
-  ok = ok && dal((void **)&c->err, sizeof(int));
+  ok = ok && dal(&c->sup_pixels, 8 * sizeof(unsigned long long));
+  ok = ok && dal(&c->mask, nn);
+  ok = ok && dal(&c->input, nn * sizeof(uint32_t));
+  ok = ok && dal(&c->grid, nn * sizeof(uint32_t));
+  for (int k = 0; k < 3; ++k) ok = ok && dal(&c->bits[k], words * sizeof(uint64_t));
+  ok = ok && dal(&c->prev, words * sizeof(int16_t));
+  ok = ok && dal(&c->next, words * sizeof(int16_t));
+  ok = ok && dal(&c->st, sizeof(DevState));
+  ok = ok && dal(&c->list, nn * sizeof(uint32_t));
+  for (int k = 0; k < 3; ++k) ok = ok && dal(&c->counts[k], list_blocks(n_max) * sizeof(unsigned));
+  ok = ok && dal(&c->hint, nn);
+  const size_t groups = cell_groups(n_max), slots = (groups + 63) / 64;
+  ok = ok && dal(&c->gslot, groups * sizeof(float4));
+  ok = ok && dal(&c->sslot, slots * sizeof(float4));
+  ok = ok && dal(&c->scnt, slots * sizeof(unsigned));
+  ok = ok && dal(&c->err, 2 * sizeof(int));
   if (!ok) return fail(GCVT_ERR_ALLOC);
-  if (cudaMallocHost((void **)&c->st_host, sizeof(DevState)) != cudaSuccess)
-    return fail(GCVT_ERR_ALLOC);
-  if (cudaMemsetAsync(c->mhi, 0, nn * sizeof(float4), c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->mlo, 0, nn * sizeof(float4), c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->bits[0], 0, words * sizeof(uint64_t), c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->bits[1], 0, words * sizeof(uint64_t), c->stream) != cudaSuccess)
+  if (cudaMemsetAsync(c->scnt, 0, slots * sizeof(unsigned), c->stream) != cudaSuccess)
     return fail(GCVT_ERR_CUDA);
-  if (reset_schedule(c, 0) != GCVT_OK) return fail(GCVT_ERR_CUDA);
+  if (cudaMallocHost(reinterpret_cast<void **>(&c->st_host), sizeof(DevState)) != cudaSuccess)
+    return fail(GCVT_ERR_ALLOC);
+  for (int k = 0; k < 3; ++k)
+    if (cudaMemsetAsync(c->bits[k], 0, words * sizeof(uint64_t), c->stream) != cudaSuccess)
+      return fail(GCVT_ERR_CUDA);
+  if (reset_schedule(c) != GCVT_OK) return fail(GCVT_ERR_CUDA);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(GCVT_ERR_CUDA);
   *out = c;
   return GCVT_OK;
@@ -290,23 +382,26 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   if (!c) return GCVT_ERR_ARGUMENT;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->chunk_exec) cudaGraphExecDestroy(c->chunk_exec);
-  for (int l = 0; l < 8; ++l) cudaFree(c->density[l]);
+  for (int l = 0; l < 8; ++l) {
+    cudaFree(c->density[l]);
+    cudaFree(c->support[l]);
+    cudaFree(c->sup_range[l]);
+    cudaFree(c->fixed_bits[l]);
+  }
+  cudaFree(c->sup_pixels);
   cudaFree(c->mask);
   cudaFree(c->input);
   cudaFree(c->grid);
-  cudaFree(c->bits[0]);
-  cudaFree(c->bits[1]);
+  for (int k = 0; k < 3; ++k) cudaFree(c->bits[k]);
   cudaFree(c->prev);
-  cudaFree(c->word_rank);
-  cudaFree(c->group_count);
-  cudaFree(c->group_offset);
-  for (int l = 0; l < 8; ++l) cudaFree(c->fixed_bits[l]);
   cudaFree(c->next);
-  cudaFree(c->mhi);
-  cudaFree(c->mlo);
   cudaFree(c->st);
-  cudaFree(c->blk_energy);
-  for (int l = 0; l < 8; ++l) cudaFree(c->support[l]);
+  cudaFree(c->list);
+  for (int k = 0; k < 3; ++k) cudaFree(c->counts[k]);
+  cudaFree(c->hint);
+  cudaFree(c->gslot);
+  cudaFree(c->sslot);
+  cudaFree(c->scnt);
   cudaFree(c->moments);
   cudaFree(c->err);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -321,34 +416,6 @@ int gcvt_ctx_set_stream(gcvt_ctx *c, void *stream) {
   return GCVT_OK;
 }
 
-}  // extern "C"
-
-namespace {
-// Upload a site grid and build the bitmap (pba2DInitializeInput's site part).
-int load_sites(gcvt_ctx *c, int n, const int16_t *voronoi, int mem) {
-  const size_t nn = (size_t)n * n;
-  const size_t words_max = (size_t)(c->n_max / kBand) * c->n_max;
-  int rc;
-  c->loaded = 0;
-  if ((rc = copy_in(c->input, voronoi, nn * sizeof(uint32_t), mem, c->stream))) return rc;
-  CK(cudaMemsetAsync(c->bits[0], 0, words_max * sizeof(uint64_t), c->stream));
-  CK(cudaMemsetAsync(c->bits[1], 0, words_max * sizeof(uint64_t), c->stream));
-  CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-  CK(launch_grid_to_bits(c->input, n, c->bits[0], c->err, c->stream));
-  int herr = 0;
-  CK(cudaMemcpyAsync(&herr, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  if ((rc = reset_schedule(c, 0))) return rc;
-  CK(cudaStreamSynchronize(c->stream));
-  c->input_err = herr != 0;
-  c->n = n;
-  c->cur_n = n;
-  c->loaded = 1;
-  return GCVT_OK;
-}
-}  // namespace
-
-extern "C" {
-
 int gcvt_ctx_load(gcvt_ctx *c, int n, const int16_t *voronoi, const float *density,
                   const uint8_t *mask, int mem) {
   if (!c || !voronoi || !density) return GCVT_ERR_ARGUMENT;
@@ -358,13 +425,12 @@ int gcvt_ctx_load(gcvt_ctx *c, int n, const int16_t *voronoi, const float *densi
   int rc;
   c->loaded = 0;
   if ((rc = copy_in(c->density[0], density, nn * sizeof(float), mem, c->stream))) return rc;
-  CK(launch_row_support(c->density[0], n, c->support[0], c->stream));
   if (mask) {
     if ((rc = copy_in(c->mask, mask, nn, mem, c->stream))) return rc;
   } else {
     CK(cudaMemsetAsync(c->mask, 0, nn, c->stream));
   }
-  CK(launch_fixed_bits(c->mask, n, c->fixed_bits[0], c->stream));
+  if ((rc = level_tables(c, n, 0))) return rc;
   return load_sites(c, n, voronoi, mem);
 }
 
@@ -374,9 +440,9 @@ int gcvt_ctx_label(gcvt_ctx *c, int16_t *labels, int mem) {
   if (!c->loaded) return GCVT_ERR_STATE;
   if (c->input_err) return GCVT_ERR_INPUT;
   const int n = c->cur_n;
-  LevelBufs b = level_bufs(c, n, 0);
+  const LevelBufs b = level_bufs(c, n, level_of(c, n));
   CK(launch_summary(b, 0, c->stream));
-  CK(launch_rows(b, 1 /*labels*/, 0, c->stream));
+  CK(launch_rows(b, 0, c->stream));
   return copy_out(labels, c->grid, (size_t)n * n * sizeof(uint32_t), mem, c->stream);
 }
 
@@ -397,25 +463,17 @@ int gcvt_ctx_run(gcvt_ctx *c, int depth, int max_iter, gcvt_run_info *info) {
   for (int i = 0; i < depth; ++i)       // gcvt.cu:1091
     if ((size >> i) < 256) { depth = i; break; }
   int rc;
-  // density pyramid (gcvt.cu:985-993)
+  // density pyramid (gcvt.cu:985-993) and its tables
   for (int l = 1; l < depth; ++l) {
     CK(launch_density_halve(c->density[l - 1], c->density[l], size >> l, c->stream));
-    CK(launch_row_support(c->density[l], size >> l, c->support[l], c->stream));
-    CK(launch_fixed_bits(c->mask, size >> l, c->fixed_bits[l], c->stream));
+    if ((rc = level_tables(c, size >> l, l))) return rc;
   }
   // the coarsest grid is the first (size >> (depth-1))^2 entries of the loaded
   // array (gcvt.cu:1099-1103)
   const int n0 = size >> (depth - 1);
-  const size_t words_max = (size_t)(c->n_max / kBand) * c->n_max;
-  CK(cudaMemsetAsync(c->bits[0], 0, words_max * sizeof(uint64_t), c->stream));
-  CK(cudaMemsetAsync(c->bits[1], 0, words_max * sizeof(uint64_t), c->stream));
-  CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-  CK(launch_grid_to_bits(c->input, n0, c->bits[0], c->err, c->stream));
-  int herr = 0;
-  CK(cudaMemcpyAsync(&herr, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  if ((rc = reset_schedule(c, 0))) return rc;
-  CK(cudaStreamSynchronize(c->stream));
-  if (herr) return GCVT_ERR_INPUT;
+  int bad = 0;
+  if ((rc = build_sites(c, c->input, n0, &bad))) return rc;
+  if (bad) return GCVT_ERR_INPUT;
   c->input_err = 0;
   c->cur_n = n0;
   int levels = 0;
@@ -440,7 +498,7 @@ int gcvt_ctx_sites(gcvt_ctx *c, int16_t *voronoi, int mem) {
   int rc = pull_state(c);
   if (rc) return rc;
   const int n = c->cur_n;
-  CK(launch_bits_to_grid(c->bits[c->st_host->parity], n, c->grid, c->stream));
+  CK(launch_bits_to_grid(c->bits[c->st_host->cur], n, c->grid, c->stream));
   return copy_out(voronoi, c->grid, (size_t)n * n * sizeof(uint32_t), mem, c->stream);
 }
 
@@ -450,13 +508,22 @@ int gcvt_ctx_moments(gcvt_ctx *c, double *out4, int mem) {
   if (!c->loaded) return GCVT_ERR_STATE;
   if (c->input_err) return GCVT_ERR_INPUT;
   const int n = c->cur_n;
-  if (!c->moments) CK(cudaMalloc((void **)&c->moments, (size_t)4 * c->n_max * c->n_max * sizeof(double)));
-  int level = 0;
-  while ((c->n >> level) != n && level < 7) ++level;
-  LevelBufs b = level_bufs(c, n, level);
-  CK(launch_summary(b, 0, c->stream));
-  CK(launch_rows(b, 0 /*lloyd*/, 0, c->stream));
-  CK(launch_read_moments(b, c->moments, c->stream));
+  const int level = level_of(c, n);
+  if (!c->moments &&
+      cudaMalloc(reinterpret_cast<void **>(&c->moments),
+                 (size_t)4 * c->n_max * c->n_max * sizeof(double)) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  int window = 0;
+  int rc = initial_window(c, level, &window);
+  if (rc) return rc;
+  if ((rc = pull_state(c))) return rc;
+  c->st_host->window = window;
+  if ((rc = push_state(c))) return rc;
+  if ((rc = ensure_cover(c, n, level))) return rc;
+  CK(cudaMemsetAsync(c->moments, 0, (size_t)4 * n * n * sizeof(double), c->stream));
+  const LevelBufs b = level_bufs(c, n, level);
+  CK(launch_list(b, 0, c->stream));
+  CK(launch_cells(b, 1, c->moments, c->stream));
   return copy_out(out4, c->moments, (size_t)4 * n * n * sizeof(double), mem, c->stream);
 }
 
@@ -473,42 +540,59 @@ int gcvt_ctx_info(gcvt_ctx *c, gcvt_run_info *info) {
   return GCVT_OK;
 }
 
+// Mean device time of (one Lloyd iteration: site list + cells, one labelling
+// pass) over `iterations` iterations at full resolution, each bracketed by
+// events on the context's stream; ms3[2] is 0.  The sites move as in
+// gcvt_ctx_iterate.
 int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
   if (!c || !ms3 || iterations < 1) return GCVT_ERR_ARGUMENT;
   if (!c->loaded) return GCVT_ERR_STATE;
   if (c->input_err) return GCVT_ERR_INPUT;
   if (c->cur_n != c->n) return GCVT_ERR_STATE;
-  int rc = pull_state(c);
+  int window = 0;
+  int rc = initial_window(c, 0, &window);
   if (rc) return rc;
+  if ((rc = pull_state(c))) return rc;
   DevState &h = *c->st_host;
   h.level = 0;
   h.stopped = 0;
   h.level_iters = 0;
   h.use_stop_rule = 0;
   h.fixed_iters = 0x7fffffff;
+  h.window = window;
   h.energy_scale = 1.0 / ((double)c->n * (double)c->n);
   if ((rc = push_state(c))) return rc;
-  cudaEvent_t ev[4];
-  for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
-  float acc[3] = {0.f, 0.f, 0.f};
-  LevelBufs b = level_bufs(c, c->n, 0);
-  for (int it = 0; it < iterations; ++it) {
-    CK(cudaEventRecord(ev[0], c->stream));
-    CK(launch_summary(b, 1, c->stream));
-    CK(cudaEventRecord(ev[1], c->stream));
-    CK(launch_rows(b, 0, 1, c->stream));
-    CK(cudaEventRecord(ev[2], c->stream));
-    CK(launch_update(b, c->stream));
-    CK(cudaEventRecord(ev[3], c->stream));
-    CK(cudaEventSynchronize(ev[3]));
-    for (int k = 0; k < 3; ++k) {
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
-      acc[k] += ms;
+  if ((rc = ensure_cover(c, c->n, 0))) return rc;
+  cudaEvent_t ev[3] = {};
+  for (int i = 0; i < 3; ++i)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaEventDestroy(ev[j]);
+      return GCVT_ERR_CUDA;
     }
+  float acc[2] = {0.f, 0.f};
+  const LevelBufs b = level_bufs(c, c->n, 0);
+  int status = GCVT_OK;
+  for (int it = 0; it < iterations && status == GCVT_OK; ++it) {
+    float ms0 = 0.f, ms1 = 0.f;
+    if (cudaEventRecord(ev[0], c->stream) != cudaSuccess ||
+        launch_list(b, 1, c->stream) != cudaSuccess ||
+        launch_cells(b, 0, nullptr, c->stream) != cudaSuccess ||
+        cudaEventRecord(ev[1], c->stream) != cudaSuccess ||
+        launch_summary(b, 0, c->stream) != cudaSuccess ||
+        launch_rows(b, 0, c->stream) != cudaSuccess ||
+        cudaEventRecord(ev[2], c->stream) != cudaSuccess ||
+        cudaEventSynchronize(ev[2]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms0, ev[0], ev[1]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms1, ev[1], ev[2]) != cudaSuccess)
+      status = GCVT_ERR_CUDA;
+    acc[0] += ms0;
+    acc[1] += ms1;
   }
-  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
-  for (int k = 0; k < 3; ++k) ms3[k] = acc[k] / iterations;
+  for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
+  if (status) return status;
+  ms3[0] = acc[0] / iterations;
+  ms3[1] = acc[1] / iterations;
+  ms3[2] = 0.f;
   return GCVT_OK;
 }
 

@@ -1,0 +1,690 @@
+// cells.cu -- one Lloyd iteration as two launches: k_list lays the current
+// sites out in bitmap order, then k_cell lets every site compute its own
+// Voronoi cell exactly, sum the density moments over it, and move.
+//
+// In a Lloyd iteration the labels themselves are never needed, only each
+// site's sums over its cell (gcvt.cu:1008-1023) and the energy
+// (gcvt.cu:1059-1083).  The PBA+ labelling (labeller.cu) is a total order per
+// pixel -- nearest site, then smaller x, then the 64-row band rule for a mirror
+// pair -- so "pixel p belongs to site s" is "s beats every other site t at p".
+// In coordinates relative to s (p = s + (u, v), t = s + (A, B)):
+//     |p - s|^2 - |p - t|^2 = 2Au + 2Bv - (A^2 + B^2)
+//     A > 0 (t right of s, s wins ties):   u <= floor(N / 2A)
+//     A < 0 (t left of s, t wins ties):    u >= floor(N / 2A) + 1
+//     A = 0 (same column): row v is s's iff B (2v - B) < 0, or = 0 and the
+//                          band rule picks s,
+// with N = A^2 + B^2 - 2Bv, exact in 32-bit integers.  The cell is the
+// intersection, one interval per row.
+//
+// Candidates t come from the site bitmap in the disc of radius W around s.
+// Certificate: if every summed pixel lies within R of s and 2R <= W, no site
+// outside the disc can beat s there (|p - t| > W - R >= R); otherwise the
+// window grows (W <- min(2R + 1, 2W)) and the cell is redone; a window
+// covering the grid is exact by construction.  The starting W of a site is
+// the hint its predecessor left at its pixel (2R + 3 of the cell it had).
+//
+// Rows are visited outward from s.  A row may hold no pixel of the cell while
+// a row further out does (a sliver narrower than a pixel), so the walk ends
+// only when lo > hi + 1: then the largest lower cut is at least lo - 1 >= hi + 1,
+// above the smallest upper cut (< hi + 1), so the real chord of the convex
+// cell is empty, and so is every chord further from s.
+//
+// Covering bound.  A cell at the domain boundary is open towards the empty
+// region, so its row walk alone would cross the whole grid.  Every density
+// pixel p lies within `cover` of its owner (DevState::cover), so only pixels
+// with |p - s| <= cover can be s's: the walk stays in that disc and the
+// window never needs to exceed 2 cover.  The bound carries itself from one
+// iteration to the next: if the pixel p was within R of its owner s and s
+// moved by d, p is within R + d of the site now at s's new pixel (a merged
+// site leaves another at that pixel), so cover' = ceil(sqrt(max R^2)) +
+// ceil(sqrt(max d^2)), both maxima taken over this iteration's cells.  The
+// first iteration of a level takes it from a label grid (k_cover).
+//
+// Work split.  k_cell runs one warp per block, as many blocks as fit on the
+// GPU; each warp takes the next group of 32 listed sites from a ticket, one
+// site per lane.  A lane keeps its site's candidates as 8-byte records and
+// bounds two rows per pass over them.  The energy is reduced in a fixed order
+// whatever warp takes which group: the sites of a group by a butterfly, 64
+// groups by the warp finishing the last of them, the 64-group totals by the
+// warp finishing the last 64-group; that warp also runs the schedule.  Sites move by atomicOr into the next bitmap;
+// the first to set a bit also counts it for the next k_list.
+#include "gcvt_internal.cuh"
+
+namespace cvtgb {
+
+constexpr int kMaxCand = 32;  // candidate records per site; more: streamed
+constexpr int kGroupsPerSlot = 64;
+
+__device__ __forceinline__ void tsum_c(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  float bp = __fsub_rn(s, a);
+  float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// (ah, al) += (bh, bl), two-float.  Commutative: the error term of TwoSum is
+// exact, so both lanes of a butterfly get the same result.
+__device__ __forceinline__ void dfa(float &ah, float &al, float bh, float bl) {
+  float s, e;
+  tsum_c(ah, bh, s, e);
+  e = __fadd_rn(e, __fadd_rn(al, bl));
+  ah = __fadd_rn(s, e);
+  al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
+// (ah, al) += k * (bh, bl) for a small integer k (exact product via fma).
+__device__ __forceinline__ void dfa_scaled(float &ah, float &al, float k, float bh, float bl) {
+  const float ph = __fmul_rn(k, bh);
+  const float pl = __fmaf_rn(k, bh, -ph) + k * bl;
+  dfa(ah, al, ph, pl);
+}
+
+// floor(sqrt(v)) and ceil(sqrt(v)) for 0 <= v < 2^30, exact.
+__device__ __forceinline__ int isqrt_floor(int v) {
+  int h = (int)sqrtf((float)v);
+  while (h * h > v) --h;
+  while ((h + 1) * (h + 1) <= v) ++h;
+  return h;
+}
+__device__ __forceinline__ int isqrt_ceil(int v) {
+  const int h = isqrt_floor(v);
+  return h * h == v ? h : h + 1;
+}
+
+// floor(N / D) for D > 0, exact: from a float estimate when |N| < 2^24 (then
+// the estimate is within 1 of it), else by integer division.
+__device__ __forceinline__ int floordiv_est(int N, int D, float inv, bool fast) {
+  if (fast) {
+    int q = __float2int_rd(__fmul_rn((float)N, inv));
+    const int r = N - q * D;
+    q += (r >= D) - (r < 0);
+    return q;
+  }
+  int q = N / D;
+  if ((N % D != 0) && (N < 0)) --q;
+  return q;
+}
+
+// Row-v bounds from the site t = s + (A, B), A != 0, when the candidates do
+// not fit the record list (same-column sites are already row limits).
+__device__ __forceinline__ void constrain_rel(int A, int B, int v, int &lo, int &hi) {
+  if (A == 0) return;
+  const int N = A * A + B * B - 2 * B * v;
+  if (A > 0) hi = min(hi, floordiv_est(N, 2 * A, 0.f, false));
+  else lo = max(lo, floordiv_est(-N, -2 * A, 0.f, false) + 1);
+}
+
+__device__ __forceinline__ uint64_t row_mask(int lo_i, int hi_i) {  // bits lo_i..hi_i
+  const uint64_t up = hi_i >= 63 ? ~0ull : ((2ull << hi_i) - 1ull);
+  return up & ~((1ull << lo_i) - 1ull);
+}
+
+struct CellSums {
+  float wh, wl, xh, xl, yh, yl, eh, el;  // W, SX, SY (relative to the site), E
+  int r2;                                // max |p - s|^2 over the summed pixels
+};
+
+// floor(N / D), D > 0, |N| < 2^23, given r ~ 1/D from rcp.approx (at most 1
+// ulp off): the estimate is within 1, one exact correction fixes it.
+__device__ __forceinline__ int floordiv_r(int N, int D, float r) {
+  int q = __float2int_rd(__fmul_rn((float)N, r));
+  const int rem = N - q * D;
+  q += (rem >= D) - (rem < 0);
+  return q;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Bounds of rows v0 and v0 + dir (relative to s) in one pass over the
+// records.  A record {K, S | D << 16} bounds row v by floor((K - S v) / |D|):
+// an upper bound when D > 0, a lower one (+1) when D < 0.  When the records
+// did not hold every candidate, the candidates are read from the bitmap.
+struct RowPair {
+  int lo0, hi0, lo1, hi1;
+};
+
+__device__ __forceinline__ RowPair row_bounds2(const int2 *rec, int cnt, bool ovf, bool fast,
+                                               const uint64_t *__restrict__ bits, int n, int sx,
+                                               int sy, int x0, int x1, int b0, int b1, int y0,
+                                               int y1, long long Wc, int v0, int dir) {
+  RowPair p{-sx, n - 1 - sx, -sx, n - 1 - sx};
+  const int v1 = v0 + dir;
+  if (!ovf) {
+    for (int k = 0; k < cnt; ++k) {
+      const int2 r = rec[k];
+      const int S = (int)(int16_t)((unsigned)r.y & 0xffffu);
+      const int D = (int)(int16_t)((unsigned)r.y >> 16);
+      const int aD = abs(D);
+      const int N0 = r.x - S * v0, N1 = N0 - S * dir;
+      int q0, q1;
+      if (fast) {
+        const float rr = rcp_approx((float)aD);
+        q0 = floordiv_r(N0, aD, rr);
+        q1 = floordiv_r(N1, aD, rr);
+      } else {
+        q0 = floordiv_est(N0, aD, 0.f, false);
+        q1 = floordiv_est(N1, aD, 0.f, false);
+      }
+      if (D > 0) {
+        p.hi0 = min(p.hi0, q0);
+        p.hi1 = min(p.hi1, q1);
+      } else {
+        p.lo0 = max(p.lo0, q0 + 1);
+        p.lo1 = max(p.lo1, q1 + 1);
+      }
+    }
+    return p;
+  }
+  for (int x = x0; x <= x1; ++x)
+    for (int b = b0; b <= b1; ++b) {
+      uint64_t w = __ldg(bits + (size_t)b * n + x) &
+                   row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63));
+      while (w) {
+        const int i = __ffsll((long long)w) - 1;
+        w &= w - 1ull;
+        const int A = x - sx, B = 64 * b + i - sy;
+        const int K = A * A + B * B;
+        if (K == 0 || (long long)K > Wc) continue;
+        constrain_rel(A, B, v0, p.lo0, p.hi0);
+        constrain_rel(A, B, v1, p.lo1, p.hi1);
+      }
+    }
+  return p;
+}
+
+// Sums of row v = [da, db] (relative columns) into c.
+__device__ __forceinline__ void row_sums(const float *__restrict__ row, int da, int db, int v,
+                                         CellSums &c) {
+  float rw = 0.f, rwl = 0.f, rx = 0.f, rxl = 0.f, rq = 0.f;
+  float dx = (float)da;
+  for (int u = da; u <= db; ++u, dx += 1.0f) {
+    const float rho = __ldg(row + u);
+    float s1, e1;
+    tsum_c(rw, rho, s1, e1);
+    rw = s1;
+    rwl = __fadd_rn(rwl, e1);
+    const float pr = __fmul_rn(dx, rho);
+    const float pe = __fmaf_rn(dx, rho, -pr);
+    tsum_c(rx, pr, s1, e1);
+    rx = s1;
+    rxl = __fadd_rn(rxl, __fadd_rn(e1, pe));
+    rq = __fmaf_rn(__fmul_rn(dx, dx), rho, rq);
+  }
+  dfa(c.wh, c.wl, rw, rwl);
+  dfa(c.xh, c.xl, rx, rxl);
+  dfa_scaled(c.yh, c.yl, (float)v, rw, rwl);
+  float qh = rq, ql = 0.f;
+  dfa_scaled(qh, ql, (float)(v * v), rw, rwl);
+  dfa(c.eh, c.el, qh, ql);
+}
+
+// Row v of the cell with bounds [lo, hi]: clip to the density support and
+// the covering disc, sum it, track R2.
+__device__ __forceinline__ void take_row(const LevelBufs &a, int n, int sx, int sy, int rb2, int v,
+                                         int lo, int hi, int &R2, CellSums &c) {
+  const int y = sy + v;
+  const int2 s = a.support[y];
+  const int hx = isqrt_floor(rb2 - v * v);
+  const int da = max(max(lo, s.x - sx), -hx), db = min(min(hi, s.y - 1 - sx), hx);
+  if (da > db) return;
+  R2 = max(R2, max(da * da, db * db) + v * v);
+  row_sums(a.density + (size_t)y * n + sx, da, db, v, c);
+}
+
+// Exact cell of site (sx, sy) and its sums.  bits: current site bitmap;
+// W: initial window radius; rb: the covering bound.
+__device__ CellSums cell_sums(const LevelBufs &a, const uint64_t *__restrict__ bits, int n, int sx,
+                              int sy, int W, int rb) {
+  int2 rec[kMaxCand];  // {K, S | D << 16} of the window's candidates
+  const int2 yr = *a.sup_range;  // rows [yr.x, yr.y) hold every nonzero density
+  const int vlo_sup = max(yr.x, sy - rb) - sy, vhi_sup = min(yr.y - 1, sy + rb) - sy;
+  const int rb2 = rb * rb;
+  W = max(1, min(W, 2 * rb));
+  CellSums c;
+  for (;;) {
+    const int x0 = max(0, sx - W), x1 = min(n - 1, sx + W);
+    const int y0 = max(0, sy - W), y1 = min(n - 1, sy + W);
+    const bool whole = x0 == 0 && y0 == 0 && x1 == n - 1 && y1 == n - 1;
+    const int b0 = y0 >> 6, b1 = y1 >> 6;
+    const long long W2 = (long long)W * W;
+    // candidates: the disc of radius W, or every site when the window holds
+    // the grid (no certificate needed then)
+    const long long Wc = whole ? (1ll << 62) : W2;
+    int cnt = 0;
+    bool ovf = false;
+    int vmin = vlo_sup, vmax = vhi_sup;  // row limits, same-column sites folded in
+    for (int x = x0; x <= x1; ++x) {
+      const int A = x - sx;
+      for (int b = b0; b <= b1; ++b) {
+        uint64_t w = __ldg(bits + (size_t)b * n + x) &
+                     row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63));
+        while (w) {
+          const int i = __ffsll((long long)w) - 1;
+          w &= w - 1ull;
+          const int B = 64 * b + i - sy;
+          const int K = A * A + B * B;
+          if (K == 0 || (long long)K > Wc) continue;  // s itself; outside the disc
+          if (A == 0) {
+            // same column: s keeps the rows strictly on its side of the
+            // mirror row, and the mirror row (B even) if the band rule says so
+            if (B > 0) {
+              int m = (B - 1) >> 1;
+              if (!(B & 1) && (((sy + B) >> 6) != ((sy + B / 2) >> 6))) m = B / 2;
+              vmax = min(vmax, m);
+            } else {
+              int m = -((-B - 1) >> 1);
+              if (!(B & 1) && ((sy >> 6) == ((sy + B / 2) >> 6))) m = B / 2;
+              vmin = max(vmin, m);
+            }
+            continue;
+          }
+          if (cnt >= kMaxCand) {
+            ovf = true;
+            continue;
+          }
+          // |S|, |D| <= 2 (n - 1) fit 16 bits
+          const int S = A > 0 ? 2 * B : -2 * B;
+          rec[cnt++] = make_int2(A > 0 ? K : -K,
+                                 (int)(((unsigned)S & 0xffffu) | ((unsigned)(2 * A) << 16)));
+        }
+      }
+    }
+    // |K - S v| <= 2 W^2 + 2 W rb: below 2^23 the reciprocal estimate is safe
+    const bool fast = 2 * W2 + 2 * (long long)W * rb < (1ll << 23);
+    c = CellSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+    int R2 = 0;
+    // rows outward from s, two per pass over the records: up from v = 0, down
+    // from v = -1, inside the row limits
+    for (int dir = 1; dir >= -1; dir -= 2) {
+      const int vend = dir > 0 ? vmax : vmin;
+      for (int v = dir > 0 ? max(0, vmin) : min(-1, vmax); dir > 0 ? v <= vend : v >= vend;
+           v += 2 * dir) {
+        const RowPair p =
+            row_bounds2(rec, cnt, ovf, fast, bits, n, sx, sy, x0, x1, b0, b1, y0, y1, Wc, v, dir);
+        if (p.lo0 > p.hi0 + 1) break;  // the cell has ended in this direction
+        if (p.lo0 <= p.hi0) take_row(a, n, sx, sy, rb2, v, p.lo0, p.hi0, R2, c);
+        const int v1 = v + dir;
+        if ((dir > 0 ? v1 > vend : v1 < vend) || p.lo1 > p.hi1 + 1) break;
+        if (p.lo1 <= p.hi1) take_row(a, n, sx, sy, rb2, v1, p.lo1, p.hi1, R2, c);
+      }
+    }
+    c.r2 = R2;
+    // R2 <= rb^2, so a window of 2 rb always passes
+    if (whole || 4 * (long long)R2 <= W2) return c;
+    W = min(min(2 * isqrt_ceil(R2) + 1, 2 * W), 2 * rb);
+  }
+}
+
+// Centroid coordinate base + (Sh + Sl) / (Wh + Wl), rounded once to float
+// (two-float quotient; W = 0 gives NaN as the reference's 0/0 does).
+__device__ __forceinline__ float cell_centroid(int base, float Sh, float Sl, float Wh, float Wl) {
+  const float q = __fdiv_rn(Sh, Wh);
+  const float rr = __fadd_rn(__fmaf_rn(-q, Wh, Sh), __fmaf_rn(-q, Wl, Sl));
+  const float q2 = __fdiv_rn(rr, Wh);
+  float s, e;
+  tsum_c((float)base, q, s, e);
+  return __fadd_rn(s, __fadd_rn(e, q2));
+}
+
+__device__ __forceinline__ uint64_t *bits_at(const LevelBufs &a, int k) {
+  return k == 0 ? a.bits[0] : (k == 1 ? a.bits[1] : a.bits[2]);
+}
+__device__ __forceinline__ unsigned *counts_at(const LevelBufs &a, int k) {
+  return k == 0 ? a.counts[0] : (k == 1 ? a.counts[1] : a.counts[2]);
+}
+
+// Warp reduction of (energy two-float, max r2, max move2) in a fixed order.
+__device__ __forceinline__ void warp_reduce(float &eh, float &el, unsigned &r2, unsigned &mv) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, eh, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, el, o);
+    dfa(eh, el, oh, ol);
+  }
+  r2 = __reduce_max_sync(0xffffffffu, r2);
+  mv = __reduce_max_sync(0xffffffffu, mv);
+}
+
+// The gCVT schedule after an iteration of energy E (gcvt.cu:1105-1142), the
+// next covering bound, and the rotation of the bitmaps.
+__device__ void run_schedule(DevState *st, double E, unsigned r2, unsigned mv, int n, int cur) {
+  st->energy = E;
+  const int i = st->iter;
+  if (i % 10 == 0) st->sampled = E;          // gcvt.cu:1116-1117
+  st->iter = i + 1;                          // gcvt.cu:1123
+  st->level_iters += 1;
+  int stop = 0;
+  if ((i + 1) % 10 == 0) {                   // gcvt.cu:1125-1140
+    const double diff = st->last_energy - st->sampled;
+    const double grad = diff / 10.0;
+    st->omega = (float)fmin(2.0, 1.0 + diff);
+    if (st->use_stop_rule && (st->level ? grad < 3e-1 : grad < 1e-5)) stop = 1;
+    else st->last_energy = st->sampled;
+  }
+  if (st->use_stop_rule ? (st->iter >= st->max_iter) : (st->level_iters >= st->fixed_iters))
+    stop = 1;                                // gcvt.cu:1142
+  if (stop) st->stopped = 1;
+  st->cover = min(isqrt_ceil((int)r2) + isqrt_ceil((int)mv), 2 * n);
+  st->cur = cur == 2 ? 0 : cur + 1;
+  st->done_blocks = 0;
+  __threadfence();
+}
+
+// MODE 0: one Lloyd iteration (sums, move, energy, schedule).
+// MODE 1: sums only, written as doubles (W, X, Y, E) at each site pixel of
+//         out4 (four n*n planes); the sites do not move.
+template <int MODE>
+__global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
+  DevState *st = a.st;
+  if (MODE == 0 && st->stopped) return;
+  const int n = a.n;
+  const int lane = threadIdx.x;
+  const int cur = st->cur;
+  const uint64_t *bits = bits_at(a, cur);
+  uint64_t *nxt = bits_at(a, cur == 2 ? 0 : cur + 1);
+  unsigned *cnt_nxt = counts_at(a, cur == 2 ? 0 : cur + 1);
+  const float omega = st->omega;
+  const int W0 = st->window;
+  const int rb = st->cover;
+  const int nsites = st->list_count;
+  const unsigned ngroups = (unsigned)(nsites + 31) / 32;
+  if (MODE == 0) {
+    // the buffers the next iteration writes; nobody reads them now
+    const size_t nwords = (size_t)(n / kBand) * n;
+    const size_t gthreads = (size_t)gridDim.x * 32;
+    uint64_t *zro = bits_at(a, cur == 0 ? 2 : cur - 1);
+    unsigned *czro = counts_at(a, cur == 0 ? 2 : cur - 1);
+    const size_t t0 = (size_t)blockIdx.x * 32 + lane;
+    for (size_t i = t0; i < nwords; i += gthreads) zro[i] = 0ull;
+    const size_t nlb = (nwords + kListWords - 1) / kListWords;
+    for (size_t i = t0; i < nlb; i += gthreads) czro[i] = 0u;
+    if (ngroups == 0) {  // no sites: the schedule still advances
+      if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, n, cur);
+      return;
+    }
+  }
+  for (;;) {
+    unsigned g = 0;
+    if (lane == 0) g = atomicAdd(&st->ticket, 1u);
+    g = __shfl_sync(0xffffffffu, g, 0);
+    if (g >= ngroups) break;
+    float eh = 0.f, el = 0.f;
+    unsigned r2 = 0, mv = 0;
+    const int idx = (int)g * 32 + lane;
+    if (idx < nsites) {
+      const uint32_t e = a.list[idx];
+      const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
+      const size_t pid = (size_t)sy * n + sx;
+      const int h = a.hint[pid];
+      const CellSums cs = cell_sums(a, bits, n, sx, sy, h ? h : W0, rb);
+      if (MODE == 1) {
+        const size_t nn = (size_t)n * n;
+        const double Wd = (double)cs.wh + (double)cs.wl;
+        out4[pid] = Wd;
+        out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
+        out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
+        out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
+      } else {
+        dfa(eh, el, cs.eh, cs.el);
+        const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
+        const float cy = cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl);
+        const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)sx), omega, (float)sx), 0.5f);
+        const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)sy), omega, (float)sy), 0.5f);
+        int nx = min(max(__float2int_rz(fx), 0), n - 1);
+        int ny = min(max(__float2int_rz(fy), 0), n - 1);
+        if ((e & 0x8000u) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = sx; ny = sy; }
+        r2 = max(r2, (unsigned)cs.r2);
+        mv = max(mv, (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy)));
+        const size_t widx = (size_t)(ny / kBand) * n + nx;
+        const unsigned long long bit = 1ull << (ny % kBand);
+        const unsigned long long old =
+            atomicOr(reinterpret_cast<unsigned long long *>(nxt + widx), bit);
+        if (!(old & bit)) atomicAdd(cnt_nxt + widx / kListWords, 1u);
+        a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 3, 255);
+      }
+    }
+    __syncwarp();
+    if (MODE == 1) continue;
+    warp_reduce(eh, el, r2, mv);
+    // group total -> slot; the warp finishing the last group of a 64-group
+    // reduces the 64 slots; the warp finishing the last 64-group totals them
+    int last = 0;
+    const unsigned sg = g / kGroupsPerSlot;
+    const unsigned sbase = sg * kGroupsPerSlot;
+    const unsigned starget = min((unsigned)kGroupsPerSlot, ngroups - sbase);
+    if (lane == 0) {
+      a.gslot[g] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
+      __threadfence();
+      last = atomicAdd(a.scnt + sg, 1u) == starget - 1;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    __threadfence();
+    eh = el = 0.f;
+    r2 = mv = 0;
+    for (unsigned k = lane; k < starget; k += 32) {
+      const float4 v = __ldcg(a.gslot + sbase + k);
+      dfa(eh, el, v.x, v.y);
+      r2 = max(r2, __float_as_uint(v.z));
+      mv = max(mv, __float_as_uint(v.w));
+    }
+    warp_reduce(eh, el, r2, mv);
+    const unsigned nslots = (ngroups + kGroupsPerSlot - 1) / kGroupsPerSlot;
+    last = 0;
+    if (lane == 0) {
+      a.sslot[sg] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
+      a.scnt[sg] = 0u;
+      __threadfence();
+      last = atomicAdd(&st->done_blocks, 1u) == nslots - 1;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    __threadfence();
+    eh = el = 0.f;
+    r2 = mv = 0;
+    for (unsigned k = lane; k < nslots; k += 32) {
+      const float4 v = __ldcg(a.sslot + k);
+      dfa(eh, el, v.x, v.y);
+      r2 = max(r2, __float_as_uint(v.z));
+      mv = max(mv, __float_as_uint(v.w));
+    }
+    warp_reduce(eh, el, r2, mv);
+    if (lane == 0) run_schedule(st, ((double)eh + (double)el) * st->energy_scale, r2, mv, n, cur);
+  }
+}
+
+// Site list of the current bitmap in bitmap order (word by word, bits in
+// row order), with the fixed flag; block b covers words
+// [b kListWords, (b+1) kListWords) and finds its offset from the per-block
+// counts.  Also rearms the Lloyd kernel's ticket.
+__global__ void __launch_bounds__(256) k_list(LevelBufs a, int respect_stop) {
+  constexpr int kPer = kListWords / 256;
+  __shared__ unsigned wsum[8];
+  __shared__ unsigned base_s;
+  DevState *st = a.st;
+  if (respect_stop && st->stopped) return;
+  const int n = a.n;
+  const int cur = st->cur;
+  const uint64_t *bits = bits_at(a, cur);
+  const unsigned *counts = counts_at(a, cur);
+  const size_t nwords = (size_t)(n / kBand) * n;
+  const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+  if (blockIdx.x == 0 && tid == 0) {
+    st->ticket = 0u;
+    st->done_blocks = 0u;
+  }
+  // offset of this block: the counts of the blocks before it
+  unsigned pre = 0;
+  for (unsigned k = tid; k < blockIdx.x; k += 256) pre += counts[k];
+  pre = __reduce_add_sync(0xffffffffu, pre);
+  if (lane == 0) wsum[wib] = pre;
+  __syncthreads();
+  if (tid == 0) {
+    unsigned s = 0;
+    for (int k = 0; k < 8; ++k) s += wsum[k];
+    base_s = s;
+  }
+  __syncthreads();
+  const unsigned base = base_s;
+  // this thread's words and their sites
+  const size_t w0 = (size_t)blockIdx.x * kListWords + (size_t)tid * kPer;
+  uint64_t w[kPer];
+  unsigned cnt = 0;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    w[k] = (w0 + k < nwords) ? bits[w0 + k] : 0ull;
+    cnt += __popcll(w[k]);
+  }
+  // exclusive scan of cnt over the block
+  unsigned incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  __syncthreads();  // every thread has read base_s / wsum
+  if (lane == 31) wsum[wib] = incl;
+  __syncthreads();
+  unsigned woff = 0, total = 0;
+  for (int k = 0; k < 8; ++k) {
+    const unsigned v = wsum[k];
+    if (k < wib) woff += v;
+    total += v;
+  }
+  unsigned pos = base + woff + incl - cnt;
+  const unsigned cap = (unsigned)n * (unsigned)n;  // list capacity at this size
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    uint64_t word = w[k];
+    if (!word) continue;
+    const size_t t = w0 + k;
+    const int x = (int)(t % (unsigned)n), band = (int)(t / (unsigned)n);
+    const uint64_t fw = a.fixed_bits[t];
+    while (word) {
+      const int i = __ffsll((long long)word) - 1;
+      word &= word - 1ull;
+      if (pos < cap)
+        a.list[pos] = (uint32_t)x | ((uint32_t)(band * kBand + i) << 16) |
+                      ((uint32_t)((fw >> i) & 1ull) << 15);
+      ++pos;
+    }
+  }
+  if (blockIdx.x == gridDim.x - 1 && tid == 0) st->list_count = (int)min(base + total, cap);
+}
+
+// Per-block site counts of the current bitmap (for the first k_list of a
+// level; afterwards k_cell counts the sites it places).
+__global__ void __launch_bounds__(256) k_count(LevelBufs a) {
+  constexpr int kPer = kListWords / 256;
+  __shared__ unsigned wsum[8];
+  const int n = a.n;
+  const int cur = a.st->cur;
+  const uint64_t *bits = bits_at(a, cur);
+  unsigned *counts = counts_at(a, cur);
+  const size_t nwords = (size_t)(n / kBand) * n;
+  const size_t w0 = (size_t)blockIdx.x * kListWords + (size_t)threadIdx.x * kPer;
+  unsigned cnt = 0;
+  for (int k = 0; k < kPer; ++k)
+    if (w0 + k < nwords) cnt += __popcll(bits[w0 + k]);
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned s = 0;
+    for (int k = 0; k < 8; ++k) s += wsum[k];
+    counts[blockIdx.x] = s;
+  }
+}
+
+// Covering bound from a label grid: cover = ceil(sqrt(max |p - label(p)|^2))
+// over the pixels of the density's row support.  One block per row.
+__global__ void __launch_bounds__(256) k_cover(LevelBufs a) {
+  const int n = a.n, y = blockIdx.x;
+  const int2 yr = *a.sup_range;
+  unsigned m = 0;
+  if (y >= yr.x && y < yr.y) {
+    const int2 s = a.support[y];
+    const uint32_t *row = a.labels + (size_t)y * n;
+    for (int x = s.x + threadIdx.x; x < s.y; x += blockDim.x) {
+      const uint32_t v = row[x];
+      const int lx = (int16_t)(v & 0xffffu), ly = (int16_t)(v >> 16);
+      if (lx == kMarker) continue;  // no site at all
+      m = max(m, (unsigned)((x - lx) * (x - lx) + (y - ly) * (y - ly)));
+    }
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(&a.st->cover_acc, m);
+}
+
+__global__ void k_cover_finish(LevelBufs a) {
+  DevState *st = a.st;
+  st->cover = min(isqrt_ceil((int)st->cover_acc), 2 * a.n);
+  st->cover_acc = 0;
+}
+
+cudaError_t launch_cover(const LevelBufs &b, cudaStream_t s) {
+  k_cover<<<b.n, 256, 0, s>>>(b);
+  k_cover_finish<<<1, 1, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+size_t list_blocks(int n) {
+  const size_t nwords = (size_t)(n / kBand) * n;
+  return (nwords + kListWords - 1) / kListWords;
+}
+
+size_t cell_groups(int n) { return ((size_t)n * n + 31) / 32; }
+
+cudaError_t launch_list(const LevelBufs &b, int respect_stop, cudaStream_t s) {
+  k_list<<<(unsigned)list_blocks(b.n), 256, 0, s>>>(b, respect_stop);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count(const LevelBufs &b, cudaStream_t s) {
+  k_count<<<(unsigned)list_blocks(b.n), 256, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+// Persistent grid of the Lloyd kernel: every warp that fits, per device.
+static int g_cell_grid[64] = {};
+
+cudaError_t cells_configure() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (g_cell_grid[dev]) return cudaSuccess;
+  int sms = 0, per0 = 0, per1 = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return e;
+  // the candidate records live in local memory: shared memory only for the
+  // 1 KB the runtime reserves per block (32 blocks per SM), the rest as L1
+  const int carve = 15;
+  if ((e = cudaFuncSetAttribute(k_cell<0>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                carve)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(k_cell<1>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                carve)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, k_cell<0>, 32, 0)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_cell<1>, 32, 0)) != cudaSuccess)
+    return e;
+  g_cell_grid[dev] = sms * max(1, min(per0, per1));
+  return cudaSuccess;
+}
+
+cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
+  const int grid = g_cell_grid[dev];
+  if (moments_only) k_cell<1><<<grid, 32, 0, s>>>(b, out4);
+  else k_cell<0><<<grid, 32, 0, s>>>(b, out4);
+  return cudaGetLastError();
+}
+
+}  // namespace cvtgb

@@ -18,7 +18,7 @@ constexpr int kNoneBelow = 32767;   // "no site below"
 constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 for
                                     // every entry of gcvt.cu:842-847
 constexpr int kRowsPerBlock = 4;    // rows (one warp each) per row-pass block
-constexpr int kUpdateThreads = 256;
+constexpr int kListWords = 2048;   // bitmap words per site-list block
 constexpr int kMinN = 256;   // n must be a multiple of 256 (S = n/32 >= 8)
 constexpr int kMaxN = 8192;  // row-pass shared memory: 4 rows x 32 KB at 8192
 
@@ -26,20 +26,12 @@ __host__ __device__ inline uint32_t pack_xy(int x, int y) {
   return (uint32_t)(uint16_t)x | ((uint32_t)(uint16_t)y << 16);
 }
 
-// Slot of the site at (x, y): sites are numbered group by group (32 columns),
-// inside a group band by band and column by column, inside a word by row.
-__device__ __forceinline__ int site_slot(const uint64_t *bits, const int *word_rank,
-                                         const int *group_offset, int n, int x, int y) {
-  const size_t w = (size_t)(y >> 6) * n + x;
-  const uint64_t below = bits[w] & ((1ull << (y & 63)) - 1ull);
-  return group_offset[x >> 5] + word_rank[w] + __popcll(below);
-}
 
 // Per-context device state.  Kernels of one Lloyd iteration read it; the last
 // block of the update kernel advances it, so a whole iteration runs without a
 // host round trip and can be captured in a CUDA graph.
 struct DevState {
-  int parity;          // which site bitmap is current
+  int cur;             // which of the three site bitmaps holds the current sites
   int iter;            // Lloyd iterations completed (gcvtIterations)
   int level_iters;     // iterations completed at the current level
   int stopped;         // set when the level's loop condition ends it
@@ -47,7 +39,7 @@ struct DevState {
   int max_iter;        // total iteration cap (maxIter)
   int use_stop_rule;   // 1: energy stop rule of gcvt.cu:1125-1140; 0: fixed count
   int fixed_iters;     // iterations per level when use_stop_rule == 0
-  int error;           // input validation flags
+  int window;          // initial half-size of the candidate window (pixels)
   unsigned done_blocks;
   float omega;         // over-relaxation (pbaOmega)
   float pad0;
@@ -55,44 +47,59 @@ struct DevState {
   double sampled;      // Energy, sampled when iter % 10 == 0
   double energy;       // energy of the most recent iteration
   double energy_scale; // 4^level / n^2
+  int cover;           // bound on |p - owner(p)| over the density pixels p
+  unsigned cover_acc;  // max |p - owner(p)|^2 from the labels (k_cover)
+  int list_count;      // sites in the site list (k_list)
+  unsigned ticket;     // next 32-site group of the Lloyd kernel
 };
 
 // Buffers of one resolution level, passed by value to every kernel.
 struct LevelBufs {
   int n;
-  uint64_t *bits[2];       // site bitmaps [band][column], bit i = row 64*band+i
+  uint64_t *bits[3];       // site bitmaps [band][column], bit i = row 64*band+i;
+                           // the Lloyd kernel reads bits[cur], writes
+                           // bits[cur+1] and clears bits[cur+2] (mod 3)
   int16_t *prev;           // [band][column]: nearest site row above the band
   int16_t *next;           // [band][column]: nearest site row below the band
   const float *density;    // n*n
-  const uint8_t *fixed;    // full-resolution mask, indexed with this level's n
-                           // (only used to build fixed_bits)
-  float4 *mhi, *mlo;       // per-site compensated moments (W, SX, SY, E), SX and
-                           // SY relative to the site, indexed by the site's slot
-  uint64_t *fixed_bits;    // fixed sites of this level, same layout as bits
-  int *word_rank;          // [band][column]: sites in earlier words of the
-                           // column's 32-column group (band-major order)
-  int *group_count;        // per 32-column group: its number of sites
-  int *group_offset;       // exclusive prefix of group_count
-  uint32_t *labels;        // n*n label words (label passes only)
   const int2 *support;     // per row [first, last+1) of nonzero density
+  const int2 *sup_range;   // rows [x, y) containing every nonzero density
+  const uint64_t *fixed_bits;  // fixed sites of this level, same layout as bits
+  uint32_t *labels;        // n*n label words (label passes only)
   DevState *st;
-  float *blk_energy;       // one two-float partial per update block
+  uint32_t *list;          // current sites in bitmap order: x | fixed << 15 | y << 16
+  unsigned *counts[3];     // sites per kListWords words of bits[k]
+  uint8_t *hint;           // per pixel: window half-size for the site there
+  float4 *gslot;           // per 32-site group: energy (two-float), max cell
+                           // radius^2 and max move^2 (as bits)
+  float4 *sslot;           // per 64 groups: the same, reduced
+  unsigned *scnt;          // per 64 groups: groups finished
 };
 
-// Kernels (launch helpers in labeller.cu / lloyd.cu).
+__device__ __forceinline__ const uint64_t *cur_bits(const LevelBufs &a) {
+  const int c = a.st->cur;
+  return c == 0 ? a.bits[0] : (c == 1 ? a.bits[1] : a.bits[2]);
+}
+
+// Kernels (launch helpers in labeller.cu / lloyd.cu / cells.cu).
 cudaError_t launch_grid_to_bits(const uint32_t *grid, int n, uint64_t *bits, int *err,
-                                cudaStream_t s);
+                                int *count, cudaStream_t s);
 cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s);
 cudaError_t launch_summary(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, cudaStream_t s);
-cudaError_t launch_rows(const LevelBufs &b, int label_mode, int respect_stop, cudaStream_t s);
-cudaError_t launch_update(const LevelBufs &b, cudaStream_t s);
+cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s);
+cudaError_t launch_list(const LevelBufs &b, int respect_stop, cudaStream_t s);
+cudaError_t launch_count(const LevelBufs &b, cudaStream_t s);
+cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s);
 cudaError_t launch_zoom(const uint64_t *src, int n, uint64_t *dst, cudaStream_t s);
 cudaError_t launch_density_halve(const float *in, float *out, int n_out, cudaStream_t s);
-cudaError_t launch_read_moments(const LevelBufs &b, double *out4, cudaStream_t s);
-cudaError_t launch_row_support(const float *density, int n, int2 *sup, cudaStream_t s);
+cudaError_t launch_row_support(const float *density, int n, int2 *sup, int2 *range,
+                               unsigned long long *pixels, cudaStream_t s);
+cudaError_t launch_cover(const LevelBufs &b, cudaStream_t s);
 size_t rows_smem_bytes(int n);
 cudaError_t rows_configure();
-int update_blocks(int n);
+cudaError_t cells_configure();
+size_t list_blocks(int n);
+size_t cell_groups(int n);
 
 }  // namespace cvtgb

@@ -37,7 +37,7 @@ namespace cvtgb {
 // A pixel is a site when its x half is not MARKER (gcvt.cu:90); a site pixel
 // must hold its own coordinates, else err gets bit 0.
 __global__ void k_grid_to_bits(const uint32_t *__restrict__ grid, int n,
-                               uint64_t *__restrict__ bits, int *err) {
+                               uint64_t *__restrict__ bits, int *err, int *count) {
   int x = blockIdx.x * blockDim.x + threadIdx.x;
   int b = blockIdx.y;
   if (x >= n) return;
@@ -56,6 +56,7 @@ __global__ void k_grid_to_bits(const uint32_t *__restrict__ grid, int n,
   }
   bits[(size_t)b * n + x] = w;
   if (bad) atomicOr(err, 1);
+  if (count && w) atomicAdd(count, __popcll(w));
 }
 
 __global__ void k_bits_to_grid(const uint64_t *__restrict__ bits, int n,
@@ -71,9 +72,9 @@ __global__ void k_bits_to_grid(const uint64_t *__restrict__ bits, int n,
 }
 
 cudaError_t launch_grid_to_bits(const uint32_t *grid, int n, uint64_t *bits, int *err,
-                                cudaStream_t s) {
+                                int *count, cudaStream_t s) {
   dim3 blk(128), grd((n + 127) / 128, n / kBand);
-  k_grid_to_bits<<<grd, blk, 0, s>>>(grid, n, bits, err);
+  k_grid_to_bits<<<grd, blk, 0, s>>>(grid, n, bits, err, count);
   return cudaGetLastError();
 }
 
@@ -84,97 +85,51 @@ cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cud
 }
 
 // ---------------------------------------------------------------------------
-// Column summaries and site slots, one block per 32-column group (32 columns x
-// 32 band groups; each thread owns ceil(nb/32) consecutive bands):
-//   prev[b][x] = last site row in bands < b, next[b][x] = first site row in
-//   bands > b (kNoneAbove / kNoneBelow when there is none);
-//   word_rank[b][x] = sites of the group in earlier words (band-major, then
-//   column), group_count[g] = sites of the group.  A second one-block kernel
-//   turns group_count into group_offset, which completes the site slots used
-//   by the moment accumulators (see site_slot).
+// Column summaries: prev[b][x] = last site row in bands < b, next[b][x] =
+// first site row in bands > b (kNoneAbove / kNoneBelow when there is none).
+// One block per 32-column group: 32 columns x 32 band groups, each thread
+// owning ceil(nb/32) consecutive bands.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_summary(LevelBufs a, int respect_stop) {
   if (respect_stop && a.st->stopped) return;
   __shared__ int sLast[32][33];
   __shared__ int sFirst[32][33];
-  __shared__ int sCnt[32];    // sites in each warp's bands (all 32 columns)
   const int n = a.n, nb = n / kBand;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = blockIdx.x * 32 + tx;
-  const uint64_t *bits = (a.st->parity ? a.bits[1] : a.bits[0]);
+  const uint64_t *bits = cur_bits(a);
   const int G = (nb + 31) / 32;
   const int b0 = min(nb, ty * G), b1 = min(nb, b0 + G);
-  int myLast = kNoneAbove, myFirst = kNoneBelow, myCnt = 0;
+  int myLast = kNoneAbove, myFirst = kNoneBelow;
   for (int b = b0; b < b1; ++b) {
     uint64_t w = bits[(size_t)b * n + x];
     if (w) {
       if (myFirst == kNoneBelow) myFirst = b * kBand + __ffsll((long long)w) - 1;
       myLast = b * kBand + 63 - __clzll((long long)w);
-      myCnt += __popcll(w);
     }
   }
   sLast[ty][tx] = myLast;
   sFirst[ty][tx] = myFirst;
-  int wsum = myCnt;
-  for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-  if (tx == 0) sCnt[ty] = wsum;
   __syncthreads();
   int pv = kNoneAbove;
   for (int k = 0; k < ty; ++k) pv = max(pv, sLast[k][tx]);
   int nx = kNoneBelow;
   for (int k = ty + 1; k < 32; ++k) nx = min(nx, sFirst[k][tx]);
-  int rank = 0;  // sites of the group in bands before b0
-  for (int k = 0; k < ty; ++k) rank += sCnt[k];
   for (int b = b0; b < b1; ++b) {
-    const size_t wi = (size_t)b * n + x;
-    a.prev[wi] = (int16_t)pv;
-    const uint64_t w = bits[wi];
+    a.prev[(size_t)b * n + x] = (int16_t)pv;
+    uint64_t w = bits[(size_t)b * n + x];
     if (w) pv = b * kBand + 63 - __clzll((long long)w);
-    // rank of this word: earlier bands + earlier columns of this band
-    const int c = __popcll(w);
-    int incl = c;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, incl, o);
-      if (tx >= o) incl += t;
-    }
-    a.word_rank[wi] = rank + incl - c;
-    rank += __shfl_sync(0xffffffffu, incl, 31);
   }
   for (int b = b1 - 1; b >= b0; --b) {
     a.next[(size_t)b * n + x] = (int16_t)nx;
     uint64_t w = bits[(size_t)b * n + x];
     if (w) nx = b * kBand + __ffsll((long long)w) - 1;
   }
-  if (tx == 0 && ty == 31) {
-    int tot = 0;
-    for (int k = 0; k < 32; ++k) tot += sCnt[k];
-    a.group_count[blockIdx.x] = tot;
-  }
-}
-
-// Exclusive scan of the per-group site counts (n/32 <= 256 groups).
-__global__ void __launch_bounds__(256) k_group_offsets(LevelBufs a, int respect_stop) {
-  if (respect_stop && a.st->stopped) return;
-  __shared__ int s[256];
-  const int ng = a.n / 32, t = threadIdx.x;
-  int v = t < ng ? a.group_count[t] : 0;
-  s[t] = v;
-  __syncthreads();
-  for (int o = 1; o < 256; o <<= 1) {
-    int add = t >= o ? s[t - o] : 0;
-    __syncthreads();
-    s[t] += add;
-    __syncthreads();
-  }
-  if (t < ng) a.group_offset[t] = s[t] - v;
 }
 
 cudaError_t launch_summary(const LevelBufs &b, int respect_stop, cudaStream_t s) {
   dim3 blk(32, 32), grd(b.n / 32);
   k_summary<<<grd, blk, 0, s>>>(b, respect_stop);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_group_offsets<<<1, 256, 0, s>>>(b, respect_stop);
   return cudaGetLastError();
 }
 
@@ -244,32 +199,6 @@ __device__ __forceinline__ int column_candidate(uint64_t w, int pv, int nx, uint
   return da < db ? a : (db < da ? b : (be ? b : a));
 }
 
-// Two-float helpers (error-free transformations).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = __fadd_rn(a, b);
-  float bp = __fsub_rn(s, a);
-  float ap = __fsub_rn(s, bp);
-  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
-}
-
-// Compensated accumulation of the two-float value (vh, vl) into the per-site
-// (hi, lo) pair: the vector atomic returns the old hi; the rounding error of
-// old + vh (the atomic rounds to nearest) is recovered exactly by TwoSum and
-// added to lo together with vl.
-__device__ __forceinline__ float4 atom_add_v4(float4 *p, float4 v) {
-  float4 o;
-  asm volatile("atom.global.add.v4.f32 {%0,%1,%2,%3}, [%4], {%5,%6,%7,%8};"
-               : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w)
-               : "l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-               : "memory");
-  return o;
-}
-__device__ __forceinline__ void red_add_v4(float4 *p, float4 v) {
-  asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(v.x), "f"(v.y),
-               "f"(v.z), "f"(v.w)
-               : "memory");
-}
-
 // Lower envelope of the row's column candidates, left in C[0, K).
 // Candidates are generated 32 columns at a time (lane = column, coalesced
 // loads) and the first round of chord removal is applied on the fly; further
@@ -287,7 +216,7 @@ __device__ int row_hull(const LevelBufs &a, int r, int *C) {
   const int band = r >> 6, bi = r & 63;
   const uint64_t le = (bi == 63) ? ~0ull : ((2ull << bi) - 1ull);
   const int base = band * kBand;
-  const uint64_t *wrow = (a.st->parity ? a.bits[1] : a.bits[0]) + (size_t)band * n;
+  const uint64_t *wrow = cur_bits(a) + (size_t)band * n;
   const int16_t *prow = a.prev + (size_t)band * n;
   const int16_t *nrow = a.next + (size_t)band * n;
 
@@ -370,8 +299,7 @@ __device__ int row_hull(const LevelBufs &a, int r, int *C) {
   return K;
 }
 
-// Row support: [s0, s1) holds every pixel of the row with density != 0.
-template <int MODE>  // 0: write labels; 1: accumulate Lloyd moments
+// Label pass: one warp per row writes the row's label words.
 __global__ void __launch_bounds__(kRowsPerBlock * 32) k_rows(LevelBufs a, int respect_stop) {
   extern __shared__ __align__(16) int smem[];
   if (respect_stop && a.st->stopped) return;
@@ -381,128 +309,54 @@ __global__ void __launch_bounds__(kRowsPerBlock * 32) k_rows(LevelBufs a, int re
   if (r >= n) return;
   int *C = smem + warp * n;
   const int K = row_hull(a, r, C);
-
-  if (MODE == 0) {
-    uint32_t *out = a.labels + (size_t)r * n;
-    if (K == 0) {  // no site anywhere
-      for (int p = lane; p < n; p += 32) out[p] = kMarkerWord;
-      return;
-    }
-    for (int k0 = 0; k0 < K; k0 += 32) {
-      const int k = k0 + lane;
-      int s0 = 0, s1 = 0;
-      uint32_t lab = 0;
-      if (k < K) {
-        const int e = C[k];
-        s0 = k == 0 ? 0 : max(0, start_pixel(C[k - 1], e));
-        s1 = k + 1 == K ? n : min(n, start_pixel(e, C[k + 1]));
-        lab = pack_xy(ent_x(e), ent_g(e) + r);
-        if (s1 - s0 <= 16)
-          for (int p = s0; p < s1; ++p) out[p] = lab;
-      }
-      // long ranges: written by the whole warp, coalesced
-      unsigned lm = __ballot_sync(0xffffffffu, s1 - s0 > 16);
-      while (lm) {
-        const int L = __ffs(lm) - 1;
-        lm &= lm - 1;
-        const int b0 = __shfl_sync(0xffffffffu, s0, L), b1 = __shfl_sync(0xffffffffu, s1, L);
-        const uint32_t lv = __shfl_sync(0xffffffffu, lab, L);
-        for (int p = b0 + lane; p < b1; p += 32) out[p] = lv;
-      }
-    }
+  uint32_t *out = a.labels + (size_t)r * n;
+  if (K == 0) {  // no site anywhere
+    for (int p = lane; p < n; p += 32) out[p] = kMarkerWord;
     return;
   }
-
-  // MODE 1: per entry, two-float sums over its pixels inside the row's density
-  // support, then one converged compensated flush per entry.  The flush's
-  // atomic returns the old accumulator; its TwoSum correction is completed at
-  // the next flush, so the atomic's round trip overlaps the next entry's work.
-  if (K == 0) return;
-  const int2 sup = a.support[r];
-  const float *drow = a.density + (size_t)r * n;
-  const uint64_t *bits = (a.st->parity ? a.bits[1] : a.bits[0]);
-  float4 pend_o = make_float4(0.f, 0.f, 0.f, 0.f), pend_v = pend_o, pend_l = pend_o;
-  int pend_slot = -1;
-  auto complete = [&]() {
-    if (pend_slot >= 0) {
-      float4 lo;
-      float t;
-      two_sum(pend_o.x, pend_v.x, t, lo.x);
-      two_sum(pend_o.y, pend_v.y, t, lo.y);
-      two_sum(pend_o.z, pend_v.z, t, lo.z);
-      two_sum(pend_o.w, pend_v.w, t, lo.w);
-      lo.x = __fadd_rn(lo.x, pend_l.x);
-      lo.y = __fadd_rn(lo.y, pend_l.y);
-      lo.z = __fadd_rn(lo.z, pend_l.z);
-      red_add_v4(a.mlo + pend_slot, lo);
-      pend_slot = -1;
-    }
-  };
   for (int k0 = 0; k0 < K; k0 += 32) {
     const int k = k0 + lane;
-    float Wh = 0.f, Wl = 0.f, Xh = 0.f, Xl = 0.f, Q = 0.f;
-    int e = 0;
+    int s0 = 0, s1 = 0;
+    uint32_t lab = 0;
     if (k < K) {
-      e = C[k];
-      const int s0 = max(sup.x, k == 0 ? 0 : start_pixel(C[k - 1], e));
-      const int s1 = min(sup.y, k + 1 == K ? n : start_pixel(e, C[k + 1]));
-      const int ex = ent_x(e);
-      for (int p = s0; p < s1; ++p) {
-        const float rho = __ldg(drow + p);
-        const float dx = (float)(p - ex);
-        float s, er;
-        two_sum(Wh, rho, s, er);
-        Wh = s;
-        Wl = __fadd_rn(Wl, er);
-        const float pr = __fmul_rn(dx, rho);
-        const float pe = __fmaf_rn(dx, rho, -pr);
-        two_sum(Xh, pr, s, er);
-        Xh = s;
-        Xl = __fadd_rn(Xl, __fadd_rn(er, pe));
-        Q = __fmaf_rn(__fmul_rn(dx, dx), rho, Q);
-      }
+      const int e = C[k];
+      s0 = k == 0 ? 0 : max(0, start_pixel(C[k - 1], e));
+      s1 = k + 1 == K ? n : min(n, start_pixel(e, C[k + 1]));
+      lab = pack_xy(ent_x(e), ent_g(e) + r);
+      if (s1 - s0 <= 16)
+        for (int p = s0; p < s1; ++p) out[p] = lab;
     }
-    if (k < K && Wh != 0.f) {
-      const int eg = ent_g(e), ex = ent_x(e);
-      const float fg = (float)(-eg);
-      // SY = -g * W (two-float), E = Q + g^2 * W
-      const float yh = __fmul_rn(fg, Wh);
-      const float yl = __fmaf_rn(fg, Wh, -yh) + fg * Wl;
-      const float Ev = __fmaf_rn((float)(eg * eg), Wh, Q);
-      const int slot = site_slot(bits, a.word_rank, a.group_offset, n, ex, eg + r);
-      const float4 v = make_float4(Wh, Xh, yh, Ev);
-      const float4 o = atom_add_v4(a.mhi + slot, v);
-      complete();
-      pend_o = o;
-      pend_v = v;
-      pend_l = make_float4(Wl, Xl, yl, 0.f);
-      pend_slot = slot;
+    // long ranges: written by the whole warp, coalesced
+    unsigned lm = __ballot_sync(0xffffffffu, s1 - s0 > 16);
+    while (lm) {
+      const int L = __ffs(lm) - 1;
+      lm &= lm - 1;
+      const int b0 = __shfl_sync(0xffffffffu, s0, L), b1 = __shfl_sync(0xffffffffu, s1, L);
+      const uint32_t lv = __shfl_sync(0xffffffffu, lab, L);
+      for (int p = b0 + lane; p < b1; p += 32) out[p] = lv;
     }
   }
-  complete();
 }
 
 size_t rows_smem_bytes(int n) { return (size_t)kRowsPerBlock * n * sizeof(int); }
 
 cudaError_t rows_configure() {
-  cudaError_t e = cudaFuncSetAttribute(k_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)rows_smem_bytes(kMaxN));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)rows_smem_bytes(kMaxN));
 }
 
-cudaError_t launch_rows(const LevelBufs &b, int label_mode, int respect_stop, cudaStream_t s) {
+cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s) {
   size_t smem = rows_smem_bytes(b.n);
   dim3 blk(kRowsPerBlock * 32), grd((b.n + kRowsPerBlock - 1) / kRowsPerBlock);
-  if (label_mode) k_rows<0><<<grd, blk, smem, s>>>(b, respect_stop);
-  else k_rows<1><<<grd, blk, smem, s>>>(b, respect_stop);
+  k_rows<<<grd, blk, smem, s>>>(b, respect_stop);
   return cudaGetLastError();
 }
 
-// Row support of a density grid: [first, last + 1) of its nonzero pixels
-// (an empty row gets [0, 0)).  One warp per row.
-__global__ void k_row_support(const float *__restrict__ d, int n, int2 *sup) {
+// Row support of a density grid: [first, last + 1) of its nonzero pixels per
+// row (an empty row gets [0, 0)), the range of rows holding any (range must
+// start at (n, 0)), and the number of support pixels.  One warp per row.
+__global__ void k_row_support(const float *__restrict__ d, int n, int2 *sup, int2 *range,
+                              unsigned long long *pixels) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= n) return;
@@ -517,11 +371,24 @@ __global__ void k_row_support(const float *__restrict__ d, int n, int2 *sup) {
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
   }
-  if (lane == 0) sup[r] = hi < 0 ? make_int2(0, 0) : make_int2(lo, hi + 1);
+  if (lane == 0) {
+    sup[r] = hi < 0 ? make_int2(0, 0) : make_int2(lo, hi + 1);
+    if (hi >= 0) {
+      atomicMin(&range->x, r);
+      atomicMax(&range->y, r + 1);
+      atomicAdd(pixels, (unsigned long long)(hi + 1 - lo));
+    }
+  }
 }
 
-cudaError_t launch_row_support(const float *density, int n, int2 *sup, cudaStream_t s) {
-  k_row_support<<<(n + 7) / 8, 256, 0, s>>>(density, n, sup);
+cudaError_t launch_row_support(const float *density, int n, int2 *sup, int2 *range,
+                               unsigned long long *pixels, cudaStream_t s) {
+  const int2 init = make_int2(n, 0);
+  cudaError_t e = cudaMemcpyAsync(range, &init, sizeof(int2), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(pixels, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  k_row_support<<<(n + 7) / 8, 256, 0, s>>>(density, n, sup, range, pixels);
   return cudaGetLastError();
 }
 

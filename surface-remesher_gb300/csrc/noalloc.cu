@@ -6,13 +6,13 @@
 // grid; every other buffer the labeller needs lives in one static device
 // array of this file.
 //
-// The array holds the site bitmap, the column summaries, the word ranks, the
-// group counts and offsets, the iteration state and an error flag for grids
-// up to kNoAllocMaxN = 2048 (about 1 MB; every GPU that loads the library
-// keeps it until the process exits).  All calls share it: a call rewrites
-// everything it reads before reading it, so the previous call's contents
-// never leak, but two calls whose work overlaps on the GPU (different streams
-// or threads without ordering between them) race on it.
+// The array holds the site bitmap, the column summaries, the iteration state
+// and an error flag for grids up to kNoAllocMaxN = 2048 (about 0.8 MB; every
+// GPU that loads the library keeps it until the process exits).  All calls
+// share it: a call rewrites everything it reads before reading it, so the
+// previous call's contents never leak, but two calls whose work overlaps on
+// the GPU (different streams or threads without ordering between them) race
+// on it.
 //
 // Host code may not use the array's name as a device address (in host code it
 // names a host-side stand-in).  The first call on a device takes the array's
@@ -32,17 +32,14 @@ constexpr size_t kWords = (size_t)(kNoAllocMaxN / kBand) * kNoAllocMaxN;
 constexpr size_t kOffBits = 0;
 constexpr size_t kOffPrev = align_up(kOffBits + kWords * sizeof(uint64_t));
 constexpr size_t kOffNext = align_up(kOffPrev + kWords * sizeof(int16_t));
-constexpr size_t kOffRank = align_up(kOffNext + kWords * sizeof(int16_t));
-constexpr size_t kOffGroupCount = align_up(kOffRank + kWords * sizeof(int));
-constexpr size_t kOffGroupOffset = align_up(kOffGroupCount + (kNoAllocMaxN / 32) * sizeof(int));
-constexpr size_t kOffState = align_up(kOffGroupOffset + (kNoAllocMaxN / 32) * sizeof(int));
+constexpr size_t kOffState = align_up(kOffNext + kWords * sizeof(int16_t));
 constexpr size_t kOffErr = align_up(kOffState + sizeof(DevState));
 constexpr size_t kNoAllocBytes = align_up(kOffErr + sizeof(int));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-// Per-call reset of what must start at zero: the state (parity 0, not
-// stopped) and the error flag.  The bitmap, summaries and ranks are fully
+// Per-call reset of what must start at zero: the state (bitmap 0 current, not
+// stopped) and the error flag.  The bitmap and the summaries are fully
 // rewritten by the labelling kernels before they are read.
 __global__ void k_noalloc_reset(DevState *st, int *err) {
   if (threadIdx.x == 0) {
@@ -93,22 +90,20 @@ extern "C" int gcvt_label_grid_static(const int16_t *sites, int16_t *labels, int
   int *err = reinterpret_cast<int *>(base + kOffErr);
   k_noalloc_reset<<<1, 32, 0, s>>>(st, err);
   if (cudaGetLastError() != cudaSuccess) return GCVT_ERR_CUDA;
-  if (launch_grid_to_bits(reinterpret_cast<const uint32_t *>(sites), n, bits, err, s) !=
+  if (launch_grid_to_bits(reinterpret_cast<const uint32_t *>(sites), n, bits, err, nullptr, s) !=
       cudaSuccess)
     return GCVT_ERR_CUDA;
   LevelBufs b = {};
   b.n = n;
   b.bits[0] = bits;
   b.bits[1] = bits;
+  b.bits[2] = bits;
   b.prev = reinterpret_cast<int16_t *>(base + kOffPrev);
   b.next = reinterpret_cast<int16_t *>(base + kOffNext);
-  b.word_rank = reinterpret_cast<int *>(base + kOffRank);
-  b.group_count = reinterpret_cast<int *>(base + kOffGroupCount);
-  b.group_offset = reinterpret_cast<int *>(base + kOffGroupOffset);
   b.labels = reinterpret_cast<uint32_t *>(labels);
   b.st = st;
   if (launch_summary(b, 0, s) != cudaSuccess) return GCVT_ERR_CUDA;
-  if (launch_rows(b, 1, 0, s) != cudaSuccess) return GCVT_ERR_CUDA;
+  if (launch_rows(b, 0, s) != cudaSuccess) return GCVT_ERR_CUDA;
   int herr = 0;  // host stack: the only readback, no allocation
   if (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)

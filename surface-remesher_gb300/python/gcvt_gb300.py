@@ -186,7 +186,8 @@ class Context:
         return out
 
     def time_kernels(self, iterations):
-        """Mean ms of (summary, row pass, update) over `iterations` iterations."""
+        """Mean device ms of (one Lloyd iteration, one labelling pass, 0) over
+        `iterations` iterations; the sites move as in iterate()."""
         ms = (ctypes.c_float * 3)()
         _check(self.lib.gcvt_ctx_time_kernels(self.h, int(iterations), ms), "gcvt_ctx_time_kernels")
         return list(ms)
