@@ -18,9 +18,10 @@ Metric: Gpix-pass/s = n^2 x labelling passes / second, 101 passes per step
   e2e   : the same through the C ABI with pinned host buffers: host->device
           copies of sites, density and mask and the device->host copy of the
           label grid inside every timed step.
-  roofline: the dominant kernel (k_cell<0>, one whole Lloyd iteration):
-          algorithmic bytes per launch / its mean launch duration (CUDA events
-          on the launching stream over the same workload) against the measured
+  roofline: one Lloyd iteration, the launch pair k_list + k_cell<0> (88 % +
+          4 % of the step's device time): algorithmic bytes per iteration /
+          its mean duration over iterations 2-100 of the timed steps (CUDA
+          events on the launching stream around them) against the measured
           HBM copy bandwidth.
 --impl reference runs the reference's algorithm on the host cores (the
 oracle's OpenMP restatement of gcvt.cu, all threads) on a bounded sample of
@@ -49,17 +50,20 @@ ITERS = 100
 PASSES = ITERS + 1
 METRIC = "Gpix-pass/s, plain Lloyd CVT (gCVT loop), 4096^2 grid, 262,144 sites, 100 iterations"
 UNIT = "Gpix-pass/s"
-# Algorithmic bytes of one Lloyd-iteration launch (k_cell<0>): the density
+# Algorithmic bytes of one Lloyd iteration (k_list + k_cell<0>): the density
 # once over its row support (4 B per support pixel: every such pixel belongs
-# to exactly one cell), the current site bitmap read and the bitmap two
-# iterations ahead cleared (1/8 B per pixel each), and per site its word of the
-# fixed-site bitmap read and its bit OR-ed into the next bitmap (8 + 8 B).
+# to exactly one cell); the current site bitmap read by k_list and the bitmap
+# two iterations ahead cleared by k_cell (1/8 B per pixel each); per site its
+# list entry written and read (4 + 4 B), its word of the fixed-site bitmap
+# read and its bit OR-ed into the next bitmap (8 + 8 B).
 ALG_BYTES_PER_SUPPORT_PX = 4.0
 ALG_BYTES_PER_PX = 0.125 + 0.125
-ALG_BYTES_PER_SITE = 16.0
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_cell<0> launch on this
-# workload, from the ncu capture summarised in profiles/ (None until captured).
-NCU_TRAFFIC_BYTES = None
+ALG_BYTES_PER_SITE = 24.0
+# dram__bytes_read.sum + dram__bytes_write.sum of k_list + k_cell<0> for one
+# iteration of this workload (iteration 31 of a graph-replayed run, warm L2),
+# from the ncu capture summarised in profiles/cell_kernel_plain_4096.md:
+# k_list 1,493,248 + 693,248, k_cell 33,864,960 + 18,889,984 bytes.
+NCU_TRAFFIC_BYTES = 54941440
 
 
 def support_pixels(rho):
@@ -219,14 +223,24 @@ def run_ours(args):
     ctx = G.Context(n)
     ctx.set_stream(stream.cuda_stream)
 
-    def step_device():
+    loop_ms = []  # iterations 2..ITERS of each timed device step
+
+    def step_device(record=False):
         ctx.load(d_sites, d_rho, d_mask)
-        ctx.iterate(ITERS)
+        ctx.iterate(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.iterate(ITERS - 1)
+        b.record(stream)
         ctx.label(d_out)
+        if record:
+            loop_ms.append((a, b))
 
     def step_host():
         ctx.load(h_sites, h_rho, h_mask)
-        ctx.iterate(ITERS)
+        ctx.iterate(1)
+        ctx.iterate(ITERS - 1)
         ctx.label(h_out)
 
     def barrier():
@@ -254,15 +268,16 @@ def run_ours(args):
         for _ in range(args.warmup):
             step_device()
         with ClockSampler(local) as clk:
-            t_dev = timed(step_device, args.steps)
+            t_dev = timed(lambda: step_device(True), args.steps)
+        iter_ms = statistics.mean(a.elapsed_time(b) for a, b in loop_ms) / (ITERS - 1)
+        info = ctx.info()  # state after the last timed step's 100 iterations
         for _ in range(max(1, args.warmup // 2)):
             step_host()
         t_e2e = timed(step_host, args.steps)
-        # dominant kernel: per-launch durations on the launching stream
+        # a labelling pass (final output), timed alone
         ctx.load(d_sites, d_rho, d_mask)
-        kms = ctx.time_kernels(20)
+        kms = ctx.time_kernels(5)
         torch.cuda.synchronize(dev)
-        info = ctx.info()
     if ws > 1:
         t = torch.tensor([t_dev, t_e2e], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -274,7 +289,7 @@ def run_ours(args):
     support_px = support_pixels(rho)
     alg = (support_px * ALG_BYTES_PER_SUPPORT_PX + n * n * ALG_BYTES_PER_PX
            + nsites * ALG_BYTES_PER_SITE)
-    achieved = alg / (kms[0] / 1e3) / 1e9
+    achieved = alg / (iter_ms / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
@@ -285,19 +300,22 @@ def run_ours(args):
                    "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
                    "parallelism": "replicas x%d" % ws},
         "iter_per_s": ITERS * args.steps * ws / t_dev,
-        "kernel_ms": {"lloyd_iteration": kms[0], "label_pass": kms[1]},
+        "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
-                     "peak_source": peak_kind, "kernel": "k_cell<0> (one Lloyd iteration)",
+                     "peak_source": peak_kind,
+                     "kernel": "k_list + k_cell<0> (one Lloyd iteration, iterations 2-100)",
                      "algorithmic_bytes": alg},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(h_sites.numel() * 2 + h_rho.numel() * 4 + h_mask.numel()),
                 "d2h_bytes_per_step": int(h_out.numel() * 2),
                 "ms_per_step": t_e2e / args.steps * 1e3},
-        # per step: load (row support, fixed bitmap, site bitmap), covering
-        # bound (column summaries, rows, k_cover, k_cover_finish), one k_cell
-        # per iteration, final labelling (column summaries, rows)
-        "gpu_launches": args.steps * (3 + 4 + ITERS + 2),
+        # per step: load (row support, fixed bitmap, site bitmap); level
+        # start (column summaries, rows, k_cover, k_cover_finish, k_count);
+        # iterate(1) and iterate(ITERS - 1) as graphs of ten (k_list, k_cell)
+        # pairs, launches past the last iteration returning at once; final
+        # labelling (column summaries, rows)
+        "gpu_launches": args.steps * (3 + 5 + 2 * 10 * (1 + (ITERS - 1 + 9) // 10) + 2),
         "clocks": clk.summary(),
         "final_energy": info["energy"],
     }
@@ -331,17 +349,25 @@ def reference_gpu(sites, rho, mask):
 
 def run_profile_case(iterations):
     """The bench workload for ncu captures: load once, then `iterations` Lloyd
-    iterations as plain (non-graph) launches."""
+    iterations as the bench runs them (CUDA graphs of k_list + k_cell), timed
+    as a whole with CUDA events on the context's stream."""
     import torch
     import gcvt_gb300 as G
     from workloads import config_inputs
     sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    stream = torch.cuda.Stream()
     ctx = G.Context(sites.shape[0])
+    ctx.set_stream(stream.cuda_stream)
     ctx.load(sites, rho, mask)
-    per_iter = [ctx.time_kernels(1)[0] for _ in range(iterations)]
-    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.iterate(iterations)
+    e1.record(stream)
+    e1.synchronize()
     print(json.dumps({"profile_case": CONFIG, "iterations": iterations,
-                      "lloyd_ms_per_iteration": per_iter}))
+                      "lloyd_ms_per_iteration": e0.elapsed_time(e1) / iterations,
+                      "energy": ctx.info()["energy"]}))
     ctx.close()
     return 0
 

@@ -118,12 +118,39 @@ int gcvt_ctx_time_kernels(gcvt_ctx *ctx, int iterations, float *ms3);
 /* Schedule state (iterations, omega, energies). */
 int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
 
+/* The CDT's input points from the current sites, as delaunayInput collects
+ * them (delaunay.h:46-57) from the label grid: every site that is not fixed,
+ * in x-major then y order, as the FP64 pair (x * scale + left,
+ * y * scale + lower).  Writes min(count, capacity) points (2 doubles each)
+ * to xy and the number of points to *count.  Computed on the GPU from the
+ * site bitmap, so no label grid leaves the device. */
+int gcvt_ctx_extract_points(gcvt_ctx *ctx, double scale, double left, double lower, double *xy,
+                            int capacity, int *count, int mem);
+
 /* ---- one-call forms ---------------------------------------------------- */
 
 /* gCVT with a status code: host buffers in, label grid out in `voronoi`
  * (gcvt.cu:1087-1156).  size is a power of two in [256, 8192]. */
 int gcvt_compute(int16_t *voronoi, const float *density, const uint8_t *mask, int size,
                  int depth, int max_iter);
+
+/* Initial sites as the reference's centroidalVoronoi makes them
+ * (gcvt.h:76-122), host buffers: every mask pixel becomes a fixed site, every
+ * other pixel MARKER, then `num` distinct free pixels are drawn by rejection
+ * against the density from the reference's generator (gcvt.h:57-73).
+ * state: the generator's four 64-bit words (z, w, jsr, jcong), updated; NULL
+ * uses the library's own generator, which starts at zero like the
+ * reference's unseeded globals and carries over between calls.  mask may be
+ * NULL (no fixed sites).  Returns GCVT_ERR_ARGUMENT when num exceeds the free
+ * pixels of positive density (the reference would loop forever) and
+ * GCVT_ERR_INPUT when a draw budget of 1000 n^2 + 10^6 runs out. */
+int gcvt_seed_sites(int16_t *voronoi, const float *density, const uint8_t *mask, int num,
+                    int size, uint64_t *state);
+
+/* centroidalVoronoi (gcvt.h:124-139) with a status code: gcvt_seed_sites
+ * with the library's generator, then gcvt_compute; labels out in voronoi. */
+int gcvt_centroidal_voronoi(int16_t *voronoi, float *density, const uint8_t *mask, int vertices,
+                            int size, int depth, int max_iter);
 
 /* Label a site grid once (pba2DCompute on a given grid). */
 int gcvt_label_grid(const int16_t *sites, int16_t *labels, int n, int mem);
@@ -145,7 +172,7 @@ int gcvt_rasterize(const double *points, const double *weight, int num_point,
  * reference.  `sites` and `labels` are device pointers (2*n*n int16 each) on
  * the current device; `stream` is a cudaStream_t (NULL: the legacy default
  * stream).  Nothing is allocated: the scratch lives in one static device
- * array sized for n <= 2048 (about 1 MB, held by every device that loads the
+ * array sized for n <= 2048 (about 0.8 MB, held by every device that loads the
  * library until exit); larger n returns GCVT_ERR_SIZE.  The first call on a
  * device looks up that array's device address -- make it before any stream
  * capture.  Calls share the array, so calls that overlap on the GPU race. */

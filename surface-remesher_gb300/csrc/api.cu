@@ -45,6 +45,7 @@ struct gcvt_ctx {
   uint8_t *hint = nullptr;      // per pixel window hints
   float4 *gslot = nullptr, *sslot = nullptr;
   unsigned *scnt = nullptr;
+  unsigned *colcnt = nullptr;   // point extraction: n_max column counts + total
   int cover_valid = 0;          // the covering bound, list counts and hints
                                 // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
@@ -363,6 +364,7 @@ int gcvt_ctx_create(int n_max, gcvt_ctx **out) {
   ok = ok && dal(&c->gslot, groups * sizeof(float4));
   ok = ok && dal(&c->sslot, slots * sizeof(float4));
   ok = ok && dal(&c->scnt, slots * sizeof(unsigned));
+  ok = ok && dal(&c->colcnt, ((size_t)n_max + 1) * sizeof(unsigned));
   ok = ok && dal(&c->err, 2 * sizeof(int));
   if (!ok) return fail(GCVT_ERR_ALLOC);
   if (cudaMemsetAsync(c->scnt, 0, slots * sizeof(unsigned), c->stream) != cudaSuccess)
@@ -402,6 +404,7 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->gslot);
   cudaFree(c->sslot);
   cudaFree(c->scnt);
+  cudaFree(c->colcnt);
   cudaFree(c->moments);
   cudaFree(c->err);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -525,6 +528,38 @@ int gcvt_ctx_moments(gcvt_ctx *c, double *out4, int mem) {
   CK(launch_list(b, 0, c->stream));
   CK(launch_cells(b, 1, c->moments, c->stream));
   return copy_out(out4, c->moments, (size_t)4 * n * n * sizeof(double), mem, c->stream);
+}
+
+int gcvt_ctx_extract_points(gcvt_ctx *c, double scale, double left, double lower, double *xy,
+                            int capacity, int *count, int mem) {
+  if (!c || !count || capacity < 0 || (capacity > 0 && !xy)) return GCVT_ERR_ARGUMENT;
+  if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  const int n = c->cur_n;
+  const int level = level_of(c, n);
+  double *dst = xy;
+  if (mem == GCVT_MEM_HOST) {  // stage in the moments buffer (32 B per pixel >= 16 B per point)
+    if (!c->moments &&
+        cudaMalloc(reinterpret_cast<void **>(&c->moments),
+                   (size_t)4 * c->n_max * c->n_max * sizeof(double)) != cudaSuccess)
+      return GCVT_ERR_ALLOC;
+    dst = c->moments;
+  }
+  const unsigned cap = (unsigned)capacity;
+  CK(launch_extract(c->bits[c->st_host->cur], c->fixed_bits[level], n, c->colcnt, scale, left,
+                    lower, dst, cap, c->colcnt + c->n_max, c->stream));
+  unsigned total = 0;
+  CK(cudaMemcpyAsync(&total, c->colcnt + c->n_max, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *count = (int)total;
+  const size_t written = total < cap ? total : cap;
+  if (mem == GCVT_MEM_HOST && written)
+    return copy_out(xy, dst, written * 2 * sizeof(double), GCVT_MEM_HOST, c->stream);
+  return GCVT_OK;
 }
 
 int gcvt_ctx_info(gcvt_ctx *c, gcvt_run_info *info) {

@@ -21,7 +21,7 @@
 // outside the disc can beat s there (|p - t| > W - R >= R); otherwise the
 // window grows (W <- min(2R + 1, 2W)) and the cell is redone; a window
 // covering the grid is exact by construction.  The starting W of a site is
-// the hint its predecessor left at its pixel (2R + 3 of the cell it had).
+// the hint its predecessor left at its pixel (2R + 2 of the cell it had).
 //
 // Rows are visited outward from s.  A row may hold no pixel of the cell while
 // a row further out does (a sliver narrower than a pixel), so the walk ends
@@ -196,30 +196,32 @@ __device__ __forceinline__ RowPair row_bounds2(const int2 *rec, int cnt, bool ov
   return p;
 }
 
-// Sums of row v = [da, db] (relative columns) into c.
+// Sums of row v = [da, db] (relative columns) into c: FP32 over chunks of at
+// most 16 pixels (relative error below 16 ulp of the chunk), chunks folded
+// into the two-float cell sums.
 __device__ __forceinline__ void row_sums(const float *__restrict__ row, int da, int db, int v,
                                          CellSums &c) {
-  float rw = 0.f, rwl = 0.f, rx = 0.f, rxl = 0.f, rq = 0.f;
-  float dx = (float)da;
-  for (int u = da; u <= db; ++u, dx += 1.0f) {
-    const float rho = __ldg(row + u);
-    float s1, e1;
-    tsum_c(rw, rho, s1, e1);
-    rw = s1;
-    rwl = __fadd_rn(rwl, e1);
-    const float pr = __fmul_rn(dx, rho);
-    const float pe = __fmaf_rn(dx, rho, -pr);
-    tsum_c(rx, pr, s1, e1);
-    rx = s1;
-    rxl = __fadd_rn(rxl, __fadd_rn(e1, pe));
-    rq = __fmaf_rn(__fmul_rn(dx, dx), rho, rq);
+  const float fv = (float)v, fv2 = (float)(v * v);
+  for (int u0 = da; u0 <= db; u0 += 16) {
+    const int u1 = min(db, u0 + 15);
+    float rw = 0.f, rx = 0.f, rq = 0.f;
+    float dx = (float)u0;
+#pragma unroll 4
+    for (int u = u0; u <= u1; ++u) {
+      const float rho = __ldg(row + u);
+      const float t = __fmul_rn(dx, rho);
+      rw = __fadd_rn(rw, rho);
+      rx = __fadd_rn(rx, t);
+      rq = __fmaf_rn(t, dx, rq);
+      dx = __fadd_rn(dx, 1.0f);
+    }
+    dfa(c.wh, c.wl, rw, 0.f);
+    dfa(c.xh, c.xl, rx, 0.f);
+    dfa_scaled(c.yh, c.yl, fv, rw, 0.f);
+    float qh = rq, ql = 0.f;
+    dfa_scaled(qh, ql, fv2, rw, 0.f);
+    dfa(c.eh, c.el, qh, ql);
   }
-  dfa(c.wh, c.wl, rw, rwl);
-  dfa(c.xh, c.xl, rx, rxl);
-  dfa_scaled(c.yh, c.yl, (float)v, rw, rwl);
-  float qh = rq, ql = 0.f;
-  dfa_scaled(qh, ql, (float)(v * v), rw, rwl);
-  dfa(c.eh, c.el, qh, ql);
 }
 
 // Row v of the cell with bounds [lo, hi]: clip to the density support and
@@ -228,11 +230,52 @@ __device__ __forceinline__ void take_row(const LevelBufs &a, int n, int sx, int 
                                          int lo, int hi, int &R2, CellSums &c) {
   const int y = sy + v;
   const int2 s = a.support[y];
-  const int hx = isqrt_floor(rb2 - v * v);
-  const int da = max(max(lo, s.x - sx), -hx), db = min(min(hi, s.y - 1 - sx), hx);
+  int da = max(lo, s.x - sx), db = min(hi, s.y - 1 - sx);
   if (da > db) return;
+  if (max(da * da, db * db) + v * v > rb2) {  // clip to the covering disc
+    const int hx = isqrt_floor(rb2 - v * v);
+    da = max(da, -hx);
+    db = min(db, hx);
+    if (da > db) return;
+  }
   R2 = max(R2, max(da * da, db * db) + v * v);
   row_sums(a.density + (size_t)y * n + sx, da, db, v, c);
+}
+
+// The sites of one bitmap word (column offset A, bit i at row offset B0 + i)
+// as candidates of s: a record each, or a row limit for a site in s's column.
+__device__ __forceinline__ void gather_word(uint64_t w, int A, int B0, int sy, long long Wc,
+                                            int2 *rec, int &cnt, bool &ovf, int &vmin,
+                                            int &vmax) {
+  while (w) {
+    const int i = __ffsll((long long)w) - 1;
+    w &= w - 1ull;
+    const int B = B0 + i;
+    const int K = A * A + B * B;
+    if (K == 0 || (long long)K > Wc) continue;  // s itself; outside the disc
+    if (A == 0) {
+      // same column: s keeps the rows strictly on its side of the mirror row,
+      // and the mirror row (B even) if the band rule says so
+      if (B > 0) {
+        int m = (B - 1) >> 1;
+        if (!(B & 1) && (((sy + B) >> 6) != ((sy + B / 2) >> 6))) m = B / 2;
+        vmax = min(vmax, m);
+      } else {
+        int m = -((-B - 1) >> 1);
+        if (!(B & 1) && ((sy >> 6) == ((sy + B / 2) >> 6))) m = B / 2;
+        vmin = max(vmin, m);
+      }
+      continue;
+    }
+    if (cnt >= kMaxCand) {
+      ovf = true;
+      continue;
+    }
+    // |S|, |D| <= 2 (n - 1) fit 16 bits
+    const int S = A > 0 ? 2 * B : -2 * B;
+    rec[cnt++] = make_int2(A > 0 ? K : -K,
+                           (int)(((unsigned)S & 0xffffu) | ((unsigned)(2 * A) << 16)));
+  }
 }
 
 // Exact cell of site (sx, sy) and its sums.  bits: current site bitmap;
@@ -257,41 +300,28 @@ __device__ CellSums cell_sums(const LevelBufs &a, const uint64_t *__restrict__ b
     int cnt = 0;
     bool ovf = false;
     int vmin = vlo_sup, vmax = vhi_sup;  // row limits, same-column sites folded in
-    for (int x = x0; x <= x1; ++x) {
-      const int A = x - sx;
-      for (int b = b0; b <= b1; ++b) {
-        uint64_t w = __ldg(bits + (size_t)b * n + x) &
-                     row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63));
-        while (w) {
-          const int i = __ffsll((long long)w) - 1;
-          w &= w - 1ull;
-          const int B = 64 * b + i - sy;
-          const int K = A * A + B * B;
-          if (K == 0 || (long long)K > Wc) continue;  // s itself; outside the disc
-          if (A == 0) {
-            // same column: s keeps the rows strictly on its side of the
-            // mirror row, and the mirror row (B even) if the band rule says so
-            if (B > 0) {
-              int m = (B - 1) >> 1;
-              if (!(B & 1) && (((sy + B) >> 6) != ((sy + B / 2) >> 6))) m = B / 2;
-              vmax = min(vmax, m);
-            } else {
-              int m = -((-B - 1) >> 1);
-              if (!(B & 1) && ((sy >> 6) == ((sy + B / 2) >> 6))) m = B / 2;
-              vmin = max(vmin, m);
-            }
-            continue;
-          }
-          if (cnt >= kMaxCand) {
-            ovf = true;
-            continue;
-          }
-          // |S|, |D| <= 2 (n - 1) fit 16 bits
-          const int S = A > 0 ? 2 * B : -2 * B;
-          rec[cnt++] = make_int2(A > 0 ? K : -K,
-                                 (int)(((unsigned)S & 0xffffu) | ((unsigned)(2 * A) << 16)));
+    if (b1 - b0 <= 1) {  // one or two bands: load the next column ahead
+      const uint64_t *p0 = bits + (size_t)b0 * n, *p1 = bits + (size_t)b1 * n;
+      const uint64_t m0 = row_mask(y0 - 64 * b0, min(y1 - 64 * b0, 63));
+      const uint64_t m1 = b1 > b0 ? row_mask(0, y1 - 64 * b1) : 0ull;
+      uint64_t c0 = __ldg(p0 + x0) & m0, c1 = m1 ? __ldg(p1 + x0) & m1 : 0ull;
+      for (int x = x0; x <= x1; ++x) {
+        uint64_t n0 = 0ull, n1 = 0ull;
+        if (x < x1) {
+          n0 = __ldg(p0 + x + 1) & m0;
+          if (m1) n1 = __ldg(p1 + x + 1) & m1;
         }
+        gather_word(c0, x - sx, 64 * b0 - sy, sy, Wc, rec, cnt, ovf, vmin, vmax);
+        gather_word(c1, x - sx, 64 * b1 - sy, sy, Wc, rec, cnt, ovf, vmin, vmax);
+        c0 = n0;
+        c1 = n1;
       }
+    } else {
+      for (int x = x0; x <= x1; ++x)
+        for (int b = b0; b <= b1; ++b)
+          gather_word(__ldg(bits + (size_t)b * n + x) &
+                          row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63)),
+                      x - sx, 64 * b - sy, sy, Wc, rec, cnt, ovf, vmin, vmax);
     }
     // |K - S v| <= 2 W^2 + 2 W rb: below 2^23 the reciprocal estimate is safe
     const bool fast = 2 * W2 + 2 * (long long)W * rb < (1ll << 23);
@@ -444,7 +474,7 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
         const unsigned long long old =
             atomicOr(reinterpret_cast<unsigned long long *>(nxt + widx), bit);
         if (!(old & bit)) atomicAdd(cnt_nxt + widx / kListWords, 1u);
-        a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 3, 255);
+        a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 2, 255);
       }
     }
     __syncwarp();

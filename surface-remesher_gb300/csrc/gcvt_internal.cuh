@@ -98,6 +98,9 @@ cudaError_t launch_row_support(const float *density, int n, int2 *sup, int2 *ran
 cudaError_t launch_cover(const LevelBufs &b, cudaStream_t s);
 size_t rows_smem_bytes(int n);
 cudaError_t rows_configure();
+cudaError_t launch_extract(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *colcnt,
+                           double scale, double left, double lower, double *xy,
+                           unsigned capacity, unsigned *total, cudaStream_t s);
 cudaError_t cells_configure();
 size_t list_blocks(int n);
 size_t cell_groups(int n);

@@ -64,6 +64,10 @@ SIGNATURES = {
     "gcvt_label_grid": ([P, P, I, I], I),
     "gcvt_label_grid_static": ([P, P, I, P], I),
     "gcvt_rasterize": ([P, P, I, P, I, P, ctypes.c_double, I, I], I),
+    "gcvt_ctx_extract_points": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I,
+                                 ctypes.POINTER(I), I], I),
+    "gcvt_seed_sites": ([P, P, P, I, I, P], I),
+    "gcvt_centroidal_voronoi": ([P, P, P, I, I, I, I], I),
 }
 CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii",
                "discretization_d": "_Z16discretization_dPdS_iPiiPfdi"}
@@ -192,6 +196,21 @@ class Context:
         _check(self.lib.gcvt_ctx_time_kernels(self.h, int(iterations), ms), "gcvt_ctx_time_kernels")
         return list(ms)
 
+    def extract_points(self, scale=1.0, left=0.0, lower=0.0, capacity=None):
+        """CDT input points (count, 2) float64 of the current free sites, in
+        delaunayInput's order (delaunay.h:46-57)."""
+        cnt = I(0)
+        if capacity is None:
+            _check(self.lib.gcvt_ctx_extract_points(self.h, float(scale), float(left),
+                                                    float(lower), None, 0, ctypes.byref(cnt),
+                                                    MEM_HOST), "gcvt_ctx_extract_points")
+            capacity = cnt.value
+        out = np.empty((max(capacity, 1), 2), np.float64)
+        _check(self.lib.gcvt_ctx_extract_points(self.h, float(scale), float(left), float(lower),
+                                                out.ctypes.data, int(capacity), ctypes.byref(cnt),
+                                                MEM_HOST), "gcvt_ctx_extract_points")
+        return out[:min(cnt.value, capacity)]
+
     def info(self):
         info = RunInfo()
         _check(self.lib.gcvt_ctx_info(self.h, ctypes.byref(info)), "gcvt_ctx_info")
@@ -208,6 +227,35 @@ def gcvt(voronoi, density, mask, depth=1, max_iter=1000):
                             _host_ptr(mask, np.uint8, (n, n)), n, int(depth), int(max_iter)),
            "gcvt_compute")
     return voronoi
+
+
+def seed_sites(density, mask, num, state=None):
+    """Initial site grid (n, n, 2) int16 as centroidalVoronoi makes it
+    (gcvt.h:76-122).  state: None for the library's own generator, or a
+    numpy uint64 array of 4 words (z, w, jsr, jcong), updated in place."""
+    lib = load_library()
+    n = int(density.shape[0])
+    v = np.empty((n, n, 2), np.int16)
+    sp = None
+    if state is not None:
+        if not (isinstance(state, np.ndarray) and state.dtype == np.uint64 and state.size == 4):
+            raise TypeError("state must be a numpy uint64 array of 4 words")
+        sp = state.ctypes.data
+    mp = None if mask is None else _host_ptr(mask, np.uint8, (n, n))
+    _check(lib.gcvt_seed_sites(v.ctypes.data, _host_ptr(density, np.float32, (n, n)), mp,
+                               int(num), n, sp), "gcvt_seed_sites")
+    return v
+
+
+def centroidal_voronoi(density, mask, vertices, depth=1, max_iter=1000):
+    """centroidalVoronoi (gcvt.h:124-139): seed, then gCVT; returns the label grid."""
+    lib = load_library()
+    n = int(density.shape[0])
+    v = np.empty((n, n, 2), np.int16)
+    _check(lib.gcvt_centroidal_voronoi(v.ctypes.data, _host_ptr(density, np.float32, (n, n)),
+                                       _host_ptr(mask, np.uint8, (n, n)), int(vertices), n,
+                                       int(depth), int(max_iter)), "gcvt_centroidal_voronoi")
+    return v
 
 
 def label_grid(sites):
