@@ -372,6 +372,96 @@ def run_profile_case(iterations):
     return 0
 
 
+def run_batched(args):
+    """Batched uneven charts (64 charts of side 256-2048, 8 Gaussians each,
+    sites = domain pixels / 64, 100 iterations): every chart loaded from HBM,
+    iterated in one launch pair per iteration (gcvt_batch_iterate), labelled;
+    against the same charts run one after the other (gcvt_ctx_iterate)."""
+    import torch
+    import gcvt_gb300 as G
+    from workloads import BATCH, batched_inputs
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    charts = batched_inputs(seed=SEED)
+    stream = torch.cuda.Stream(device=dev)
+    dev_in, ctxs = [], []
+    for sites, rho, mask in charts:
+        n = sites.shape[0]
+        dev_in.append((torch.from_numpy(sites).to(dev), torch.from_numpy(rho).to(dev),
+                       torch.from_numpy(mask).to(dev), torch.empty_like(torch.from_numpy(sites)).to(dev)))
+        c = G.Context(n)
+        c.set_stream(stream.cuda_stream)
+        ctxs.append(c)
+    batch = G.Batch(ctxs)
+    batch.set_stream(stream.cuda_stream)
+    iters = BATCH["iters"]
+    px = sum(int(s.shape[0]) ** 2 for s, _, _ in charts)
+    sites_total = sum(int((s[..., 0] != -32768).sum()) for s, _, _ in charts)
+
+    def load_all():
+        for c, (ds, dr, dm, _) in zip(ctxs, dev_in):
+            c.load(ds, dr, dm)
+
+    def label_all():
+        for c, (_, _, _, out) in zip(ctxs, dev_in):
+            c.label(out)
+
+    def step_batched():
+        load_all()
+        batch.iterate(iters)
+        label_all()
+
+    def step_solo():
+        load_all()
+        for c in ctxs:
+            c.iterate(iters)
+        label_all()
+
+    def timed(fn, steps):
+        ms = []
+        for _ in range(steps):
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return statistics.mean(ms)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_batched()
+        with ClockSampler(0) as clk:
+            t_b = timed(step_batched, args.steps)
+        energies = [c.info()["energy"] for c in ctxs]
+        for _ in range(1):
+            step_solo()
+        t_s = timed(step_solo, max(1, args.steps // 2))
+        same = all(abs(c.info()["energy"] - e) == 0.0 for c, e in zip(ctxs, energies))
+    line = {
+        "metric": "Gpix-pass/s, batched uneven charts (64 charts, side 256-2048, 100 iterations)",
+        "value": px * (iters + 1) / (t_b / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+int16", "data": "synthetic (seeded Gaussian densities on disks, uniform sites)",
+        "config": {"workload": "batched_64", "charts": len(charts),
+                   "sides": sorted({int(s.shape[0]) for s, _, _ in charts}),
+                   "pixels": px, "sites": sites_total, "iterations": iters},
+        "solo": {"ms_per_step": t_s, "value": px * (iters + 1) / (t_s / 1e3) / 1e9,
+                 "what": "the same charts one after the other, gcvt_ctx_iterate each"},
+        "batched_over_solo": t_s / t_b,
+        "same_energies_as_solo": same,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    batch.close()
+    for c in ctxs:
+        c.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,11 +473,15 @@ def main():
                     help="also time the reference's own kernels on this GPU")
     ap.add_argument("--profile-case", type=int, default=0, metavar="ITERS",
                     help="only run ITERS Lloyd iterations of the workload (for ncu)")
+    ap.add_argument("--config", default=CONFIG, choices=[CONFIG, "batched_64"],
+                    help="batched_64: the batched-charts workload (its own JSON line)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args.profile_case)
     if args.warmup < 3:
         args.warmup = 3
+    if args.config == "batched_64" and args.impl == "ours":
+        return run_batched(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -127,6 +127,29 @@ int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
 int gcvt_ctx_extract_points(gcvt_ctx *ctx, double scale, double left, double lower, double *xy,
                             int capacity, int *count, int mem);
 
+/* ---- batches: many charts, one launch pair per iteration ---------------
+ * No reference counterpart: the reference runs one chart per gCVT call.  A
+ * batch groups loaded contexts (any mix of sizes, one device); its
+ * iterations run every member's Lloyd iteration in one site-list launch and
+ * one persistent cell launch, the charts' 32-site groups handed out from one
+ * work queue.  Each chart keeps its own schedule (omega, energy, stop), so a
+ * chart's results are the same as from its own context.  Level 0 only
+ * (depth 1); the members are read and written through their contexts
+ * (gcvt_ctx_label, gcvt_ctx_sites, gcvt_ctx_info ...) once the batch call
+ * has returned. */
+typedef struct gcvt_batch gcvt_batch;
+
+int gcvt_batch_create(int count, gcvt_ctx *const *charts, gcvt_batch **out);
+int gcvt_batch_destroy(gcvt_batch *batch);
+/* Stream for the batch's work (a cudaStream_t; NULL = its own stream). */
+int gcvt_batch_set_stream(gcvt_batch *batch, void *stream);
+/* `iterations` plain Lloyd iterations of every member (fixed count). */
+int gcvt_batch_iterate(gcvt_batch *batch, int iterations);
+/* gCVT's schedule on every member at depth 1: each chart runs until its own
+ * stop rule or max_iter (gcvt.cu:1105-1147); infos (may be NULL) receives
+ * one gcvt_run_info per member. */
+int gcvt_batch_run(gcvt_batch *batch, int max_iter, gcvt_run_info *infos);
+
 /* ---- one-call forms ---------------------------------------------------- */
 
 /* gCVT with a status code: host buffers in, label grid out in `voronoi`

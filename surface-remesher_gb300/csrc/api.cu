@@ -15,6 +15,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <new>
+#include <vector>
 
 using namespace cvtgb;
 
@@ -196,7 +198,9 @@ int initial_window(gcvt_ctx *c, int level, int *w) {
 
 // Run one level until the device schedule stops it.  fixed > 0: exactly that
 // many iterations without the stop rule.
-int run_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter, int poll) {
+// Start a level on the device: schedule state (fixed > 0: that many
+// iterations without the stop rule), covering bound, list counts, hints.
+int start_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter) {
   int window = 0;
   int rc = initial_window(c, level, &window);
   if (rc) return rc;
@@ -213,7 +217,12 @@ int run_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter, int poll) 
   h.done_blocks = 0;
   if ((rc = push_state(c))) return rc;
   c->cur_n = n;
-  if ((rc = ensure_cover(c, n, level))) return rc;
+  return ensure_cover(c, n, level);
+}
+
+int run_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter, int poll) {
+  int rc = start_level(c, n, level, fixed, max_iter);
+  if (rc) return rc;
   if (fixed > 0 && !poll) {
     for (int done = 0; done < fixed; done += kChunk)
       if ((rc = enqueue_chunk(c, n, level))) return rc;
@@ -675,6 +684,197 @@ int gcvt_label_grid(const int16_t *sites, int16_t *labels, int n, int mem) {
   if (rc) return rc;
   if ((rc = load_sites(c, n, sites, mem))) return rc;
   return gcvt_ctx_label(c, labels, mem);
+}
+
+// ---- batches: many contexts, one launch pair per iteration ----------------
+
+}  // extern "C"
+
+struct gcvt_batch {
+  int device = 0;
+  std::vector<gcvt_ctx *> charts;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  LevelBufs *descs = nullptr;  // device: one LevelBufs per chart
+  unsigned *lofs = nullptr;    // device: first list block of each chart, and the total
+  unsigned *gofs = nullptr;    // device: first 32-site group of each chart, and the total
+  unsigned *done = nullptr;    // device: list blocks finished
+  unsigned *ticket = nullptr;  // device: next group
+  unsigned nblocks = 0;
+  std::vector<LevelBufs> host_descs;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev = nullptr;    // orders the batch's stream with its members' streams
+};
+
+namespace {
+
+// Level start of every chart on the batch's stream, then the charts' buffer
+// descriptors to the device.
+int batch_start(gcvt_batch *b, int fixed, int max_iter) {
+  std::vector<unsigned> lofs(b->charts.size() + 1, 0);
+  for (size_t i = 0; i < b->charts.size(); ++i) {
+    gcvt_ctx *c = b->charts[i];
+    if (!c->loaded) return GCVT_ERR_STATE;
+    if (c->input_err) return GCVT_ERR_INPUT;
+    if (c->cur_n != c->n) return GCVT_ERR_STATE;
+    // work already queued on the member's own stream comes first
+    CK(cudaEventRecord(b->ev, c->stream));
+    CK(cudaStreamWaitEvent(b->stream, b->ev, 0));
+    cudaStream_t keep = c->stream;
+    c->stream = b->stream;
+    const int rc = start_level(c, c->n, 0, fixed, max_iter);
+    c->stream = keep;
+    if (rc) return rc;
+    b->host_descs[i] = level_bufs(c, c->n, 0);
+    lofs[i + 1] = lofs[i] + (unsigned)list_blocks(c->n);
+  }
+  if (lofs.back() != b->nblocks && b->exec) {  // the captured grid no longer fits
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  b->nblocks = lofs.back();
+  CK(cudaMemcpyAsync(b->descs, b->host_descs.data(), b->host_descs.size() * sizeof(LevelBufs),
+                     cudaMemcpyHostToDevice, b->stream));
+  CK(cudaMemcpyAsync(b->lofs, lofs.data(), lofs.size() * sizeof(unsigned),
+                     cudaMemcpyHostToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return GCVT_OK;
+}
+
+// The members' streams wait for the batch's work.
+int batch_finish(gcvt_batch *b) {
+  CK(cudaEventRecord(b->ev, b->stream));
+  for (gcvt_ctx *c : b->charts) CK(cudaStreamWaitEvent(c->stream, b->ev, 0));
+  return GCVT_OK;
+}
+
+int batch_chunk(gcvt_batch *b) {
+  const int nc = (int)b->charts.size();
+  if (!b->exec) {
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      for (int i = 0; i < kChunk; ++i) {
+        CK(launch_list_batch(b->descs, nc, b->lofs, b->nblocks, b->gofs, b->done, b->ticket,
+                             b->stream));
+        CK(launch_cells_batch(b->descs, nc, b->gofs, b->ticket, b->stream));
+      }
+      return GCVT_OK;
+    }
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < kChunk && le == cudaSuccess; ++i) {
+      le = launch_list_batch(b->descs, nc, b->lofs, b->nblocks, b->gofs, b->done, b->ticket,
+                             b->stream);
+      if (le == cudaSuccess) le = launch_cells_batch(b->descs, nc, b->gofs, b->ticket, b->stream);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return GCVT_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      b->exec = nullptr;
+      return GCVT_ERR_CUDA;
+    }
+  }
+  CK(cudaGraphLaunch(b->exec, b->stream));
+  return GCVT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gcvt_batch_create(int count, gcvt_ctx *const *charts, gcvt_batch **out) {
+  if (!out || count < 1 || !charts) return GCVT_ERR_ARGUMENT;
+  *out = nullptr;
+  gcvt_batch *b = new (std::nothrow) gcvt_batch();
+  if (!b) return GCVT_ERR_ALLOC;
+  auto fail = [&](int code) {
+    gcvt_batch_destroy(b);
+    return code;
+  };
+  if (cudaGetDevice(&b->device) != cudaSuccess) return fail(GCVT_ERR_CUDA);
+  for (int i = 0; i < count; ++i) {
+    gcvt_ctx *c = charts[i];
+    if (!c) return fail(GCVT_ERR_ARGUMENT);
+    if (c->device != b->device) return fail(GCVT_ERR_ARGUMENT);
+    for (gcvt_ctx *d : b->charts)
+      if (d == c) return fail(GCVT_ERR_ARGUMENT);  // a context appears once
+    b->charts.push_back(c);
+  }
+  b->host_descs.resize(count);
+  if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(GCVT_ERR_CUDA);
+  b->stream = b->own_stream;
+  bool ok = cudaMalloc(reinterpret_cast<void **>(&b->descs), count * sizeof(LevelBufs)) == cudaSuccess;
+  ok = ok && cudaMalloc(reinterpret_cast<void **>(&b->lofs), (count + 1) * sizeof(unsigned)) == cudaSuccess;
+  ok = ok && cudaMalloc(reinterpret_cast<void **>(&b->gofs), (count + 1) * sizeof(unsigned)) == cudaSuccess;
+  ok = ok && cudaMalloc(reinterpret_cast<void **>(&b->done), 2 * sizeof(unsigned)) == cudaSuccess;
+  if (!ok) return fail(GCVT_ERR_ALLOC);
+  b->ticket = b->done + 1;
+  if (cudaMemset(b->done, 0, 2 * sizeof(unsigned)) != cudaSuccess) return fail(GCVT_ERR_CUDA);
+  if (cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming) != cudaSuccess)
+    return fail(GCVT_ERR_CUDA);
+  *out = b;
+  return GCVT_OK;
+}
+
+int gcvt_batch_destroy(gcvt_batch *b) {
+  if (!b) return GCVT_ERR_ARGUMENT;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  cudaFree(b->descs);
+  cudaFree(b->lofs);
+  cudaFree(b->gofs);
+  cudaFree(b->done);
+  if (b->ev) cudaEventDestroy(b->ev);
+  if (b->own_stream) cudaStreamDestroy(b->own_stream);
+  delete b;
+  return GCVT_OK;
+}
+
+int gcvt_batch_set_stream(gcvt_batch *b, void *stream) {
+  if (!b) return GCVT_ERR_ARGUMENT;
+  b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+  return GCVT_OK;
+}
+
+int gcvt_batch_iterate(gcvt_batch *b, int iterations) {
+  if (!b || iterations < 0) return GCVT_ERR_ARGUMENT;
+  if (iterations == 0) return GCVT_OK;
+  int rc = batch_start(b, iterations, 0x7fffffff);
+  if (rc) return rc;
+  for (int done = 0; done < iterations; done += kChunk)
+    if ((rc = batch_chunk(b))) return rc;
+  return batch_finish(b);
+}
+
+int gcvt_batch_run(gcvt_batch *b, int max_iter, gcvt_run_info *infos) {
+  if (!b) return GCVT_ERR_ARGUMENT;
+  int rc = batch_start(b, 0, max_iter);
+  if (rc) return rc;
+  for (;;) {
+    if ((rc = batch_chunk(b))) return rc;
+    bool all = true;
+    for (gcvt_ctx *c : b->charts) {
+      cudaStream_t keep = c->stream;
+      c->stream = b->stream;
+      rc = pull_state(c);
+      c->stream = keep;
+      if (rc) return rc;
+      all = all && c->st_host->stopped;
+    }
+    if (all) break;
+  }
+  if ((rc = batch_finish(b))) return rc;
+  for (size_t i = 0; i < b->charts.size(); ++i) {
+    b->charts[i]->last_levels = 1;
+    if (infos && (rc = gcvt_ctx_info(b->charts[i], infos + i))) return rc;
+  }
+  return GCVT_OK;
 }
 
 }  // extern "C"

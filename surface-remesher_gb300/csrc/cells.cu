@@ -404,36 +404,156 @@ __device__ void run_schedule(DevState *st, double E, unsigned r2, unsigned mv, i
   __threadfence();
 }
 
-// MODE 0: one Lloyd iteration (sums, move, energy, schedule).
-// MODE 1: sums only, written as doubles (W, X, Y, E) at each site pixel of
-//         out4 (four n*n planes); the sites do not move.
+// What one chart's iteration reads at its start.
+struct IterView {
+  const uint64_t *bits;  // current sites
+  uint64_t *nxt;         // where the moved sites go
+  unsigned *cnt_nxt;     // their per-list-block counts
+  float omega;
+  int W0, rb, nsites, cur;
+  unsigned ngroups;      // 32-site groups of the list
+};
+
+__device__ __forceinline__ IterView iter_view(const LevelBufs &a) {
+  const DevState *st = a.st;
+  IterView v;
+  v.cur = st->snap_cur;
+  v.bits = bits_at(a, v.cur);
+  v.nxt = bits_at(a, v.cur == 2 ? 0 : v.cur + 1);
+  v.cnt_nxt = counts_at(a, v.cur == 2 ? 0 : v.cur + 1);
+  v.omega = st->snap_omega;
+  v.W0 = st->snap_window;
+  v.rb = st->snap_cover;
+  v.nsites = st->snap_count;
+  v.ngroups = (unsigned)(v.nsites + 31) / 32;
+  return v;
+}
+
+// The snapshot k_cell reads (k_list, before the iteration; thread 0 of the
+// chart's first list block).  A stopped chart records only that it stopped.
+__device__ __forceinline__ void take_snapshot(DevState *st) {
+  st->snap_stopped = st->stopped;
+  st->snap_cur = st->cur;
+  st->snap_omega = st->omega;
+  st->snap_window = st->window;
+  st->snap_cover = st->cover;
+}
+
+// Clear the bitmap and counts the next iteration writes (nobody reads them
+// in this one); this thread's grid-stride share.
+__device__ __forceinline__ void clear_ahead(const LevelBufs &a, int cur, size_t t0,
+                                            size_t gthreads) {
+  const size_t nwords = (size_t)(a.n / kBand) * a.n;
+  uint64_t *zro = bits_at(a, cur == 0 ? 2 : cur - 1);
+  unsigned *czro = counts_at(a, cur == 0 ? 2 : cur - 1);
+  for (size_t i = t0; i < nwords; i += gthreads) zro[i] = 0ull;
+  const size_t nlb = (nwords + kListWords - 1) / kListWords;
+  for (size_t i = t0; i < nlb; i += gthreads) czro[i] = 0u;
+}
+
+// Group g of a chart (32 listed sites, one per lane).  MODE 0: cells, moves,
+// and the group's share of the energy reduction; the warp that completes the
+// chart's last 64-group runs its schedule.  MODE 1: moments only, written as
+// doubles (W, X, Y, E) at each site pixel of out4 (four n*n planes).
+template <int MODE>
+__device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, int lane,
+                           double *out4) {
+  const int n = a.n;
+  float eh = 0.f, el = 0.f;
+  unsigned r2 = 0, mv = 0;
+  const int idx = (int)g * 32 + lane;
+  if (idx < v.nsites) {
+    const uint32_t e = a.list[idx];
+    const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
+    const size_t pid = (size_t)sy * n + sx;
+    const int h = a.hint[pid];
+    const CellSums cs = cell_sums(a, v.bits, n, sx, sy, h ? h : v.W0, v.rb);
+    if (MODE == 1) {
+      const size_t nn = (size_t)n * n;
+      const double Wd = (double)cs.wh + (double)cs.wl;
+      out4[pid] = Wd;
+      out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
+      out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
+      out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
+    } else {
+      dfa(eh, el, cs.eh, cs.el);
+      const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
+      const float cy = cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl);
+      const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)sx), v.omega, (float)sx), 0.5f);
+      const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)sy), v.omega, (float)sy), 0.5f);
+      int nx = min(max(__float2int_rz(fx), 0), n - 1);
+      int ny = min(max(__float2int_rz(fy), 0), n - 1);
+      if ((e & 0x8000u) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = sx; ny = sy; }
+      r2 = (unsigned)cs.r2;
+      mv = (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy));
+      const size_t widx = (size_t)(ny / kBand) * n + nx;
+      const unsigned long long bit = 1ull << (ny % kBand);
+      const unsigned long long old =
+          atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
+      if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
+      a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 2, 255);
+    }
+  }
+  __syncwarp();
+  if (MODE == 1) return;
+  DevState *st = a.st;
+  warp_reduce(eh, el, r2, mv);
+  // group total -> slot; the warp finishing the last group of a 64-group
+  // reduces the 64 slots; the warp finishing the last 64-group totals them
+  int last = 0;
+  const unsigned sg = g / kGroupsPerSlot;
+  const unsigned sbase = sg * kGroupsPerSlot;
+  const unsigned starget = min((unsigned)kGroupsPerSlot, v.ngroups - sbase);
+  if (lane == 0) {
+    a.gslot[g] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
+    __threadfence();
+    last = atomicAdd(a.scnt + sg, 1u) == starget - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence();
+  eh = el = 0.f;
+  r2 = mv = 0;
+  for (unsigned k = lane; k < starget; k += 32) {
+    const float4 q = __ldcg(a.gslot + sbase + k);
+    dfa(eh, el, q.x, q.y);
+    r2 = max(r2, __float_as_uint(q.z));
+    mv = max(mv, __float_as_uint(q.w));
+  }
+  warp_reduce(eh, el, r2, mv);
+  const unsigned nslots = (v.ngroups + kGroupsPerSlot - 1) / kGroupsPerSlot;
+  last = 0;
+  if (lane == 0) {
+    a.sslot[sg] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
+    a.scnt[sg] = 0u;
+    __threadfence();
+    last = atomicAdd(&st->done_blocks, 1u) == nslots - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence();
+  eh = el = 0.f;
+  r2 = mv = 0;
+  for (unsigned k = lane; k < nslots; k += 32) {
+    const float4 q = __ldcg(a.sslot + k);
+    dfa(eh, el, q.x, q.y);
+    r2 = max(r2, __float_as_uint(q.z));
+    mv = max(mv, __float_as_uint(q.w));
+  }
+  warp_reduce(eh, el, r2, mv);
+  if (lane == 0) run_schedule(st, ((double)eh + (double)el) * st->energy_scale, r2, mv, n, v.cur);
+}
+
+// One chart.  MODE 0: one Lloyd iteration (sums, move, energy, schedule).
+// MODE 1: moments only (gcvt_ctx_moments); the sites do not move.
 template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
   DevState *st = a.st;
-  if (MODE == 0 && st->stopped) return;
-  const int n = a.n;
+  if (MODE == 0 && st->snap_stopped) return;
   const int lane = threadIdx.x;
-  const int cur = st->cur;
-  const uint64_t *bits = bits_at(a, cur);
-  uint64_t *nxt = bits_at(a, cur == 2 ? 0 : cur + 1);
-  unsigned *cnt_nxt = counts_at(a, cur == 2 ? 0 : cur + 1);
-  const float omega = st->omega;
-  const int W0 = st->window;
-  const int rb = st->cover;
-  const int nsites = st->list_count;
-  const unsigned ngroups = (unsigned)(nsites + 31) / 32;
+  const IterView v = iter_view(a);
   if (MODE == 0) {
-    // the buffers the next iteration writes; nobody reads them now
-    const size_t nwords = (size_t)(n / kBand) * n;
-    const size_t gthreads = (size_t)gridDim.x * 32;
-    uint64_t *zro = bits_at(a, cur == 0 ? 2 : cur - 1);
-    unsigned *czro = counts_at(a, cur == 0 ? 2 : cur - 1);
-    const size_t t0 = (size_t)blockIdx.x * 32 + lane;
-    for (size_t i = t0; i < nwords; i += gthreads) zro[i] = 0ull;
-    const size_t nlb = (nwords + kListWords - 1) / kListWords;
-    for (size_t i = t0; i < nlb; i += gthreads) czro[i] = 0u;
-    if (ngroups == 0) {  // no sites: the schedule still advances
-      if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, n, cur);
+    clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
+    if (v.ngroups == 0) {  // no sites: the schedule still advances
+      if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, v.cur);
       return;
     }
   }
@@ -441,113 +561,69 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
     unsigned g = 0;
     if (lane == 0) g = atomicAdd(&st->ticket, 1u);
     g = __shfl_sync(0xffffffffu, g, 0);
-    if (g >= ngroups) break;
-    float eh = 0.f, el = 0.f;
-    unsigned r2 = 0, mv = 0;
-    const int idx = (int)g * 32 + lane;
-    if (idx < nsites) {
-      const uint32_t e = a.list[idx];
-      const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
-      const size_t pid = (size_t)sy * n + sx;
-      const int h = a.hint[pid];
-      const CellSums cs = cell_sums(a, bits, n, sx, sy, h ? h : W0, rb);
-      if (MODE == 1) {
-        const size_t nn = (size_t)n * n;
-        const double Wd = (double)cs.wh + (double)cs.wl;
-        out4[pid] = Wd;
-        out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
-        out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
-        out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
-      } else {
-        dfa(eh, el, cs.eh, cs.el);
-        const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
-        const float cy = cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl);
-        const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)sx), omega, (float)sx), 0.5f);
-        const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)sy), omega, (float)sy), 0.5f);
-        int nx = min(max(__float2int_rz(fx), 0), n - 1);
-        int ny = min(max(__float2int_rz(fy), 0), n - 1);
-        if ((e & 0x8000u) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = sx; ny = sy; }
-        r2 = max(r2, (unsigned)cs.r2);
-        mv = max(mv, (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy)));
-        const size_t widx = (size_t)(ny / kBand) * n + nx;
-        const unsigned long long bit = 1ull << (ny % kBand);
-        const unsigned long long old =
-            atomicOr(reinterpret_cast<unsigned long long *>(nxt + widx), bit);
-        if (!(old & bit)) atomicAdd(cnt_nxt + widx / kListWords, 1u);
-        a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 2, 255);
-      }
-    }
-    __syncwarp();
-    if (MODE == 1) continue;
-    warp_reduce(eh, el, r2, mv);
-    // group total -> slot; the warp finishing the last group of a 64-group
-    // reduces the 64 slots; the warp finishing the last 64-group totals them
-    int last = 0;
-    const unsigned sg = g / kGroupsPerSlot;
-    const unsigned sbase = sg * kGroupsPerSlot;
-    const unsigned starget = min((unsigned)kGroupsPerSlot, ngroups - sbase);
-    if (lane == 0) {
-      a.gslot[g] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
-      __threadfence();
-      last = atomicAdd(a.scnt + sg, 1u) == starget - 1;
-    }
-    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
-    __threadfence();
-    eh = el = 0.f;
-    r2 = mv = 0;
-    for (unsigned k = lane; k < starget; k += 32) {
-      const float4 v = __ldcg(a.gslot + sbase + k);
-      dfa(eh, el, v.x, v.y);
-      r2 = max(r2, __float_as_uint(v.z));
-      mv = max(mv, __float_as_uint(v.w));
-    }
-    warp_reduce(eh, el, r2, mv);
-    const unsigned nslots = (ngroups + kGroupsPerSlot - 1) / kGroupsPerSlot;
-    last = 0;
-    if (lane == 0) {
-      a.sslot[sg] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
-      a.scnt[sg] = 0u;
-      __threadfence();
-      last = atomicAdd(&st->done_blocks, 1u) == nslots - 1;
-    }
-    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
-    __threadfence();
-    eh = el = 0.f;
-    r2 = mv = 0;
-    for (unsigned k = lane; k < nslots; k += 32) {
-      const float4 v = __ldcg(a.sslot + k);
-      dfa(eh, el, v.x, v.y);
-      r2 = max(r2, __float_as_uint(v.z));
-      mv = max(mv, __float_as_uint(v.w));
-    }
-    warp_reduce(eh, el, r2, mv);
-    if (lane == 0) run_schedule(st, ((double)eh + (double)el) * st->energy_scale, r2, mv, n, cur);
+    if (g >= v.ngroups) break;
+    cell_group<MODE>(a, v, g, lane, out4);
   }
 }
 
-// Site list of the current bitmap in bitmap order (word by word, bits in
-// row order), with the fixed flag; block b covers words
-// [b kListWords, (b+1) kListWords) and finds its offset from the per-block
-// counts.  Also rearms the Lloyd kernel's ticket.
-__global__ void __launch_bounds__(256) k_list(LevelBufs a, int respect_stop) {
+// Many charts, one launch: the groups of all charts that have not stopped form
+// one sequence (group offsets per chart from k_list_batch, gofs[c] .. gofs[c+1]),
+// handed out by one ticket; each chart keeps its own state, reduction and
+// schedule, so a chart's iteration is the same as in k_cell.
+__global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restrict__ charts,
+                                                       int nchart,
+                                                       const unsigned *__restrict__ gofs,
+                                                       unsigned *ticket) {
+  const int lane = threadIdx.x;
+  const size_t t0 = (size_t)blockIdx.x * 32 + lane, gthreads = (size_t)gridDim.x * 32;
+  for (int c = 0; c < nchart; ++c) {
+    const LevelBufs &a = charts[c];
+    DevState *st = a.st;
+    if (st->snap_stopped) continue;
+    const int cur = st->snap_cur;
+    clear_ahead(a, cur, t0, gthreads);
+    if (st->snap_count == 0 && blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, cur);
+  }
+  const unsigned total = gofs[nchart];
+  for (;;) {
+    unsigned g = 0;
+    if (lane == 0) g = atomicAdd(ticket, 1u);
+    g = __shfl_sync(0xffffffffu, g, 0);
+    if (g >= total) break;
+    int lo = 0, hi = nchart - 1;  // the chart c with gofs[c] <= g < gofs[c + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(gofs + mid) <= g) lo = mid;
+      else hi = mid - 1;
+    }
+    const LevelBufs &a = charts[lo];
+    const IterView v = iter_view(a);
+    cell_group<0>(a, v, g - __ldg(gofs + lo), lane, nullptr);
+  }
+}
+
+// Block `blk` of a chart's site list: the sites of bitmap words
+// [blk kListWords, (blk+1) kListWords) in bitmap order (word by word, bits in
+// row order) with the fixed flag, at the offset the per-block counts give.
+// The chart's last block records the list length.
+__device__ void list_block(const LevelBufs &a, unsigned blk, unsigned nblk) {
   constexpr int kPer = kListWords / 256;
   __shared__ unsigned wsum[8];
   __shared__ unsigned base_s;
   DevState *st = a.st;
-  if (respect_stop && st->stopped) return;
   const int n = a.n;
   const int cur = st->cur;
   const uint64_t *bits = bits_at(a, cur);
   const unsigned *counts = counts_at(a, cur);
   const size_t nwords = (size_t)(n / kBand) * n;
   const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
-  if (blockIdx.x == 0 && tid == 0) {
-    st->ticket = 0u;
+  if (blk == 0 && tid == 0) {
     st->done_blocks = 0u;
+    take_snapshot(st);
   }
   // offset of this block: the counts of the blocks before it
   unsigned pre = 0;
-  for (unsigned k = tid; k < blockIdx.x; k += 256) pre += counts[k];
+  for (unsigned k = tid; k < blk; k += 256) pre += counts[k];
   pre = __reduce_add_sync(0xffffffffu, pre);
   if (lane == 0) wsum[wib] = pre;
   __syncthreads();
@@ -559,7 +635,7 @@ __global__ void __launch_bounds__(256) k_list(LevelBufs a, int respect_stop) {
   __syncthreads();
   const unsigned base = base_s;
   // this thread's words and their sites
-  const size_t w0 = (size_t)blockIdx.x * kListWords + (size_t)tid * kPer;
+  const size_t w0 = (size_t)blk * kListWords + (size_t)tid * kPer;
   uint64_t w[kPer];
   unsigned cnt = 0;
 #pragma unroll
@@ -601,7 +677,61 @@ __global__ void __launch_bounds__(256) k_list(LevelBufs a, int respect_stop) {
       ++pos;
     }
   }
-  if (blockIdx.x == gridDim.x - 1 && tid == 0) st->list_count = (int)min(base + total, cap);
+  if (blk == nblk - 1 && tid == 0) st->list_count = st->snap_count = (int)min(base + total, cap);
+  __syncthreads();  // the shared scratch may be reused by the caller
+}
+
+// One chart's site list; also rearms the chart's ticket.  respect_stop = 0
+// lists a stopped chart too (moments, point extraction) and marks the
+// snapshot running.
+__global__ void __launch_bounds__(256) k_list(LevelBufs a, int respect_stop) {
+  DevState *st = a.st;
+  if (respect_stop && st->stopped) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->snap_stopped = 1;
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->ticket = 0u;
+  list_block(a, blockIdx.x, gridDim.x);
+  if (!respect_stop && blockIdx.x == 0 && threadIdx.x == 0) st->snap_stopped = 0;
+}
+
+// The site lists of many charts: chart c owns blocks lofs[c] .. lofs[c+1].
+// The block that finishes last lays out the group offsets of the charts that
+// run (gofs) for k_cell_batch and rearms its ticket.
+__global__ void __launch_bounds__(256) k_list_batch(const LevelBufs *__restrict__ charts,
+                                                    int nchart,
+                                                    const unsigned *__restrict__ lofs,
+                                                    unsigned *gofs, unsigned *done,
+                                                    unsigned *ticket) {
+  __shared__ bool is_last;
+  int lo = 0, hi = nchart - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(lofs + mid) <= blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const LevelBufs &a = charts[lo];
+  const unsigned blk = blockIdx.x - __ldg(lofs + lo);
+  if (!a.st->stopped) list_block(a, blk, __ldg(lofs + lo + 1) - __ldg(lofs + lo));
+  else if (blk == 0 && threadIdx.x == 0) a.st->snap_stopped = 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    is_last = atomicAdd(done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!is_last || threadIdx.x != 0) return;
+  __threadfence();
+  unsigned acc = 0;
+  for (int c = 0; c < nchart; ++c) {
+    gofs[c] = acc;
+    const DevState *st = charts[c].st;
+    const int cnt = *((volatile const int *)&st->snap_count);
+    if (!*((volatile const int *)&st->snap_stopped)) acc += (unsigned)(cnt + 31) / 32;
+  }
+  gofs[nchart] = acc;
+  *ticket = 0u;
+  *done = 0u;
+  __threadfence();
 }
 
 // Per-block site counts of the current bitmap (for the first k_list of a
@@ -702,8 +832,33 @@ cudaError_t cells_configure() {
     return e;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_cell<1>, 32, 0)) != cudaSuccess)
     return e;
+  int per2 = 0;
+  if ((e = cudaFuncSetAttribute(k_cell_batch, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                carve)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_cell_batch, 32, 0)) !=
+      cudaSuccess)
+    return e;
+  per0 = min(per0, per2);
   g_cell_grid[dev] = sms * max(1, min(per0, per1));
   return cudaSuccess;
+}
+
+cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigned *lofs,
+                              unsigned nblocks, unsigned *gofs, unsigned *done, unsigned *ticket,
+                              cudaStream_t s) {
+  k_list_batch<<<nblocks, 256, 0, s>>>(charts, nchart, lofs, gofs, done, ticket);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
+                               unsigned *ticket, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
+  k_cell_batch<<<g_cell_grid[dev], 32, 0, s>>>(charts, nchart, gofs, ticket);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s) {

@@ -51,6 +51,11 @@ struct DevState {
   unsigned cover_acc;  // max |p - owner(p)|^2 from the labels (k_cover)
   int list_count;      // sites in the site list (k_list)
   unsigned ticket;     // next 32-site group of the Lloyd kernel
+  // The iteration's own view, copied by k_list before the iteration's k_cell
+  // runs: the schedule (last warp of k_cell) changes the fields above for
+  // the next iteration while other warps of the same launch may still start.
+  int snap_cur, snap_stopped, snap_window, snap_cover, snap_count;
+  float snap_omega;
 };
 
 // Buffers of one resolution level, passed by value to every kernel.
@@ -101,6 +106,11 @@ cudaError_t rows_configure();
 cudaError_t launch_extract(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *colcnt,
                            double scale, double left, double lower, double *xy,
                            unsigned capacity, unsigned *total, cudaStream_t s);
+cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigned *lofs,
+                              unsigned nblocks, unsigned *gofs, unsigned *done, unsigned *ticket,
+                              cudaStream_t s);
+cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
+                               unsigned *ticket, cudaStream_t s);
 cudaError_t cells_configure();
 size_t list_blocks(int n);
 size_t cell_groups(int n);

@@ -67,6 +67,11 @@ SIGNATURES = {
     "gcvt_ctx_extract_points": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I,
                                  ctypes.POINTER(I), I], I),
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
+    "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
+    "gcvt_batch_destroy": ([P], I),
+    "gcvt_batch_set_stream": ([P, P], I),
+    "gcvt_batch_iterate": ([P, I], I),
+    "gcvt_batch_run": ([P, I, P], I),
     "gcvt_centroidal_voronoi": ([P, P, P, I, I, I, I], I),
 }
 CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii",
@@ -227,6 +232,42 @@ def gcvt(voronoi, density, mask, depth=1, max_iter=1000):
                             _host_ptr(mask, np.uint8, (n, n)), n, int(depth), int(max_iter)),
            "gcvt_compute")
     return voronoi
+
+
+class Batch:
+    """Several loaded Contexts iterated together (gcvt_batch_*): one launch
+    pair per iteration for all of them; results are read through the
+    Contexts."""
+
+    def __init__(self, contexts):
+        self.lib = load_library()
+        self.contexts = list(contexts)
+        arr = (P * len(self.contexts))(*[c.h for c in self.contexts])
+        self.h = P()
+        _check(self.lib.gcvt_batch_create(len(self.contexts), arr, ctypes.byref(self.h)),
+               "gcvt_batch_create")
+
+    def set_stream(self, stream):
+        _check(self.lib.gcvt_batch_set_stream(self.h, stream), "gcvt_batch_set_stream")
+
+    def iterate(self, iterations):
+        _check(self.lib.gcvt_batch_iterate(self.h, int(iterations)), "gcvt_batch_iterate")
+
+    def run(self, max_iter=1000):
+        infos = (RunInfo * len(self.contexts))()
+        _check(self.lib.gcvt_batch_run(self.h, int(max_iter), infos), "gcvt_batch_run")
+        return [i.as_dict() for i in infos]
+
+    def close(self):
+        if self.h:
+            self.lib.gcvt_batch_destroy(self.h)
+            self.h = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def seed_sites(density, mask, num, state=None):

@@ -24,6 +24,27 @@ CONFIGS = {
 }
 
 
+# Batched uneven charts: 64 charts, side drawn from SIDES, config-0 density
+# family (8 Gaussians), sites = domain pixels / 64, 100 iterations.
+BATCH = dict(charts=64, sides=(256, 512, 1024, 2048), k=8, a_max=4.0, s_lo=0.02, s_hi=0.15,
+             px_per_site=64, iters=100)
+
+
+def batched_inputs(seed=1, charts=None):
+    """[(sites, density, mask)] of the batched configuration: chart i has a
+    seeded side from BATCH['sides'] and density seed seed * 1000 + i."""
+    c = BATCH
+    count = c["charts"] if charts is None else charts
+    rng = np.random.default_rng(seed)
+    sides = rng.choice(c["sides"], size=count)
+    out = []
+    for i, n in enumerate(sides.tolist()):
+        rho = gaussian_density(n, c["k"], c["a_max"], c["s_lo"], c["s_hi"], seed * 1000 + i)
+        m = int((rho > 0).sum()) // c["px_per_site"]
+        out.append((disk_sites(n, m, seed * 1000 + i, rho), rho, np.zeros((n, n), np.uint8)))
+    return out
+
+
 def disk_mask(n, radius=0.48):
     c = (np.arange(n) + 0.5) / n
     X, Y = np.meshgrid(c, c)
@@ -64,10 +85,12 @@ def disk_sites(n, m, seed, density=None, radius=0.48):
     return g
 
 
-def mesh_inputs(nv=256, n=2048, sites=65536, seed=2):
-    """Mesh-driven configuration: the rasterised area-ratio density of a
-    jittered disk mesh (see disk_mesh) and sites uniform over its support.
-    Returns (mesh tuple (points, weight, triangles, scale), sites, mask)."""
+def mesh_inputs(nv=256, n=2048, seed=2):
+    """Mesh-driven configuration inputs before rasterisation: the jittered
+    disk mesh of disk_mesh with its per-vertex area-ratio weights, shifted and
+    scaled as discretization.h marshals them.  Returns ((points, weight,
+    triangles, scale), mask); the density comes from rasterising the mesh
+    and the sites from disk_sites over that density."""
     P, w, T = disk_mesh(nv, seed=seed)
     Q, scale, _, _ = raster_inputs(P, n)
     return (Q, w, T, scale), np.zeros((n, n), np.uint8)
