@@ -75,6 +75,27 @@ def support_pixels(rho):
     return int(((last - first + 1) * rows).sum())
 
 
+def jfa_line(n, ms, stats, peak):
+    """Jump-flooding labelling of the workload's sites: logical passes n/2 ..
+    1 plus 1, launches = passes >= 16 plus one fused tail (8, 4, 2, 1, 1);
+    algorithmic 8 B per pixel per launch (labels in and out)."""
+    k, passes = 1, 1
+    while 2 * k <= n // 2:
+        k *= 2
+    while k >= 1:
+        passes += 1
+        k //= 2
+    launches = passes - 5 + 1
+    alg = 8.0 * n * n * launches
+    return {"ms": ms, "logical_passes": passes, "launches": launches,
+            "gpix_pass_per_s": n * n * passes / (ms / 1e3) / 1e9,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
+                         "algorithmic_bytes": alg},
+            "mislabelled_px": stats[0], "farther_px": stats[1], "pixels": stats[2],
+            "mislabel_rate": stats[0] / stats[2], "farther_rate": stats[1] / stats[2]}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -274,8 +295,10 @@ def run_ours(args):
         for _ in range(max(1, args.warmup // 2)):
             step_host()
         t_e2e = timed(step_host, args.steps)
-        # a labelling pass (final output), timed alone
+        # a labelling pass (final output) and a jump-flooding labelling,
+        # timed alone; the jump-flooding error on the initial sites
         ctx.load(d_sites, d_rho, d_mask)
+        _, jfa_stats = ctx.jfa_label(labels=False)
         kms = ctx.time_kernels(5)
         torch.cuda.synchronize(dev)
     if ws > 1:
@@ -300,7 +323,8 @@ def run_ours(args):
                    "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
                    "parallelism": "replicas x%d" % ws},
         "iter_per_s": ITERS * args.steps * ws / t_dev,
-        "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1]},
+        "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1], "jfa_labelling": kms[2]},
+        "jfa": jfa_line(n, kms[2], jfa_stats, peak),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
                      "peak_source": peak_kind,

@@ -107,13 +107,24 @@ int gcvt_ctx_sites(gcvt_ctx *ctx, int16_t *voronoi, int mem);
 int gcvt_ctx_moments(gcvt_ctx *ctx, double *out4, int mem);
 
 /* Run `iterations` plain Lloyd iterations as separate launches, each
- * followed by a labelling pass, and return in ms3 the mean duration (ms) of
- * [0] one Lloyd iteration (one kernel), [1] one labelling pass (column
- * summaries + rows), [2] 0 -- timed with CUDA events on the context's
- * stream.  The sites advance as in gcvt_ctx_iterate.  No reference
+ * followed by a labelling pass, then as many jump-flooding labellings of the
+ * final sites, and return in ms3 the mean duration (ms) of [0] one Lloyd
+ * iteration (site list + cells), [1] one exact labelling pass (column
+ * summaries + rows), [2] one jump-flooding labelling (its step launches and
+ * fused tail) -- timed with CUDA events on the context's stream.  The sites advance as in gcvt_ctx_iterate.  No reference
  * counterpart: the reference times nothing (gcvt.cu:27 includes a timer
  * header it never uses). */
 int gcvt_ctx_time_kernels(gcvt_ctx *ctx, int iterations, float *ms3);
+
+/* Jump-flooding labels of the current sites (approximate; no reference
+ * counterpart -- the reference labels exactly with PBA+): steps n/2 ... 1
+ * (from the largest power of two <= n/2) plus one more step of 1, each pixel
+ * taking the nearest of the nine labels
+ * at offsets (dx, dy) * k, ties to the smaller x, then y.  labels (may be
+ * NULL) receives the n*n label grid.  stats (may be NULL) receives, against
+ * the exact labels of gcvt_ctx_label: [0] pixels whose label differs,
+ * [1] pixels whose label is strictly farther than the exact one's, [2] n*n. */
+int gcvt_ctx_jfa_label(gcvt_ctx *ctx, int16_t *labels, unsigned long long *stats, int mem);
 
 /* Schedule state (iterations, omega, energies). */
 int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);

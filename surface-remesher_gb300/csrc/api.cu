@@ -48,6 +48,7 @@ struct gcvt_ctx {
   float4 *gslot = nullptr, *sslot = nullptr;
   unsigned *scnt = nullptr;
   unsigned *colcnt = nullptr;   // point extraction: n_max column counts + total
+  uint32_t *jfa = nullptr;      // jump flooding: two n_max^2 label grids + counters
   int cover_valid = 0;          // the covering bound, list counts and hints
                                 // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
@@ -414,6 +415,7 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->sslot);
   cudaFree(c->scnt);
   cudaFree(c->colcnt);
+  cudaFree(c->jfa);
   cudaFree(c->moments);
   cudaFree(c->err);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -571,6 +573,45 @@ int gcvt_ctx_extract_points(gcvt_ctx *c, double scale, double left, double lower
   return GCVT_OK;
 }
 
+int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, int mem) {
+  if (!c || (!labels && !stats)) return GCVT_ERR_ARGUMENT;
+  if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  const size_t nmax2 = (size_t)c->n_max * c->n_max;
+  if (!c->jfa && cudaMalloc(reinterpret_cast<void **>(&c->jfa),
+                            2 * nmax2 * sizeof(uint32_t) + 64) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  const int n = c->cur_n;
+  uint32_t *a = c->jfa, *b = c->jfa + nmax2;
+  unsigned long long *counts = reinterpret_cast<unsigned long long *>(c->jfa + 2 * nmax2);
+  CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+  CK(launch_bits_to_grid(c->bits[c->st_host->cur], n, a, c->stream));
+  uint32_t *res = nullptr;
+  CK(launch_jfa(a, b, n, c->err, &res, c->stream));
+  if (stats) {
+    const LevelBufs lb = level_bufs(c, n, level_of(c, n));
+    CK(launch_summary(lb, 0, c->stream));
+    CK(launch_rows(lb, 0, c->stream));  // exact labels into the staging grid
+    CK(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), c->stream));
+    CK(launch_jfa_compare(res, c->grid, n, counts, c->stream));
+    unsigned long long h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    stats[0] = h[0];
+    stats[1] = h[1];
+    stats[2] = (unsigned long long)n * n;
+  }
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (herr) return GCVT_ERR_CUDA;  // a tile copy did not arrive
+  if (labels) return copy_out(labels, res, (size_t)n * n * sizeof(uint32_t), mem, c->stream);
+  return GCVT_OK;
+}
+
 int gcvt_ctx_info(gcvt_ctx *c, gcvt_run_info *info) {
   if (!c) return GCVT_ERR_ARGUMENT;
   if (!info) return GCVT_OK;
@@ -585,9 +626,9 @@ int gcvt_ctx_info(gcvt_ctx *c, gcvt_run_info *info) {
 }
 
 // Mean device time of (one Lloyd iteration: site list + cells, one labelling
-// pass) over `iterations` iterations at full resolution, each bracketed by
-// events on the context's stream; ms3[2] is 0.  The sites move as in
-// gcvt_ctx_iterate.
+// pass, one jump-flooding labelling) over `iterations` iterations at full
+// resolution, each bracketed by events on the context's stream.  The sites
+// move as in gcvt_ctx_iterate.
 int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
   if (!c || !ms3 || iterations < 1) return GCVT_ERR_ARGUMENT;
   if (!c->loaded) return GCVT_ERR_STATE;
@@ -632,11 +673,32 @@ int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
     acc[0] += ms0;
     acc[1] += ms1;
   }
+  // jump flooding of the sites now held, kernels only
+  float acc2 = 0.f;
+  const size_t nmax2 = (size_t)c->n_max * c->n_max;
+  if (status == GCVT_OK && !c->jfa &&
+      cudaMalloc(reinterpret_cast<void **>(&c->jfa), 2 * nmax2 * sizeof(uint32_t) + 64) !=
+          cudaSuccess)
+    status = GCVT_ERR_ALLOC;
+  if (status == GCVT_OK && (status = pull_state(c)) == GCVT_OK) {
+    uint32_t *ja = c->jfa, *jb = c->jfa + nmax2, *res = nullptr;
+    for (int it = 0; it < iterations && status == GCVT_OK; ++it) {
+      float ms = 0.f;
+      if (launch_bits_to_grid(c->bits[c->st_host->cur], c->n, ja, c->stream) != cudaSuccess ||
+          cudaEventRecord(ev[0], c->stream) != cudaSuccess ||
+          launch_jfa(ja, jb, c->n, c->err, &res, c->stream) != cudaSuccess ||
+          cudaEventRecord(ev[1], c->stream) != cudaSuccess ||
+          cudaEventSynchronize(ev[1]) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess)
+        status = GCVT_ERR_CUDA;
+      acc2 += ms;
+    }
+  }
   for (int i = 0; i < 3; ++i) cudaEventDestroy(ev[i]);
   if (status) return status;
   ms3[0] = acc[0] / iterations;
   ms3[1] = acc[1] / iterations;
-  ms3[2] = 0.f;
+  ms3[2] = acc2 / iterations;
   return GCVT_OK;
 }
 

@@ -111,6 +111,11 @@ cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigne
                               cudaStream_t s);
 cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
                                unsigned *ticket, cudaStream_t s);
+cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
+                       cudaStream_t s);
+cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,
+                               unsigned long long *counts, cudaStream_t s);
+cudaError_t jfa_configure();
 cudaError_t cells_configure();
 size_t list_blocks(int n);
 size_t cell_groups(int n);

@@ -1,0 +1,261 @@
+// jfa.cu -- jump-flooding Voronoi labelling: an approximate labeller beside
+// the exact one (labeller.cu), with its error measured against it.
+//
+// The label grid holds one int32 per pixel (x in the low, y in the high 16
+// bits, MARKER for none), the same words as the reference's short2 grids.
+// A step of offset k gives pixel p the nearest of the nine labels at
+// p + (dx, dy) k, dx, dy in {-1, 0, 1} (ties: smaller x, then smaller y).
+// The schedule is k = n/2, n/4, ..., 1 and one more step of 1 (for a side
+// that is not a power of two, from the largest power of two <= n/2).
+//
+//   * k >= 16: k_jfa_step, one launch per step, four pixels per thread: the
+//     nine neighbours of a 4-pixel group are three rows of three aligned
+//     16-byte words (k is a multiple of 4), so every load and the store is
+//     128-bit and a warp reads 512 contiguous bytes per row.
+//   * k = 8, 4, 2, 1, 1: k_jfa_tail, one launch.  A block loads its 64 x 64
+//     tile with a 16-pixel halo (96 x 96 labels, 36 KB) into shared memory
+//     with one TMA tile copy, runs the five steps there on a region that
+//     shrinks by each step's offset (8 + 4 + 2 + 1 + 1 = 16), ping-ponging
+//     between two shared buffers, and writes the tile back with 128-bit
+//     stores: five passes over the grid for one read and one write.
+#include "gcvt_internal.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+namespace cvtgb {
+
+constexpr int kTile = 64, kHalo = 16, kReg = kTile + 2 * kHalo;  // 96
+constexpr unsigned kTailBytes = 2u * kReg * kReg * 4u + 64u;   // two buffers + mbarrier
+
+__device__ __forceinline__ int lab_x(uint32_t v) { return (int)(int16_t)(v & 0xffffu); }
+__device__ __forceinline__ int lab_y(uint32_t v) { return (int)(int16_t)(v >> 16); }
+
+// Keep the better of best and c for pixel (x, y).
+__device__ __forceinline__ void consider(uint32_t c, int x, int y, uint32_t &best, int &bd) {
+  if (c == kMarkerWord) return;
+  const int cx = lab_x(c), cy = lab_y(c);
+  const int d = (cx - x) * (cx - x) + (cy - y) * (cy - y);
+  if (d < bd || (d == bd && (cx < lab_x(best) || (cx == lab_x(best) && cy < lab_y(best))))) {
+    best = c;
+    bd = d;
+  }
+}
+
+__device__ __forceinline__ uint32_t comp(const uint4 &v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// One step of offset k (a multiple of 4), four pixels per thread.
+__global__ void __launch_bounds__(256) k_jfa_step(const uint32_t *__restrict__ in,
+                                                  uint32_t *__restrict__ out, int n, int k) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (q >= n / 4) return;
+  const int x0 = 4 * q;
+  const uint4 none = make_uint4(kMarkerWord, kMarkerWord, kMarkerWord, kMarkerWord);
+  uint4 c[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int yy = y + (r - 1) * k;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int xx = x0 + (s - 1) * k;
+      c[r][s] = (yy >= 0 && yy < n && xx >= 0 && xx < n)
+                    ? __ldg(reinterpret_cast<const uint4 *>(in + (size_t)yy * n + xx))
+                    : none;
+    }
+  }
+  uint32_t res[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    uint32_t best = kMarkerWord;
+    int bd = 0x7fffffff;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int s = 0; s < 3; ++s) consider(comp(c[r][s], i), x0 + i, y, best, bd);
+    res[i] = best;
+  }
+  *reinterpret_cast<uint4 *>(out + (size_t)y * n + x0) = make_uint4(res[0], res[1], res[2], res[3]);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Steps 8, 4, 2, 1, 1 on one 64 x 64 tile; `tm` maps the input label grid
+// (n x n uint32, box 96 x 96).  err[0] is set if the tile copy does not
+// arrive within the wait limit (the block then writes nothing).
+__global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtensorMap tm,
+                                                  uint32_t *__restrict__ out, int n, int *err) {
+  extern __shared__ __align__(1024) uint32_t smem[];
+  uint32_t *buf0 = smem, *buf1 = smem + kReg * kReg;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * kReg * kReg);
+  const int tx = blockIdx.x * kTile, ty = blockIdx.y * kTile;
+  const int ox = tx - kHalo, oy = ty - kHalo;  // grid position of buf[0][0]
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)),
+                 "r"((unsigned)(kReg * kReg * 4))
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(buf0)),
+        "l"(reinterpret_cast<uint64_t>(&tm)), "r"(ox), "r"(oy), "r"(smem_addr(mbar))
+        : "memory");
+  }
+  // wait for the tile, a bounded number of times
+  unsigned done = 0;
+  for (int it = 0; it < (1 << 22) && !done; ++it)
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_addr(mbar)), "r"(0u)
+        : "memory");
+  if (!__syncthreads_and((int)done)) {
+    if (tid == 0) atomicOr(err, 1);
+    return;
+  }
+  // the copy fills positions outside the grid with zeros: no label there
+  for (int p = tid; p < kReg * kReg; p += blockDim.x) {
+    const int gx = ox + p % kReg, gy = oy + p / kReg;
+    if (gx < 0 || gy < 0 || gx >= n || gy >= n) buf0[p] = kMarkerWord;
+  }
+  __syncthreads();
+  uint32_t *cur = buf0, *nxt = buf1;
+  int h = 0;  // rows / columns of the region already out of date
+  const int ks[5] = {8, 4, 2, 1, 1};
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const int k = ks[s];
+    h += k;
+    const int w = kReg - 2 * h;
+    for (int p = tid; p < w * w; p += blockDim.x) {
+      const int i = h + p / w, j = h + p % w;  // buffer row, column
+      const int gx = ox + j, gy = oy + i;
+      uint32_t best = kMarkerWord;
+      if (gx >= 0 && gy >= 0 && gx < n && gy < n) {
+        int bd = 0x7fffffff;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx)
+            consider(cur[(i + dy * k) * kReg + j + dx * k], gx, gy, best, bd);
+      }
+      nxt[i * kReg + j] = best;
+    }
+    __syncthreads();
+    uint32_t *t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  // the tile: buffer rows / columns [16, 80), 16-byte stores
+  for (int p = tid; p < kTile * kTile / 4; p += blockDim.x) {
+    const int i = p / (kTile / 4), j = 4 * (p % (kTile / 4));
+    const uint32_t *src = cur + (kHalo + i) * kReg + kHalo + j;
+    if (ty + i < n && tx + j < n)
+      *reinterpret_cast<uint4 *>(out + (size_t)(ty + i) * n + tx + j) =
+          *reinterpret_cast<const uint4 *>(src);
+  }
+}
+
+// Pixels whose label differs from the exact one, and pixels whose label is
+// strictly farther than the exact one's (the jump-flooding error proper).
+__global__ void __launch_bounds__(256) k_jfa_compare(const uint32_t *__restrict__ jfa,
+                                                     const uint32_t *__restrict__ exact, int n,
+                                                     unsigned long long *counts) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned diff = 0, far = 0;
+  if (p < (size_t)n * n) {
+    const uint32_t a = jfa[p], b = exact[p];
+    if (a != b) {
+      diff = 1;
+      const int x = (int)(p % n), y = (int)(p / n);
+      const int da = a == kMarkerWord ? 0x7fffffff
+                                      : (lab_x(a) - x) * (lab_x(a) - x) + (lab_y(a) - y) * (lab_y(a) - y);
+      const int db = (lab_x(b) - x) * (lab_x(b) - x) + (lab_y(b) - y) * (lab_y(b) - y);
+      far = da > db;
+    }
+  }
+  diff = __reduce_add_sync(0xffffffffu, diff);
+  far = __reduce_add_sync(0xffffffffu, far);
+  if ((threadIdx.x & 31) == 0 && diff) {
+    atomicAdd(counts, (unsigned long long)diff);
+    if (far) atomicAdd(counts + 1, (unsigned long long)far);
+  }
+}
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+bool g_tail_configured[64] = {};
+}  // namespace
+
+cudaError_t jfa_configure() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!g_encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (!g_tail_configured[dev]) {
+    e = cudaFuncSetAttribute(k_jfa_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTailBytes);
+    if (e != cudaSuccess) return e;
+    g_tail_configured[dev] = true;
+  }
+  return cudaSuccess;
+}
+
+// Jump flooding of the label grid `a` (seeded: every site labels itself,
+// MARKER elsewhere) for a grid of side n (a multiple of 64 >= 128); `b` is
+// the ping-pong partner.  Returns the buffer holding the result in *result.
+cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
+                       cudaStream_t s) {
+  cudaError_t e = jfa_configure();
+  if (e != cudaSuccess) return e;
+  uint32_t *in = a, *out = b;
+  int k = 1;
+  while (2 * k <= n / 2) k *= 2;  // the largest power of two <= n/2
+  for (; k >= 16; k /= 2) {
+    const dim3 grid((unsigned)((n / 4 + 255) / 256), (unsigned)n);
+    k_jfa_step<<<grid, 256, 0, s>>>(in, out, n, k);
+    uint32_t *t = in;
+    in = out;
+    out = t;
+  }
+  CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)n * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)kReg, (cuuint32_t)kReg};
+  const cuuint32_t estr[2] = {1, 1};
+  if (g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, in, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const dim3 grid((unsigned)(n / kTile), (unsigned)(n / kTile));
+  k_jfa_tail<<<grid, 256, kTailBytes, s>>>(tm, out, n, err);
+  *result = out;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,
+                               unsigned long long *counts, cudaStream_t s) {
+  const size_t nn = (size_t)n * n;
+  k_jfa_compare<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(jfa, exact, n, counts);
+  return cudaGetLastError();
+}
+
+}  // namespace cvtgb

@@ -67,6 +67,7 @@ SIGNATURES = {
     "gcvt_ctx_extract_points": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I,
                                  ctypes.POINTER(I), I], I),
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
+    "gcvt_ctx_jfa_label": ([P, P, P, I], I),
     "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
     "gcvt_batch_destroy": ([P], I),
     "gcvt_batch_set_stream": ([P, P], I),
@@ -195,8 +196,9 @@ class Context:
         return out
 
     def time_kernels(self, iterations):
-        """Mean device ms of (one Lloyd iteration, one labelling pass, 0) over
-        `iterations` iterations; the sites move as in iterate()."""
+        """Mean device ms of (one Lloyd iteration, one exact labelling pass,
+        one jump-flooding labelling) over `iterations` repetitions; the sites
+        move as in iterate()."""
         ms = (ctypes.c_float * 3)()
         _check(self.lib.gcvt_ctx_time_kernels(self.h, int(iterations), ms), "gcvt_ctx_time_kernels")
         return list(ms)
@@ -215,6 +217,15 @@ class Context:
                                                 out.ctypes.data, int(capacity), ctypes.byref(cnt),
                                                 MEM_HOST), "gcvt_ctx_extract_points")
         return out[:min(cnt.value, capacity)]
+
+    def jfa_label(self, labels=True):
+        """(labels or None, (differing, farther, pixels)) of jump flooding."""
+        n = self.n
+        out = np.empty((n, n, 2), np.int16) if labels else None
+        st = (ctypes.c_ulonglong * 3)()
+        _check(self.lib.gcvt_ctx_jfa_label(self.h, None if out is None else out.ctypes.data, st,
+                                           MEM_HOST), "gcvt_ctx_jfa_label")
+        return out, tuple(int(v) for v in st)
 
     def info(self):
         info = RunInfo()
