@@ -286,6 +286,10 @@ def run_ours(args):
         return total / 1e3
 
     with torch.cuda.stream(stream):
+        # launch choices for this workload (results do not depend on them)
+        ctx.load(d_sites, d_rho, d_mask)
+        ctx.iterate(3)
+        tuning = ctx.autotune()
         for _ in range(args.warmup):
             step_device()
         with ClockSampler(local) as clk:
@@ -325,6 +329,7 @@ def run_ours(args):
         "iter_per_s": ITERS * args.steps * ws / t_dev,
         "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1], "jfa_labelling": kms[2]},
         "jfa": jfa_line(n, kms[2], jfa_stats, peak),
+        "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
                      "peak_source": peak_kind,

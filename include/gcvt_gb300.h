@@ -50,6 +50,16 @@ typedef struct {
     double sampled_energy; /* energy sampled by the schedule (iter % 10 == 0) */
 } gcvt_run_info;
 
+/* Launch choices of a context (gcvt_ctx_autotune, gcvt_ctx_set_tuning).
+ * None changes any result: they only change how fast it is reached. */
+typedef struct {
+    int cell_blocks_per_sm; /* persistent Lloyd grid: blocks (warps) per SM, 0 = all that fit */
+    int hint_slack;         /* a site's next window: 2 R + hint_slack pixels              */
+    int jfa_tail_halo;      /* jump flooding: steps <= halo/2 fused in one launch (8/16/32) */
+    float lloyd_ms;         /* autotune: best time of one Lloyd iteration (ms)           */
+    float jfa_ms;           /* autotune: best time of one jump-flooding labelling (ms)   */
+} gcvt_tuning;
+
 /* Human-readable text of a status code. */
 const char *gcvt_status_string(int status);
 
@@ -125,6 +135,17 @@ int gcvt_ctx_time_kernels(gcvt_ctx *ctx, int iterations, float *ms3);
  * the exact labels of gcvt_ctx_label: [0] pixels whose label differs,
  * [1] pixels whose label is strictly farther than the exact one's, [2] n*n. */
 int gcvt_ctx_jfa_label(gcvt_ctx *ctx, int16_t *labels, unsigned long long *stats, int mem);
+
+/* Autotuner (no reference counterpart; the reference's fixed band tables,
+ * gcvt.cu:842-847, are its closest analogue): times the Lloyd iteration for
+ * persistent grids of 16, 24 and 32 blocks per SM and hint slacks 1, 2, 3,
+ * and the jump-flooding labelling for fusion depths 8, 16 and 32, on the
+ * loaded problem, restores every state it touched, and keeps the fastest
+ * choices (written to *out if not NULL). */
+int gcvt_ctx_autotune(gcvt_ctx *ctx, gcvt_tuning *out);
+
+/* Set the launch choices directly. */
+int gcvt_ctx_set_tuning(gcvt_ctx *ctx, const gcvt_tuning *tuning);
 
 /* Schedule state (iterations, omega, energies). */
 int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);

@@ -49,6 +49,11 @@ struct gcvt_ctx {
   unsigned *scnt = nullptr;
   unsigned *colcnt = nullptr;   // point extraction: n_max column counts + total
   uint32_t *jfa = nullptr;      // jump flooding: two n_max^2 label grids + counters
+  // tuning (gcvt_ctx_autotune): persistent Lloyd grid in blocks (0: all that
+  // fit), window hint slack, jump-flooding fusion depth (tail halo)
+  int cell_grid = 0;
+  int hint_slack = 2;
+  int jfa_halo = 16;
   int cover_valid = 0;          // the covering bound, list counts and hints
                                 // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
@@ -119,14 +124,14 @@ int enqueue_chunk(gcvt_ctx *c, int n, int level) {
       cudaGetLastError();
       for (int i = 0; i < kChunk; ++i) {
         CK(launch_list(b, 1, c->stream));
-        CK(launch_cells(b, 0, nullptr, c->stream));
+        CK(launch_cells(b, 0, nullptr, c->stream, c->cell_grid));
       }
       return GCVT_OK;
     }
     cudaError_t le = cudaSuccess;
     for (int i = 0; i < kChunk && le == cudaSuccess; ++i) {
       le = launch_list(b, 1, c->stream);
-      if (le == cudaSuccess) le = launch_cells(b, 0, nullptr, c->stream);
+      if (le == cudaSuccess) le = launch_cells(b, 0, nullptr, c->stream, c->cell_grid);
     }
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
@@ -216,6 +221,7 @@ int start_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter) {
   h.window = window;
   h.energy_scale = std::pow(4.0, level) / ((double)n * (double)n);
   h.done_blocks = 0;
+  h.hint_slack = c->hint_slack;
   if ((rc = push_state(c))) return rc;
   c->cur_n = n;
   return ensure_cover(c, n, level);
@@ -537,7 +543,7 @@ int gcvt_ctx_moments(gcvt_ctx *c, double *out4, int mem) {
   CK(cudaMemsetAsync(c->moments, 0, (size_t)4 * n * n * sizeof(double), c->stream));
   const LevelBufs b = level_bufs(c, n, level);
   CK(launch_list(b, 0, c->stream));
-  CK(launch_cells(b, 1, c->moments, c->stream));
+  CK(launch_cells(b, 1, c->moments, c->stream, c->cell_grid));
   return copy_out(out4, c->moments, (size_t)4 * n * n * sizeof(double), mem, c->stream);
 }
 
@@ -590,7 +596,7 @@ int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, 
   CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
   CK(launch_bits_to_grid(c->bits[c->st_host->cur], n, a, c->stream));
   uint32_t *res = nullptr;
-  CK(launch_jfa(a, b, n, c->err, &res, c->stream));
+  CK(launch_jfa(a, b, n, c->err, &res, c->stream, c->jfa_halo));
   if (stats) {
     const LevelBufs lb = level_bufs(c, n, level_of(c, n));
     CK(launch_summary(lb, 0, c->stream));
@@ -610,6 +616,141 @@ int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, 
   if (herr) return GCVT_ERR_CUDA;  // a tile copy did not arrive
   if (labels) return copy_out(labels, res, (size_t)n * n * sizeof(uint32_t), mem, c->stream);
   return GCVT_OK;
+}
+
+int gcvt_ctx_set_tuning(gcvt_ctx *c, const gcvt_tuning *t) {
+  if (!c || !t) return GCVT_ERR_ARGUMENT;
+  if (t->cell_blocks_per_sm < 0 || t->cell_blocks_per_sm > 32 || t->hint_slack < 0 ||
+      t->hint_slack > 64 || (t->jfa_tail_halo != 8 && t->jfa_tail_halo != 16 &&
+                             t->jfa_tail_halo != 32))
+    return GCVT_ERR_ARGUMENT;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+    return GCVT_ERR_CUDA;
+  const int grid = t->cell_blocks_per_sm * sms;
+  if (grid != c->cell_grid && c->chunk_exec) {  // the captured grid changes
+    cudaGraphExecDestroy(c->chunk_exec);
+    c->chunk_exec = nullptr;
+  }
+  c->cell_grid = grid;
+  c->hint_slack = t->hint_slack;
+  c->jfa_halo = t->jfa_tail_halo;
+  return GCVT_OK;
+}
+
+int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
+  if (!c) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  if (c->cur_n != c->n) return GCVT_ERR_STATE;
+  const int n = c->n;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  // save what iterations change
+  const size_t wbytes = bits_words(n) * sizeof(uint64_t), cbytes = list_blocks(n) * sizeof(unsigned);
+  const size_t hbytes = (size_t)n * n;
+  const size_t total = 3 * wbytes + 3 * cbytes + hbytes + sizeof(DevState);
+  unsigned char *save = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&save), total) != cudaSuccess) return GCVT_ERR_ALLOC;
+  DevState saved_host = *c->st_host;
+  const int saved_valid = c->cover_valid;
+  auto copy_state = [&](bool to_save) -> int {
+    size_t off = 0;
+    auto mv = [&](void *p, size_t bytes) {
+      const cudaError_t e = cudaMemcpyAsync(to_save ? save + off : p, to_save ? p : save + off,
+                                            bytes, cudaMemcpyDeviceToDevice, c->stream);
+      off += bytes;
+      return e == cudaSuccess;
+    };
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) ok = ok && mv(c->bits[k], wbytes);
+    for (int k = 0; k < 3; ++k) ok = ok && mv(c->counts[k], cbytes);
+    ok = ok && mv(c->hint, hbytes);
+    ok = ok && mv(c->st, sizeof(DevState));
+    return ok ? GCVT_OK : GCVT_ERR_CUDA;
+  };
+  int sms = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  gcvt_tuning best = {0, c->hint_slack, c->jfa_halo, 1e30f, 1e30f};
+  const int per_sm[3] = {16, 24, 32}, slack[3] = {1, 2, 3};
+  const int keep_grid = c->cell_grid, keep_slack = c->hint_slack;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  // the covering bound and counts of the current sites, then the snapshot
+  if (!rc) rc = start_level(c, n, 0, 0x7fffffff, 0x7fffffff);
+  if (!rc) rc = pull_state(c);
+  if (!rc) rc = copy_state(true);
+  // Lloyd kernel: grid x hint slack, iterations 2-4 after the same start
+  for (int gi = 0; gi < 3 && !rc; ++gi)
+    for (int si = 0; si < 3 && !rc; ++si) {
+      if ((rc = copy_state(false))) break;
+      c->st_host->hint_slack = slack[si];
+      if ((rc = push_state(c))) break;
+      const LevelBufs lb = level_bufs(c, n, 0);
+      const int grid = per_sm[gi] * sms;
+      float ms = 0.f;
+      for (int it = 0; it < 4 && !rc; ++it) {
+        if (it == 1 && cudaEventRecord(e0, c->stream) != cudaSuccess) rc = GCVT_ERR_CUDA;
+        if (launch_list(lb, 1, c->stream) != cudaSuccess ||
+            launch_cells(lb, 0, nullptr, c->stream, grid) != cudaSuccess)
+          rc = GCVT_ERR_CUDA;
+      }
+      if (!rc && (cudaEventRecord(e1, c->stream) != cudaSuccess ||
+                  cudaEventSynchronize(e1) != cudaSuccess ||
+                  cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = GCVT_ERR_CUDA;
+      if (!rc && ms / 3 < best.lloyd_ms) {
+        best.lloyd_ms = ms / 3;
+        best.cell_blocks_per_sm = per_sm[gi];
+        best.hint_slack = slack[si];
+      }
+    }
+  // jump flooding: fusion depth
+  if (!rc && !c->jfa &&
+      cudaMalloc(reinterpret_cast<void **>(&c->jfa),
+                 2 * (size_t)c->n_max * c->n_max * sizeof(uint32_t) + 64) != cudaSuccess)
+    rc = GCVT_ERR_ALLOC;
+  if (!rc) rc = copy_state(false);
+  const int halos[3] = {8, 16, 32};
+  for (int hi = 0; hi < 3 && !rc; ++hi) {
+    uint32_t *ja = c->jfa, *jb = c->jfa + (size_t)c->n_max * c->n_max, *res = nullptr;
+    float ms = 0.f;
+    for (int it = 0; it < 3 && !rc; ++it) {
+      float one = 0.f;
+      if (launch_bits_to_grid(c->bits[saved_host.cur], n, ja, c->stream) != cudaSuccess ||
+          cudaEventRecord(e0, c->stream) != cudaSuccess ||
+          launch_jfa(ja, jb, n, c->err, &res, c->stream, halos[hi]) != cudaSuccess ||
+          cudaEventRecord(e1, c->stream) != cudaSuccess ||
+          cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&one, e0, e1) != cudaSuccess)
+        rc = GCVT_ERR_CUDA;
+      if (it) ms += one;  // the first run warms up
+    }
+    if (!rc && ms / 2 < best.jfa_ms) {
+      best.jfa_ms = ms / 2;
+      best.jfa_tail_halo = halos[hi];
+    }
+  }
+  // back to the state before the search
+  if (!rc) rc = copy_state(false);
+  if (!rc) {
+    *c->st_host = saved_host;
+    rc = push_state(c);
+  }
+  if (!rc) CK(cudaStreamSynchronize(c->stream));
+  c->cover_valid = saved_valid;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(save);
+  if (rc) {
+    c->cell_grid = keep_grid;
+    c->hint_slack = keep_slack;
+    return rc;
+  }
+  rc = gcvt_ctx_set_tuning(c, &best);
+  if (!rc && out) *out = best;
+  return rc;
 }
 
 int gcvt_ctx_info(gcvt_ctx *c, gcvt_run_info *info) {
@@ -645,6 +786,7 @@ int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
   h.use_stop_rule = 0;
   h.fixed_iters = 0x7fffffff;
   h.window = window;
+  h.hint_slack = c->hint_slack;
   h.energy_scale = 1.0 / ((double)c->n * (double)c->n);
   if ((rc = push_state(c))) return rc;
   if ((rc = ensure_cover(c, c->n, 0))) return rc;
@@ -661,7 +803,7 @@ int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
     float ms0 = 0.f, ms1 = 0.f;
     if (cudaEventRecord(ev[0], c->stream) != cudaSuccess ||
         launch_list(b, 1, c->stream) != cudaSuccess ||
-        launch_cells(b, 0, nullptr, c->stream) != cudaSuccess ||
+        launch_cells(b, 0, nullptr, c->stream, c->cell_grid) != cudaSuccess ||
         cudaEventRecord(ev[1], c->stream) != cudaSuccess ||
         launch_summary(b, 0, c->stream) != cudaSuccess ||
         launch_rows(b, 0, c->stream) != cudaSuccess ||
@@ -686,7 +828,7 @@ int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
       float ms = 0.f;
       if (launch_bits_to_grid(c->bits[c->st_host->cur], c->n, ja, c->stream) != cudaSuccess ||
           cudaEventRecord(ev[0], c->stream) != cudaSuccess ||
-          launch_jfa(ja, jb, c->n, c->err, &res, c->stream) != cudaSuccess ||
+          launch_jfa(ja, jb, c->n, c->err, &res, c->stream, c->jfa_halo) != cudaSuccess ||
           cudaEventRecord(ev[1], c->stream) != cudaSuccess ||
           cudaEventSynchronize(ev[1]) != cudaSuccess ||
           cudaEventElapsedTime(&ms, ev[0], ev[1]) != cudaSuccess)

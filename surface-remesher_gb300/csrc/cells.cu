@@ -410,7 +410,7 @@ struct IterView {
   uint64_t *nxt;         // where the moved sites go
   unsigned *cnt_nxt;     // their per-list-block counts
   float omega;
-  int W0, rb, nsites, cur;
+  int W0, rb, nsites, cur, slack;
   unsigned ngroups;      // 32-site groups of the list
 };
 
@@ -425,6 +425,7 @@ __device__ __forceinline__ IterView iter_view(const LevelBufs &a) {
   v.W0 = st->snap_window;
   v.rb = st->snap_cover;
   v.nsites = st->snap_count;
+  v.slack = st->hint_slack;
   v.ngroups = (unsigned)(v.nsites + 31) / 32;
   return v;
 }
@@ -491,7 +492,7 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
       const unsigned long long old =
           atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
       if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
-      a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + 2, 255);
+      a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
     }
   }
   __syncwarp();
@@ -861,12 +862,20 @@ cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsign
   return cudaGetLastError();
 }
 
-cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s) {
+int cells_default_grid() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  return g_cell_grid[dev];
+}
+
+// grid: the persistent grid in blocks (0: every block that fits).
+cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s,
+                         int grid) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
-  const int grid = g_cell_grid[dev];
+  if (grid <= 0 || grid > g_cell_grid[dev]) grid = g_cell_grid[dev];
   if (moments_only) k_cell<1><<<grid, 32, 0, s>>>(b, out4);
   else k_cell<0><<<grid, 32, 0, s>>>(b, out4);
   return cudaGetLastError();

@@ -56,6 +56,7 @@ struct DevState {
   // the next iteration while other warps of the same launch may still start.
   int snap_cur, snap_stopped, snap_window, snap_cover, snap_count;
   float snap_omega;
+  int hint_slack;      // window hint left for a site: 2 R + hint_slack (tuned)
 };
 
 // Buffers of one resolution level, passed by value to every kernel.
@@ -95,7 +96,9 @@ cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, 
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_list(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_count(const LevelBufs &b, cudaStream_t s);
-cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s);
+cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s,
+                         int grid = 0);
+int cells_default_grid();
 cudaError_t launch_zoom(const uint64_t *src, int n, uint64_t *dst, cudaStream_t s);
 cudaError_t launch_density_halve(const float *in, float *out, int n_out, cudaStream_t s);
 cudaError_t launch_row_support(const float *density, int n, int2 *sup, int2 *range,
@@ -112,7 +115,7 @@ cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigne
 cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
                                unsigned *ticket, cudaStream_t s);
 cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
-                       cudaStream_t s);
+                       cudaStream_t s, int tail_halo = 16);
 cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,
                                unsigned long long *counts, cudaStream_t s);
 cudaError_t jfa_configure();

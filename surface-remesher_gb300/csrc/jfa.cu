@@ -8,16 +8,17 @@
 // The schedule is k = n/2, n/4, ..., 1 and one more step of 1 (for a side
 // that is not a power of two, from the largest power of two <= n/2).
 //
-//   * k >= 16: k_jfa_step, one launch per step, four pixels per thread: the
+//   * k > H/2: k_jfa_step, one launch per step, four pixels per thread: the
 //     nine neighbours of a 4-pixel group are three rows of three aligned
 //     16-byte words (k is a multiple of 4), so every load and the store is
 //     128-bit and a warp reads 512 contiguous bytes per row.
-//   * k = 8, 4, 2, 1, 1: k_jfa_tail, one launch.  A block loads its 64 x 64
-//     tile with a 16-pixel halo (96 x 96 labels, 36 KB) into shared memory
-//     with one TMA tile copy, runs the five steps there on a region that
-//     shrinks by each step's offset (8 + 4 + 2 + 1 + 1 = 16), ping-ponging
-//     between two shared buffers, and writes the tile back with 128-bit
-//     stores: five passes over the grid for one read and one write.
+//   * k = H/2, ..., 1, 1: k_jfa_tail<H>, one launch (H = 8, 16 or 32, the
+//     fusion depth; 16 by default, the autotuner picks).  A block loads its
+//     64 x 64 tile with an H-pixel halo (96 x 96 labels, 36 KB, for H = 16)
+//     into shared memory with one TMA tile copy, runs the steps there on a
+//     region that shrinks by each step's offset (8 + 4 + 2 + 1 + 1 = 16),
+//     ping-ponging between two shared buffers, and writes the tile back with
+//     128-bit stores: five passes over the grid for one read and one write.
 #include "gcvt_internal.cuh"
 
 #include <cuda.h>
@@ -25,8 +26,13 @@
 
 namespace cvtgb {
 
-constexpr int kTile = 64, kHalo = 16, kReg = kTile + 2 * kHalo;  // 96
-constexpr unsigned kTailBytes = 2u * kReg * kReg * 4u + 64u;   // two buffers + mbarrier
+constexpr int kTile = 64;
+// Tail of halo H: steps H/2, H/4, ..., 1 and the extra 1 (they sum to H) on
+// a (64 + 2H)^2 region; H = 8, 16 or 32 (the fusion depth the autotuner picks).
+template <int H> constexpr int tail_reg() { return kTile + 2 * H; }
+template <int H> constexpr unsigned tail_bytes() {
+  return 2u * tail_reg<H>() * tail_reg<H>() * 4u + 64u;  // two buffers + mbarrier
+}
 
 __device__ __forceinline__ int lab_x(uint32_t v) { return (int)(int16_t)(v & 0xffffu); }
 __device__ __forceinline__ int lab_y(uint32_t v) { return (int)(int16_t)(v >> 16); }
@@ -84,11 +90,13 @@ __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Steps 8, 4, 2, 1, 1 on one 64 x 64 tile; `tm` maps the input label grid
-// (n x n uint32, box 96 x 96).  err[0] is set if the tile copy does not
+// Steps H/2 .. 1, 1 on one 64 x 64 tile; `tm` maps the input label grid
+// (n x n uint32, box (64 + 2H)^2).  err[0] is set if the tile copy does not
 // arrive within the wait limit (the block then writes nothing).
+template <int H>
 __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtensorMap tm,
                                                   uint32_t *__restrict__ out, int n, int *err) {
+  constexpr int kHalo = H, kReg = tail_reg<H>();
   extern __shared__ __align__(1024) uint32_t smem[];
   uint32_t *buf0 = smem, *buf1 = smem + kReg * kReg;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + 2 * kReg * kReg);
@@ -130,10 +138,9 @@ __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtens
   __syncthreads();
   uint32_t *cur = buf0, *nxt = buf1;
   int h = 0;  // rows / columns of the region already out of date
-  const int ks[5] = {8, 4, 2, 1, 1};
 #pragma unroll
-  for (int s = 0; s < 5; ++s) {
-    const int k = ks[s];
+  for (int k2 = H; k2 >= 1; k2 >>= 1) {  // k = H/2, ..., 1, then 1 again
+    const int k = k2 > 1 ? k2 / 2 : 1;
     h += k;
     const int w = kReg - 2 * h;
     for (int p = tid; p < w * w; p += blockDim.x) {
@@ -194,6 +201,29 @@ __global__ void __launch_bounds__(256) k_jfa_compare(const uint32_t *__restrict_
 namespace {
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 bool g_tail_configured[64] = {};
+
+template <int H>
+cudaError_t tail_attr() {
+  return cudaFuncSetAttribute(k_jfa_tail<H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tail_bytes<H>());
+}
+
+template <int H>
+cudaError_t launch_tail(uint32_t *in, uint32_t *out, int n, int *err, cudaStream_t s) {
+  CUtensorMap tm;
+  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)n * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)tail_reg<H>(), (cuuint32_t)tail_reg<H>()};
+  const cuuint32_t estr[2] = {1, 1};
+  if (g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, in, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const dim3 grid((unsigned)(n / kTile), (unsigned)(n / kTile));
+  k_jfa_tail<H><<<grid, 256, tail_bytes<H>(), s>>>(tm, out, n, err);
+  return cudaGetLastError();
+}
 }  // namespace
 
 cudaError_t jfa_configure() {
@@ -210,9 +240,9 @@ cudaError_t jfa_configure() {
     g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
   if (!g_tail_configured[dev]) {
-    e = cudaFuncSetAttribute(k_jfa_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kTailBytes);
-    if (e != cudaSuccess) return e;
+    if ((e = tail_attr<8>()) != cudaSuccess) return e;
+    if ((e = tail_attr<16>()) != cudaSuccess) return e;
+    if ((e = tail_attr<32>()) != cudaSuccess) return e;
     g_tail_configured[dev] = true;
   }
   return cudaSuccess;
@@ -220,35 +250,30 @@ cudaError_t jfa_configure() {
 
 // Jump flooding of the label grid `a` (seeded: every site labels itself,
 // MARKER elsewhere) for a grid of side n (a multiple of 64 >= 128); `b` is
-// the ping-pong partner.  Returns the buffer holding the result in *result.
+// the ping-pong partner; steps above tail_halo / 2 run one launch each, the
+// rest in one fused tail launch (tail_halo = 8, 16 or 32).  Returns the
+// buffer holding the result in *result.
 cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
-                       cudaStream_t s) {
+                       cudaStream_t s, int tail_halo) {
   cudaError_t e = jfa_configure();
   if (e != cudaSuccess) return e;
+  if (tail_halo != 8 && tail_halo != 32) tail_halo = 16;
+  while (tail_halo > 8 && tail_halo > n / 4) tail_halo /= 2;  // the steps start at <= n/2
   uint32_t *in = a, *out = b;
   int k = 1;
   while (2 * k <= n / 2) k *= 2;  // the largest power of two <= n/2
-  for (; k >= 16; k /= 2) {
+  for (; k > tail_halo / 2; k /= 2) {
     const dim3 grid((unsigned)((n / 4 + 255) / 256), (unsigned)n);
     k_jfa_step<<<grid, 256, 0, s>>>(in, out, n, k);
     uint32_t *t = in;
     in = out;
     out = t;
   }
-  CUtensorMap tm;
-  const cuuint64_t dims[2] = {(cuuint64_t)n, (cuuint64_t)n};
-  const cuuint64_t strides[1] = {(cuuint64_t)n * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)kReg, (cuuint32_t)kReg};
-  const cuuint32_t estr[2] = {1, 1};
-  if (g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, in, dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
-      CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
-  const dim3 grid((unsigned)(n / kTile), (unsigned)(n / kTile));
-  k_jfa_tail<<<grid, 256, kTailBytes, s>>>(tm, out, n, err);
+  if (tail_halo == 8) e = launch_tail<8>(in, out, n, err, s);
+  else if (tail_halo == 32) e = launch_tail<32>(in, out, n, err, s);
+  else e = launch_tail<16>(in, out, n, err, s);
   *result = out;
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,

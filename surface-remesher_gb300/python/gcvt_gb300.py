@@ -35,6 +35,15 @@ class GcvtError(RuntimeError):
         self.code = code
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("cell_blocks_per_sm", ctypes.c_int), ("hint_slack", ctypes.c_int),
+                ("jfa_tail_halo", ctypes.c_int), ("lloyd_ms", ctypes.c_float),
+                ("jfa_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class RunInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("levels", ctypes.c_int),
                 ("omega", ctypes.c_float), ("energy", ctypes.c_double),
@@ -68,6 +77,8 @@ SIGNATURES = {
                                  ctypes.POINTER(I), I], I),
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
     "gcvt_ctx_jfa_label": ([P, P, P, I], I),
+    "gcvt_ctx_autotune": ([P, ctypes.POINTER(Tuning)], I),
+    "gcvt_ctx_set_tuning": ([P, ctypes.POINTER(Tuning)], I),
     "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
     "gcvt_batch_destroy": ([P], I),
     "gcvt_batch_set_stream": ([P, P], I),
@@ -217,6 +228,17 @@ class Context:
                                                 out.ctypes.data, int(capacity), ctypes.byref(cnt),
                                                 MEM_HOST), "gcvt_ctx_extract_points")
         return out[:min(cnt.value, capacity)]
+
+    def autotune(self):
+        """Pick the fastest launch choices for the loaded problem (results
+        unchanged); returns them as a dict."""
+        t = Tuning()
+        _check(self.lib.gcvt_ctx_autotune(self.h, ctypes.byref(t)), "gcvt_ctx_autotune")
+        return t.as_dict()
+
+    def set_tuning(self, cell_blocks_per_sm=0, hint_slack=2, jfa_tail_halo=16):
+        t = Tuning(int(cell_blocks_per_sm), int(hint_slack), int(jfa_tail_halo), 0.0, 0.0)
+        _check(self.lib.gcvt_ctx_set_tuning(self.h, ctypes.byref(t)), "gcvt_ctx_set_tuning")
 
     def jfa_label(self, labels=True):
         """(labels or None, (differing, farther, pixels)) of jump flooding."""

@@ -1,0 +1,56 @@
+"""The autotuner and the launch choices change speed only: a tuned context,
+and one set to each extreme choice by hand, give the same sites, labels and
+energies as an untuned one, bit for bit; the search leaves the state as it
+found it."""
+import numpy as np
+import pytest
+
+from workloads import small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def run(gcvt_lib, sites, rho, mask, iters, tune=None):
+    n = sites.shape[0]
+    ctx = gcvt_lib.Context(n)
+    ctx.load(sites, rho, mask)
+    t = None
+    if tune == "auto":
+        ctx.iterate(3)
+        t = ctx.autotune()
+        ctx.iterate(iters - 3)
+    else:
+        if tune is not None:
+            ctx.set_tuning(**tune)
+        ctx.iterate(iters)
+    out = (ctx.sites(), ctx.label(), ctx.info()["energy"], ctx.jfa_label()[0])
+    ctx.close()
+    return out, t
+
+
+@pytest.mark.parametrize("case", [(512, 3000, 41), (1024, 8000, 42)])
+def test_tuning_changes_nothing(gcvt_lib, cuda_device, case):
+    n, m, seed = case
+    sites, rho, mask = small_case(n, m, seed)
+    base, _ = run(gcvt_lib, sites, rho, mask, 15)
+    tuned, t = run(gcvt_lib, sites, rho, mask, 15, "auto")
+    assert t["cell_blocks_per_sm"] in (16, 24, 32)
+    assert t["hint_slack"] in (1, 2, 3)
+    assert t["jfa_tail_halo"] in (8, 16, 32)
+    assert t["lloyd_ms"] > 0 and t["jfa_ms"] > 0
+    for a, b in zip(base, tuned):
+        assert np.array_equal(a, b)
+    for choice in ({"cell_blocks_per_sm": 16, "hint_slack": 1, "jfa_tail_halo": 8},
+                   {"cell_blocks_per_sm": 32, "hint_slack": 3, "jfa_tail_halo": 32}):
+        other, _ = run(gcvt_lib, sites, rho, mask, 15, choice)
+        for a, b in zip(base, other):
+            assert np.array_equal(a, b)
+
+
+def test_set_tuning_rejects_bad_values(gcvt_lib, cuda_device):
+    ctx = gcvt_lib.Context(256)
+    with pytest.raises(gcvt_lib.GcvtError):
+        ctx.set_tuning(jfa_tail_halo=12)
+    with pytest.raises(gcvt_lib.GcvtError):
+        ctx.set_tuning(cell_blocks_per_sm=40)
+    ctx.close()
