@@ -147,6 +147,48 @@ int gcvt_ctx_autotune(gcvt_ctx *ctx, gcvt_tuning *out);
 /* Set the launch choices directly. */
 int gcvt_ctx_set_tuning(gcvt_ctx *ctx, const gcvt_tuning *tuning);
 
+/* ---- learned steps ------------------------------------------------------
+ * No reference counterpart.  A per-site MLP (10 -> 64 -> 64 -> 2, ReLU,
+ * bfloat16 weights and activations, FP32 accumulation) maps a site's last
+ * four Lloyd moves and the density gradient over the density at the site,
+ * in units of the mean cell radius r, to a predicted displacement (in r) of
+ * the site towards the converged tessellation.  A jump moves every free site
+ * by its prediction and is kept only if the energy of the jumped sites is
+ * lower than before; otherwise the state is restored and the plain Lloyd
+ * iterations go on, so the plain method is both fallback and judge. */
+
+/* Number of MLP parameters: W1[10][64], b1[64], W2[64][64], b2[64], W3[64][2], b3[2]. */
+int gcvt_mlp_param_count(void);
+
+/* Histories (and, with track_ids, per-site ids for training data) on or off;
+ * allocates 16 (+8) bytes per pixel of n_max^2.  Takes effect at the next
+ * level start (load, run, iterate). */
+int gcvt_ctx_learning(gcvt_ctx *ctx, int enable, int track_ids);
+
+/* The MLP parameters (FP32 host array of gcvt_mlp_param_count() floats). */
+int gcvt_ctx_set_mlp(gcvt_ctx *ctx, const float *params, int count);
+
+/* Features of the current sites in list order: 10 floats each (host), and
+ * optionally their ids (track_ids) and pixel positions (x, y).  Writes up to
+ * capacity sites; *count = the number of sites. */
+int gcvt_ctx_features(gcvt_ctx *ctx, float *feat, int *ids, int *xy, int capacity, int *count);
+
+/* `iterations` plain Lloyd iterations with a gated jump after every
+ * `jump_every` of them; *tried / *kept (may be NULL) count the jumps. */
+int gcvt_ctx_iterate_learned(gcvt_ctx *ctx, int iterations, int jump_every, int *tried,
+                             int *kept);
+
+/* The MLP on host feature vectors (count x 10) -> predictions (count x 2). */
+int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out);
+
+/* Train the MLP on the GPU (hand-written forward, backward and Adam kernels):
+ * samples are count x 12 floats (10 features, 2 targets), mean squared error,
+ * `steps` Adam steps of `batch` samples drawn by a hash of (seed, step,
+ * slot).  params: initial FP32 parameters in, trained ones out; loss (may be
+ * NULL) receives the mean loss of every step. */
+int gcvt_mlp_train(const float *samples, long long count, float *params, int steps, int batch,
+                   float lr, unsigned long long seed, float *loss);
+
 /* Schedule state (iterations, omega, energies). */
 int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
 

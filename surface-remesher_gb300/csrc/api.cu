@@ -54,6 +54,13 @@ struct gcvt_ctx {
   int cell_grid = 0;
   int hint_slack = 2;
   int jfa_halo = 16;
+  // learned steps (gcvt_ctx_learning): histories, ids, features, predictions,
+  // bfloat16-rounded MLP parameters
+  int learning = 0, track_ids = 0, have_mlp = 0;
+  uint64_t *hist[2] = {};
+  int *ids[2] = {};
+  float *feat = nullptr, *pred = nullptr, *mlp_bf = nullptr;
+  size_t feat_cap = 0;
   int cover_valid = 0;          // the covering bound, list counts and hints
                                 // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
@@ -96,6 +103,15 @@ LevelBufs level_bufs(gcvt_ctx *c, int n, int level) {
   b.gslot = c->gslot;
   b.sslot = c->sslot;
   b.scnt = c->scnt;
+  if (c->learning && level == 0) {
+    b.hist[0] = c->hist[0];
+    b.hist[1] = c->hist[1];
+    if (c->track_ids) {
+      b.ids[0] = c->ids[0];
+      b.ids[1] = c->ids[1];
+    }
+    b.feat = c->feat;
+  }
   return b;
 }
 
@@ -184,6 +200,14 @@ int ensure_cover(gcvt_ctx *c, int n, int level) {
   const size_t nlb = list_blocks(n);
   CK(cudaMemsetAsync(c->counts[(c->st_host->cur + 1) % 3], 0, nlb * sizeof(unsigned), c->stream));
   CK(cudaMemsetAsync(c->hint, 0, (size_t)n * n, c->stream));
+  if (c->learning && level == 0) {  // no moves yet; ids = list positions
+    CK(cudaMemsetAsync(c->hist[c->st_host->hist_cur], 0, (size_t)n * n * sizeof(uint64_t),
+                       c->stream));
+    if (c->track_ids) {
+      CK(launch_list(b, 0, c->stream));
+      CK(launch_ids_init(b, 4 * 152, c->stream));
+    }
+  }
   c->cover_valid = 1;
   return GCVT_OK;
 }
@@ -191,7 +215,7 @@ int ensure_cover(gcvt_ctx *c, int n, int level) {
 // Initial half-size of the candidate window at a level: 2.5 mean cell radii
 // (mean cell area = density pixels / sites).  Only a starting guess: a cell
 // whose certificate fails grows its own window.
-int initial_window(gcvt_ctx *c, int level, int *w) {
+int initial_window(gcvt_ctx *c, int level, int *w, float *radius = nullptr) {
   unsigned long long pix = 0;
   CK(cudaMemcpyAsync(&pix, c->sup_pixels + level, sizeof(pix), cudaMemcpyDeviceToHost,
                      c->stream));
@@ -199,6 +223,10 @@ int initial_window(gcvt_ctx *c, int level, int *w) {
   const double per_site = c->sites > 0 ? (double)pix / c->sites : 64.0;
   const int v = (int)std::ceil(2.5 * std::sqrt(per_site / 3.14159265358979));
   *w = v < 2 ? 2 : (v > 1024 ? 1024 : v);
+  if (radius) {  // mean cell radius
+    const double r = std::sqrt(per_site / 3.14159265358979);
+    *radius = (float)(r > 0.5 ? r : 0.5);
+  }
   return GCVT_OK;
 }
 
@@ -208,7 +236,8 @@ int initial_window(gcvt_ctx *c, int level, int *w) {
 // iterations without the stop rule), covering bound, list counts, hints.
 int start_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter) {
   int window = 0;
-  int rc = initial_window(c, level, &window);
+  float radius = 1.f;
+  int rc = initial_window(c, level, &window, &radius);
   if (rc) return rc;
   if ((rc = pull_state(c))) return rc;
   DevState &h = *c->st_host;
@@ -222,6 +251,7 @@ int start_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter) {
   h.energy_scale = std::pow(4.0, level) / ((double)n * (double)n);
   h.done_blocks = 0;
   h.hint_slack = c->hint_slack;
+  h.feat_scale = radius;
   if ((rc = push_state(c))) return rc;
   c->cur_n = n;
   return ensure_cover(c, n, level);
@@ -422,6 +452,13 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->scnt);
   cudaFree(c->colcnt);
   cudaFree(c->jfa);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(c->hist[k]);
+    cudaFree(c->ids[k]);
+  }
+  cudaFree(c->feat);
+  cudaFree(c->pred);
+  cudaFree(c->mlp_bf);
   cudaFree(c->moments);
   cudaFree(c->err);
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -750,6 +787,229 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   }
   rc = gcvt_ctx_set_tuning(c, &best);
   if (!rc && out) *out = best;
+  return rc;
+}
+
+int gcvt_mlp_param_count(void) { return mlp_param_count(); }
+
+int gcvt_ctx_learning(gcvt_ctx *c, int enable, int track_ids) {
+  if (!c) return GCVT_ERR_ARGUMENT;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return GCVT_ERR_CUDA;
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(c->hist[k]);
+    cudaFree(c->ids[k]);
+    c->hist[k] = nullptr;
+    c->ids[k] = nullptr;
+  }
+  c->learning = c->track_ids = 0;
+  if (c->chunk_exec) {  // captured launches hold the old buffer pointers
+    cudaGraphExecDestroy(c->chunk_exec);
+    c->chunk_exec = nullptr;
+  }
+  c->cover_valid = 0;  // the next level start sets histories (and ids) up
+  if (!enable) return GCVT_OK;
+  const size_t nn = (size_t)c->n_max * c->n_max;
+  bool ok = true;
+  for (int k = 0; k < 2 && ok; ++k)
+    ok = cudaMalloc(reinterpret_cast<void **>(&c->hist[k]), nn * sizeof(uint64_t)) == cudaSuccess;
+  for (int k = 0; k < 2 && ok && track_ids; ++k)
+    ok = cudaMalloc(reinterpret_cast<void **>(&c->ids[k]), nn * sizeof(int)) == cudaSuccess;
+  if (ok && !c->mlp_bf)
+    ok = cudaMalloc(reinterpret_cast<void **>(&c->mlp_bf), mlp_param_count() * sizeof(float)) ==
+         cudaSuccess;
+  if (!ok) {
+    gcvt_ctx_learning(c, 0, 0);
+    return GCVT_ERR_ALLOC;
+  }
+  c->learning = 1;
+  c->track_ids = track_ids ? 1 : 0;
+  return GCVT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Feature and prediction buffers for the current site count.
+int ensure_feat(gcvt_ctx *c) {
+  const size_t need = (size_t)(c->sites > 0 ? c->sites : 1);
+  if (c->feat_cap >= need) return GCVT_OK;
+  cudaFree(c->feat);
+  cudaFree(c->pred);
+  c->feat = c->pred = nullptr;
+  c->feat_cap = 0;
+  if (c->chunk_exec) {
+    cudaGraphExecDestroy(c->chunk_exec);
+    c->chunk_exec = nullptr;
+  }
+  if (cudaMalloc(reinterpret_cast<void **>(&c->feat), need * 10 * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&c->pred), need * 2 * sizeof(float)) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  c->feat_cap = need;
+  return GCVT_OK;
+}
+
+// One gated jump from the current sites (after a plain iteration or a level
+// start): features pass, MLP, jumped sites, energy pass, keep or undo.
+int enqueue_jump(gcvt_ctx *c) {
+  const int n = c->n;
+  const LevelBufs b = level_bufs(c, n, 0);
+  const int grid = 4 * 152;
+  CK(launch_list(b, 0, c->stream));
+  CK(launch_cells(b, 2, nullptr, c->stream, c->cell_grid));
+  CK(launch_mlp_infer(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, grid, c->stream));
+  CK(launch_apply(b, c->pred, grid, c->stream));
+  CK(launch_gate_switch(c->st, n, c->stream));
+  CK(launch_list(b, 0, c->stream));
+  CK(launch_cells(b, 3, nullptr, c->stream, c->cell_grid));
+  CK(launch_gate_resolve(b, grid, c->stream));
+  return GCVT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gcvt_ctx_set_mlp(gcvt_ctx *c, const float *params, int count) {
+  if (!c || !params || count != mlp_param_count()) return GCVT_ERR_ARGUMENT;
+  if (!c->learning) return GCVT_ERR_STATE;
+  float *tmp = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&tmp), count * sizeof(float)) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  int rc = GCVT_OK;
+  if (cudaMemcpyAsync(tmp, params, count * sizeof(float), cudaMemcpyHostToDevice, c->stream) !=
+          cudaSuccess ||
+      launch_round_params(tmp, c->mlp_bf, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  cudaFree(tmp);
+  if (!rc) c->have_mlp = 1;
+  return rc;
+}
+
+int gcvt_ctx_features(gcvt_ctx *c, float *feat, int *ids, int *xy, int capacity, int *count) {
+  if (!c || !count || capacity < 0) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded || !c->learning) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  if (c->cur_n != c->n) return GCVT_ERR_STATE;
+  int rc = ensure_feat(c);
+  if (rc) return rc;
+  if ((rc = start_level(c, c->n, 0, 1, 0x7fffffff))) return rc;  // level set up, state kept
+  const LevelBufs b = level_bufs(c, c->n, 0);
+  int *dids = nullptr, *dxy = nullptr;
+  const size_t cap = c->feat_cap;
+  if (cudaMalloc(reinterpret_cast<void **>(&dids), cap * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&dxy), cap * 2 * sizeof(int)) != cudaSuccess) {
+    cudaFree(dids);
+    return GCVT_ERR_ALLOC;
+  }
+  int total = 0;
+  rc = GCVT_OK;
+  if (launch_list(b, 0, c->stream) != cudaSuccess ||
+      launch_features(b, dids, dxy, 4 * 152, c->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&total, &c->st->snap_count, sizeof(int), cudaMemcpyDeviceToHost,
+                      c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  const size_t w = (size_t)(total < capacity ? total : capacity);
+  if (!rc && w) {
+    if ((feat && cudaMemcpy(feat, c->feat, w * 10 * sizeof(float), cudaMemcpyDeviceToHost) !=
+                     cudaSuccess) ||
+        (ids && cudaMemcpy(ids, dids, w * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) ||
+        (xy && cudaMemcpy(xy, dxy, w * 2 * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = GCVT_ERR_CUDA;
+  }
+  cudaFree(dids);
+  cudaFree(dxy);
+  *count = total;
+  return rc;
+}
+
+int gcvt_ctx_iterate_learned(gcvt_ctx *c, int iterations, int jump_every, int *tried, int *kept) {
+  if (!c || iterations < 0 || jump_every < 1) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded || !c->learning || !c->have_mlp) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  if (c->cur_n != c->n) return GCVT_ERR_STATE;
+  int rc = ensure_feat(c);
+  if (rc) return rc;
+  if ((rc = start_level(c, c->n, 0, iterations > 0 ? iterations : 1, 0x7fffffff))) return rc;
+  if ((rc = pull_state(c))) return rc;
+  const int tried0 = c->st_host->gate_tried, kept0 = c->st_host->gate_kept;
+  const LevelBufs b = level_bufs(c, c->n, 0);
+  for (int done = 0; done < iterations;) {
+    const int k = iterations - done < jump_every ? iterations - done : jump_every;
+    for (int i = 0; i < k; ++i) {
+      CK(launch_list(b, 1, c->stream));
+      CK(launch_cells(b, 0, nullptr, c->stream, c->cell_grid));
+    }
+    done += k;
+    if (done < iterations && (rc = enqueue_jump(c))) return rc;
+  }
+  if ((rc = pull_state(c))) return rc;
+  if (tried) *tried = c->st_host->gate_tried - tried0;
+  if (kept) *kept = c->st_host->gate_kept - kept0;
+  return GCVT_OK;
+}
+
+int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out) {
+  if (!params || (count > 0 && (!feat || !out)) || count < 0) return GCVT_ERR_ARGUMENT;
+  if (count == 0) return GCVT_OK;
+  const int np = mlp_param_count();
+  float *d = nullptr;
+  const size_t floats = (size_t)2 * np + (size_t)count * 12 + 1;
+  if (cudaMalloc(reinterpret_cast<void **>(&d), floats * sizeof(float)) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  float *master = d, *pbf = d + np, *df = d + 2 * np, *dout = df + (size_t)count * 10;
+  int *dcount = reinterpret_cast<int *>(dout + (size_t)count * 2);
+  int rc = GCVT_OK;
+  if (cudaMemcpy(master, params, np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(df, feat, (size_t)count * 10 * sizeof(float), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(dcount, &count, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      launch_round_params(master, pbf, nullptr) != cudaSuccess ||
+      launch_mlp_infer(df, dcount, pbf, dout, 4 * 152, nullptr) != cudaSuccess ||
+      cudaMemcpy(out, dout, (size_t)count * 2 * sizeof(float), cudaMemcpyDeviceToHost) !=
+          cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  cudaFree(d);
+  return rc;
+}
+
+int gcvt_mlp_train(const float *samples, long long count, float *params, int steps, int batch,
+                   float lr, unsigned long long seed, float *loss) {
+  if (!samples || !params || count < 1 || steps < 1 || batch < 1) return GCVT_ERR_ARGUMENT;
+  if (mlp_configure() != cudaSuccess) return GCVT_ERR_CUDA;
+  const int np = mlp_param_count();
+  float *ds = nullptr, *dp = nullptr;
+  cudaStream_t s = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&ds), (size_t)count * 12 * sizeof(float)) !=
+          cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&dp), (size_t)(5 * np + steps) * sizeof(float)) !=
+          cudaSuccess) {
+    cudaFree(ds);
+    return GCVT_ERR_ALLOC;
+  }
+  // master, grad, m, v, bf copy, then one loss per step
+  float *master = dp, *grad = dp + np, *m = dp + 2 * np, *v = dp + 3 * np, *pbf = dp + 4 * np;
+  float *dloss = dp + 5 * np;
+  int rc = GCVT_OK;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMemcpyAsync(ds, samples, (size_t)count * 12 * sizeof(float), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(master, params, np * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemsetAsync(grad, 0, (size_t)(4 * np + steps) * sizeof(float), s) != cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  for (int st = 0; st < steps && !rc; ++st)
+    if (launch_mlp_train_step(ds, count, master, grad, m, v, pbf, dloss + st, batch, seed, st, lr,
+                              s) != cudaSuccess)
+      rc = GCVT_ERR_CUDA;
+  if (!rc && (cudaMemcpyAsync(params, master, np * sizeof(float), cudaMemcpyDeviceToHost, s) !=
+                  cudaSuccess ||
+              (loss && cudaMemcpyAsync(loss, dloss, steps * sizeof(float), cudaMemcpyDeviceToHost,
+                                       s) != cudaSuccess) ||
+              cudaStreamSynchronize(s) != cudaSuccess))
+    rc = GCVT_ERR_CUDA;
+  if (s) cudaStreamDestroy(s);
+  cudaFree(ds);
+  cudaFree(dp);
   return rc;
 }
 

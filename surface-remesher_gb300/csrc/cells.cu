@@ -400,6 +400,22 @@ __device__ void run_schedule(DevState *st, double E, unsigned r2, unsigned mv, i
   if (stop) st->stopped = 1;
   st->cover = min(isqrt_ceil((int)r2) + isqrt_ceil((int)mv), 2 * n);
   st->cur = cur == 2 ? 0 : cur + 1;
+  st->hist_cur ^= 1;
+  st->done_blocks = 0;
+  __threadfence();
+}
+
+// The end of a features pass (MODE 2) or energy pass (MODE 3) of a learned
+// jump: the energy of the configuration the pass saw.  After the energy pass
+// the gate decides: the jump stands if it lowered the energy.
+template <int MODE>
+__device__ void gate_pass_done(DevState *st, double E) {
+  if (MODE == 2) {
+    st->gate_e0 = E;
+  } else {
+    st->gate_e1 = E;
+    st->gate_accept = E < st->gate_e0 ? 1 : 0;
+  }
   st->done_blocks = 0;
   __threadfence();
 }
@@ -410,7 +426,7 @@ struct IterView {
   uint64_t *nxt;         // where the moved sites go
   unsigned *cnt_nxt;     // their per-list-block counts
   float omega;
-  int W0, rb, nsites, cur, slack;
+  int W0, rb, nsites, cur, slack, hc;
   unsigned ngroups;      // 32-site groups of the list
 };
 
@@ -426,6 +442,7 @@ __device__ __forceinline__ IterView iter_view(const LevelBufs &a) {
   v.rb = st->snap_cover;
   v.nsites = st->snap_count;
   v.slack = st->hint_slack;
+  v.hc = st->snap_hist;
   v.ngroups = (unsigned)(v.nsites + 31) / 32;
   return v;
 }
@@ -438,6 +455,7 @@ __device__ __forceinline__ void take_snapshot(DevState *st) {
   st->snap_omega = st->omega;
   st->snap_window = st->window;
   st->snap_cover = st->cover;
+  st->snap_hist = st->hist_cur;
 }
 
 // Clear the bitmap and counts the next iteration writes (nobody reads them
@@ -450,6 +468,29 @@ __device__ __forceinline__ void clear_ahead(const LevelBufs &a, int cur, size_t 
   for (size_t i = t0; i < nwords; i += gthreads) zro[i] = 0ull;
   const size_t nlb = (nwords + kListWords - 1) / kListWords;
   for (size_t i = t0; i < nlb; i += gthreads) czro[i] = 0u;
+}
+
+// Features of listed site idx at (sx, sy) for the learned step: its last four
+// moves (newest first) and the density gradient over the density at the
+// site, all in units of the mean cell radius (DevState::feat_scale).
+__device__ __forceinline__ void site_features(const LevelBufs &a, const IterView &v, int idx,
+                                              int sx, int sy) {
+  const int n = a.n;
+  const float r = a.st->feat_scale, ir = 1.0f / r;
+  const uint64_t h = a.hist[v.hc][(size_t)sy * n + sx];
+  float *f = a.feat + (size_t)idx * 10;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    f[2 * k] = (float)(int8_t)(h >> (16 * k)) * ir;
+    f[2 * k + 1] = (float)(int8_t)(h >> (16 * k + 8)) * ir;
+  }
+  const float *d = a.density;
+  const float r0 = d[(size_t)sy * n + sx];
+  const int xa = max(sx - 1, 0), xb = min(sx + 1, n - 1), ya = max(sy - 1, 0), yb = min(sy + 1, n - 1);
+  const float gx = (d[(size_t)sy * n + xb] - d[(size_t)sy * n + xa]) / (float)(xb - xa);
+  const float gy = (d[(size_t)yb * n + sx] - d[(size_t)ya * n + sx]) / (float)(yb - ya);
+  f[8] = r0 > 0.f ? gx / r0 * r : 0.f;
+  f[9] = r0 > 0.f ? gy / r0 * r : 0.f;
 }
 
 // Group g of a chart (32 listed sites, one per lane).  MODE 0: cells, moves,
@@ -476,6 +517,11 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
       out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
       out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
       out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
+    } else if (MODE == 2 || MODE == 3) {  // learned jump: energy, features or hints
+      dfa(eh, el, cs.eh, cs.el);
+      r2 = (unsigned)cs.r2;
+      if (MODE == 2) site_features(a, v, idx, sx, sy);
+      else a.hint[pid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
     } else {
       dfa(eh, el, cs.eh, cs.el);
       const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
@@ -492,7 +538,14 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
       const unsigned long long old =
           atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
       if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
-      a.hint[(size_t)ny * n + nx] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+      const size_t npid = (size_t)ny * n + nx;
+      a.hint[npid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+      if (a.hist[0]) {  // this move becomes the newest of the site's last four
+        const int mx = min(max(nx - sx, -127), 127), my = min(max(ny - sy, -127), 127);
+        a.hist[v.hc ^ 1][npid] = (a.hist[v.hc][pid] << 16) | (uint64_t)(uint8_t)mx |
+                                 ((uint64_t)(uint8_t)my << 8);
+      }
+      if (a.ids[0]) a.ids[v.hc ^ 1][npid] = a.ids[v.hc][pid];
     }
   }
   __syncwarp();
@@ -540,11 +593,19 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
     mv = max(mv, __float_as_uint(q.w));
   }
   warp_reduce(eh, el, r2, mv);
-  if (lane == 0) run_schedule(st, ((double)eh + (double)el) * st->energy_scale, r2, mv, n, v.cur);
+  if (lane == 0) {
+    const double E = ((double)eh + (double)el) * st->energy_scale;
+    if (MODE == 0) run_schedule(st, E, r2, mv, n, v.cur);
+    else gate_pass_done<MODE>(st, E);
+  }
 }
 
 // One chart.  MODE 0: one Lloyd iteration (sums, move, energy, schedule).
 // MODE 1: moments only (gcvt_ctx_moments); the sites do not move.
+// MODE 2: the features pass of a learned jump: energy of the sites, their
+//         features (DevState::gate_e0, LevelBufs::feat); nothing moves.
+// MODE 3: the energy pass after the jump: energy and hints of the jumped
+//         sites, and the gate's decision (DevState::gate_accept).
 template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
   DevState *st = a.st;
@@ -557,6 +618,10 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
       if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, v.cur);
       return;
     }
+  }
+  if ((MODE == 2 || MODE == 3) && v.ngroups == 0) {
+    if (blockIdx.x == 0 && lane == 0) gate_pass_done<MODE>(st, 0.0);
+    return;
   }
   for (;;) {
     unsigned g = 0;
@@ -841,6 +906,15 @@ cudaError_t cells_configure() {
       cudaSuccess)
     return e;
   per0 = min(per0, per2);
+  for (auto fn : {k_cell<2>, k_cell<3>}) {
+    int per = 0;
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32, 0)) != cudaSuccess)
+      return e;
+    per0 = min(per0, per);
+  }
   g_cell_grid[dev] = sms * max(1, min(per0, per1));
   return cudaSuccess;
 }
@@ -876,8 +950,12 @@ cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cud
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
   if (grid <= 0 || grid > g_cell_grid[dev]) grid = g_cell_grid[dev];
-  if (moments_only) k_cell<1><<<grid, 32, 0, s>>>(b, out4);
-  else k_cell<0><<<grid, 32, 0, s>>>(b, out4);
+  switch (moments_only) {
+    case 1: k_cell<1><<<grid, 32, 0, s>>>(b, out4); break;
+    case 2: k_cell<2><<<grid, 32, 0, s>>>(b, out4); break;
+    case 3: k_cell<3><<<grid, 32, 0, s>>>(b, out4); break;
+    default: k_cell<0><<<grid, 32, 0, s>>>(b, out4);
+  }
   return cudaGetLastError();
 }
 

@@ -57,6 +57,16 @@ struct DevState {
   int snap_cur, snap_stopped, snap_window, snap_cover, snap_count;
   float snap_omega;
   int hint_slack;      // window hint left for a site: 2 R + hint_slack (tuned)
+  // Learned steps (learned.cu): the site histories, and the energy gate of a
+  // jump -- the state before it, so that a rejected jump can be undone.
+  int hist_cur;        // which history buffer holds the current sites' moves
+  int snap_hist;       // hist_cur of the iteration (snapshot)
+  int gate_cur, gate_cover, gate_accept;
+  unsigned gate_jump2; // largest squared jump of the proposal
+  float feat_scale;    // mean cell radius: the unit of the learned features
+  int gate_tried, gate_kept;  // jumps proposed / kept
+  double gate_e0;      // energy before the jump (features pass)
+  double gate_e1;      // energy after it (energy pass)
 };
 
 // Buffers of one resolution level, passed by value to every kernel.
@@ -80,6 +90,13 @@ struct LevelBufs {
                            // radius^2 and max move^2 (as bits)
   float4 *sslot;           // per 64 groups: the same, reduced
   unsigned *scnt;          // per 64 groups: groups finished
+  // learned steps (null when off): per pixel the last four moves of the site
+  // there (int8 dx, dy each, newest in the low bytes), double-buffered
+  // (DevState::hist_cur); per pixel the site's id (training runs only);
+  // per list slot the site's features
+  uint64_t *hist[2];
+  int *ids[2];
+  float *feat;
 };
 
 __device__ __forceinline__ const uint64_t *cur_bits(const LevelBufs &a) {
@@ -119,6 +136,20 @@ cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **res
 cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,
                                unsigned long long *counts, cudaStream_t s);
 cudaError_t jfa_configure();
+int mlp_param_count();
+cudaError_t mlp_configure();
+cudaError_t launch_mlp_infer(const float *feat, const int *count, const float *params_bf,
+                             float *pred, int grid, cudaStream_t s);
+cudaError_t launch_apply(const LevelBufs &b, const float *pred, int grid, cudaStream_t s);
+cudaError_t launch_gate_switch(DevState *st, int n, cudaStream_t s);
+cudaError_t launch_gate_resolve(const LevelBufs &b, int grid, cudaStream_t s);
+cudaError_t launch_features(const LevelBufs &b, int *ids, int *xy, int grid, cudaStream_t s);
+cudaError_t launch_ids_init(const LevelBufs &b, int grid, cudaStream_t s);
+cudaError_t launch_mlp_train_step(const float *samples, long long count, float *master,
+                                  float *grad, float *m, float *v, float *params_bf, float *loss,
+                                  int batch, unsigned long long seed, int step, float lr,
+                                  cudaStream_t s);
+cudaError_t launch_round_params(const float *master, float *params_bf, cudaStream_t s);
 cudaError_t cells_configure();
 size_t list_blocks(int n);
 size_t cell_groups(int n);

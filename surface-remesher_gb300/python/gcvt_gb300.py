@@ -78,6 +78,13 @@ SIGNATURES = {
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
     "gcvt_ctx_jfa_label": ([P, P, P, I], I),
     "gcvt_ctx_autotune": ([P, ctypes.POINTER(Tuning)], I),
+    "gcvt_mlp_param_count": ([], I),
+    "gcvt_ctx_learning": ([P, I, I], I),
+    "gcvt_ctx_set_mlp": ([P, P, I], I),
+    "gcvt_ctx_features": ([P, P, P, P, I, ctypes.POINTER(I)], I),
+    "gcvt_ctx_iterate_learned": ([P, I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+    "gcvt_mlp_forward": ([P, P, I, P], I),
+    "gcvt_mlp_train": ([P, ctypes.c_longlong, P, I, I, ctypes.c_float, ctypes.c_ulonglong, P], I),
     "gcvt_ctx_set_tuning": ([P, ctypes.POINTER(Tuning)], I),
     "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
     "gcvt_batch_destroy": ([P], I),
@@ -240,6 +247,36 @@ class Context:
         t = Tuning(int(cell_blocks_per_sm), int(hint_slack), int(jfa_tail_halo), 0.0, 0.0)
         _check(self.lib.gcvt_ctx_set_tuning(self.h, ctypes.byref(t)), "gcvt_ctx_set_tuning")
 
+    def learning(self, enable=True, track_ids=False):
+        _check(self.lib.gcvt_ctx_learning(self.h, int(bool(enable)), int(bool(track_ids))),
+               "gcvt_ctx_learning")
+
+    def set_mlp(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self.lib.gcvt_ctx_set_mlp(self.h, p.ctypes.data, int(p.size)), "gcvt_ctx_set_mlp")
+
+    def features(self, with_ids=False):
+        """(features (m, 10), ids (m,) or None, xy (m, 2)) of the current sites."""
+        cnt = I(0)
+        _check(self.lib.gcvt_ctx_features(self.h, None, None, None, 0, ctypes.byref(cnt)),
+               "gcvt_ctx_features")
+        m = cnt.value
+        f = np.empty((max(m, 1), 10), np.float32)
+        ids = np.empty(max(m, 1), np.int32) if with_ids else None
+        xy = np.empty((max(m, 1), 2), np.int32)
+        _check(self.lib.gcvt_ctx_features(self.h, f.ctypes.data,
+                                          None if ids is None else ids.ctypes.data,
+                                          xy.ctypes.data, m, ctypes.byref(cnt)),
+               "gcvt_ctx_features")
+        return f[:m], (None if ids is None else ids[:m]), xy[:m]
+
+    def iterate_learned(self, iterations, jump_every=10):
+        tried, kept = I(0), I(0)
+        _check(self.lib.gcvt_ctx_iterate_learned(self.h, int(iterations), int(jump_every),
+                                                 ctypes.byref(tried), ctypes.byref(kept)),
+               "gcvt_ctx_iterate_learned")
+        return tried.value, kept.value
+
     def jfa_label(self, labels=True):
         """(labels or None, (differing, farther, pixels)) of jump flooding."""
         n = self.n
@@ -301,6 +338,42 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def mlp_param_count():
+    return int(load_library().gcvt_mlp_param_count())
+
+
+def mlp_init(seed=0):
+    """He-initialised FP32 parameters of the step MLP."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(mlp_param_count(), np.float32)
+    o = 0
+    for fan_in, fan_out in ((10, 64), (64, 64), (64, 2)):
+        p[o:o + fan_in * fan_out] = rng.normal(0, np.sqrt(2.0 / fan_in), fan_in * fan_out)
+        o += fan_in * fan_out + fan_out
+    return p
+
+
+def mlp_forward(params, feat):
+    lib = load_library()
+    f = np.ascontiguousarray(feat, np.float32)
+    p = np.ascontiguousarray(params, np.float32)
+    out = np.empty((len(f), 2), np.float32)
+    _check(lib.gcvt_mlp_forward(p.ctypes.data, f.ctypes.data, len(f), out.ctypes.data),
+           "gcvt_mlp_forward")
+    return out
+
+
+def mlp_train(samples, params, steps=2000, batch=4096, lr=1e-3, seed=0):
+    """Train on samples (m, 12) float32; returns (params, per-step losses)."""
+    lib = load_library()
+    s = np.ascontiguousarray(samples, np.float32)
+    p = np.array(params, np.float32, copy=True)
+    loss = np.empty(steps, np.float32)
+    _check(lib.gcvt_mlp_train(s.ctypes.data, len(s), p.ctypes.data, int(steps), int(batch),
+                              float(lr), int(seed), loss.ctypes.data), "gcvt_mlp_train")
+    return p, loss
 
 
 def seed_sites(density, mask, num, state=None):

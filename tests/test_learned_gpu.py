@@ -1,0 +1,124 @@
+"""Learned steps: the MLP kernels against numpy, training against a known
+function, the energy gate (a jump that does not lower the energy is undone
+without a trace), and the training features (histories, ids)."""
+import numpy as np
+import pytest
+
+from workloads import MARKER, small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(x):
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def forward_numpy(p, f):
+    W1 = bf16(p[:640]).reshape(10, 64).astype(np.float64)
+    b1 = bf16(p[640:704]).astype(np.float64)
+    W2 = bf16(p[704:4800]).reshape(64, 64).astype(np.float64)
+    b2 = bf16(p[4800:4864]).astype(np.float64)
+    W3 = bf16(p[4864:4992]).reshape(64, 2).astype(np.float64)
+    b3 = bf16(p[4992:4994]).astype(np.float64)
+    x = bf16(f).astype(np.float64)
+    h1 = bf16(np.maximum(x @ W1 + b1, 0).astype(np.float32)).astype(np.float64)
+    h2 = bf16(np.maximum(h1 @ W2 + b2, 0).astype(np.float32)).astype(np.float64)
+    return h2 @ W3 + b3
+
+
+def test_mlp_forward_matches_numpy(gcvt_lib, cuda_device):
+    assert gcvt_lib.mlp_param_count() == 4994
+    p = gcvt_lib.mlp_init(3)
+    p[640:704] = 0.1
+    f = np.random.default_rng(4).normal(0, 1.5, (5000, 10)).astype(np.float32)
+    got = gcvt_lib.mlp_forward(p, f)
+    want = forward_numpy(p, f)
+    # FP32 accumulation vs FP64: the bfloat16 rounding of a hidden value can
+    # flip on a tie-close sum, so compare with a loose bound on the few such
+    assert np.median(np.abs(got - want)) < 1e-4
+    assert np.mean(np.abs(got - want) > 1e-2 * (1 + np.abs(want))) < 0.01
+
+
+def test_training_fits_a_known_step(gcvt_lib, cuda_device):
+    rng = np.random.default_rng(5)
+    f = rng.normal(0, 1, (200000, 10)).astype(np.float32)
+    y = np.stack([0.8 * f[:, 0] - 0.3 * f[:, 2] + 0.2 * np.abs(f[:, 8]),
+                  0.5 * f[:, 1] + 0.4 * f[:, 3] - 0.1 * f[:, 9]], 1).astype(np.float32)
+    samples = np.concatenate([f, y], 1)
+    p0 = gcvt_lib.mlp_init(6)
+    p, loss = gcvt_lib.mlp_train(samples, p0, steps=1500, batch=2048, lr=2e-3, seed=7)
+    assert np.all(np.isfinite(loss))
+    assert loss[-50:].mean() < 0.05 * loss[:10].mean()
+    pred = gcvt_lib.mlp_forward(p, f[:2000])
+    assert np.mean((pred - y[:2000]) ** 2) < 0.02
+
+
+def test_rejected_jumps_leave_no_trace(gcvt_lib, cuda_device):
+    # a zero MLP proposes no move: the jumped sites are the sites, the energy
+    # does not drop, every jump is undone and the run is the plain run
+    sites, rho, mask = small_case(512, 2500, 51)
+    plain = gcvt_lib.Context(512)
+    plain.load(sites, rho, mask)
+    plain.iterate(30)
+    ctx = gcvt_lib.Context(512)
+    ctx.learning(True)
+    ctx.load(sites, rho, mask)
+    ctx.set_mlp(np.zeros(gcvt_lib.mlp_param_count(), np.float32))
+    tried, kept = ctx.iterate_learned(30, jump_every=5)
+    assert (tried, kept) == (5, 0)
+    assert np.array_equal(ctx.sites(), plain.sites())
+    assert ctx.info()["energy"] == plain.info()["energy"]
+    assert np.array_equal(ctx.label(), plain.label())
+    plain.close()
+    ctx.close()
+
+
+def test_kept_jumps_lower_the_energy(gcvt_lib, cuda_device):
+    sites, rho, mask = small_case(512, 2500, 52)
+    ctx = gcvt_lib.Context(512)
+    ctx.learning(True)
+    ctx.load(sites, rho, mask)
+    p = gcvt_lib.mlp_init(8) * 0.1
+    ctx.set_mlp(p)
+    ctx.iterate(10)
+    e0 = ctx.info()["energy"]
+    tried, kept = ctx.iterate_learned(40, jump_every=4)
+    assert tried == 9 and 0 <= kept <= tried
+    e1 = ctx.info()["energy"]
+    assert np.isfinite(e1) and e1 < e0
+    s = ctx.sites()
+    ys, xs = np.nonzero(s[..., 0] != MARKER)
+    assert np.array_equal(s[ys, xs, 0], xs) and np.array_equal(s[ys, xs, 1], ys)
+    ctx.close()
+
+
+def test_features_track_moves_and_ids(gcvt_lib, cuda_device):
+    sites, rho, mask = small_case(512, 2000, 53)
+    m0 = int((sites[..., 0] != MARKER).sum())
+    ctx = gcvt_lib.Context(512)
+    ctx.learning(True, track_ids=True)
+    ctx.load(sites, rho, mask)
+    f0, ids0, xy0 = ctx.features(with_ids=True)
+    assert len(f0) == m0 and np.array_equal(np.sort(ids0), np.arange(m0))
+    assert np.all(f0[:, :8] == 0)  # no moves yet
+    prev = {int(i): tuple(p) for i, p in zip(ids0, xy0)}
+    ctx.iterate(1)
+    f1, ids1, xy1 = ctx.features(with_ids=True)
+    s = ctx.sites()
+    ys, xs = np.nonzero(s[..., 0] != MARKER)
+    assert set(zip(xs.tolist(), ys.tolist())) == set(map(tuple, xy1.tolist()))
+    assert len(np.unique(ids1)) == len(ids1) and ids1.min() >= 0 and ids1.max() < m0
+    # the newest move of each site is its displacement in this iteration
+    r = None
+    for f, i, p in zip(f1, ids1, xy1):
+        dx, dy = p[0] - prev[int(i)][0], p[1] - prev[int(i)][1]
+        if dx or dy:
+            r = dx / f[0] if f[0] else dy / f[1]
+            break
+    assert r is not None and r > 0
+    moves = np.rint(f1[:, :2] * r).astype(int)
+    disp = np.array([(p[0] - prev[int(i)][0], p[1] - prev[int(i)][1]) for i, p in zip(ids1, xy1)])
+    assert np.mean(np.all(moves == disp, 1)) > 0.99  # merges may hand an id on
+    ctx.close()
