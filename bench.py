@@ -96,6 +96,31 @@ def jfa_line(n, ms, stats, peak):
             "mislabel_rate": stats[0] / stats[2], "farther_rate": stats[1] / stats[2]}
 
 
+def time_to_energy_line(G, ctx, n, sites, rho, mask, conv_iters=1000, jump_every=4):
+    """Seconds until the energy is within 1e-4 of the energy after 1000 plain
+    iterations: plain Lloyd, and Lloyd with gated jumps of the learned step
+    MLP (surface-remesher_gb300/data/step_mlp.npy), energies read every 10
+    iterations."""
+    from train_step_mlp import DATA, time_to_energy
+    ctx.load(sites, rho, mask)
+    ctx.iterate(conv_iters)
+    e_conv = ctx.info()["energy"]
+    target = e_conv * (1 + 1e-4)
+    plain = time_to_energy(ctx, sites, rho, mask, target, False, 0, conv_iters)
+    params = np.load(os.path.join(DATA, "step_mlp.npy"))
+    lctx = G.Context(n)
+    lctx.learning(True)
+    lctx.set_mlp(params)
+    learned = time_to_energy(lctx, sites, rho, mask, target, True, jump_every, conv_iters)
+    lctx.close()
+    return {"target": "E <= (1 + 1e-4) E after %d plain iterations" % conv_iters,
+            "e_conv": e_conv,
+            "plain_ms": plain[0] * 1e3, "plain_iterations": plain[1],
+            "learned_ms": learned[0] * 1e3, "learned_iterations": learned[1],
+            "jumps_tried": learned[2], "jumps_kept": learned[3], "jump_every": jump_every,
+            "learned_over_plain": plain[0] / learned[0]}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -299,6 +324,8 @@ def run_ours(args):
         for _ in range(max(1, args.warmup // 2)):
             step_host()
         t_e2e = timed(step_host, args.steps)
+        # time to E <= (1 + 1e-4) E_conv, plain and with gated learned jumps
+        tte = time_to_energy_line(G, ctx, n, sites, rho, mask)
         # a labelling pass (final output) and a jump-flooding labelling,
         # timed alone; the jump-flooding error on the initial sites
         ctx.load(d_sites, d_rho, d_mask)
@@ -330,6 +357,7 @@ def run_ours(args):
         "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1], "jfa_labelling": kms[2]},
         "jfa": jfa_line(n, kms[2], jfa_stats, peak),
         "tuning": tuning,
+        "time_to_energy": tte,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
                      "peak_source": peak_kind,

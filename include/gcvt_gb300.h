@@ -174,7 +174,8 @@ int gcvt_ctx_set_mlp(gcvt_ctx *ctx, const float *params, int count);
 int gcvt_ctx_features(gcvt_ctx *ctx, float *feat, int *ids, int *xy, int capacity, int *count);
 
 /* `iterations` plain Lloyd iterations with a gated jump after every
- * `jump_every` of them; *tried / *kept (may be NULL) count the jumps. */
+ * `jump_every` of them (iterations jump_every, 2 jump_every, ...);
+ * *tried / *kept (may be NULL) count the jumps. */
 int gcvt_ctx_iterate_learned(gcvt_ctx *ctx, int iterations, int jump_every, int *tried,
                              int *kept);
 

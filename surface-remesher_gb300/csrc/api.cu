@@ -941,7 +941,7 @@ int gcvt_ctx_iterate_learned(gcvt_ctx *c, int iterations, int jump_every, int *t
       CK(launch_cells(b, 0, nullptr, c->stream, c->cell_grid));
     }
     done += k;
-    if (done < iterations && (rc = enqueue_jump(c))) return rc;
+    if (k == jump_every && (rc = enqueue_jump(c))) return rc;
   }
   if ((rc = pull_state(c))) return rc;
   if (tried) *tried = c->st_host->gate_tried - tried0;
