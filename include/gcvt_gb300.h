@@ -179,8 +179,12 @@ int gcvt_ctx_features(gcvt_ctx *ctx, float *feat, int *ids, int *xy, int capacit
 int gcvt_ctx_iterate_learned(gcvt_ctx *ctx, int iterations, int jump_every, int *tried,
                              int *kept);
 
-/* The MLP on host feature vectors (count x 10) -> predictions (count x 2). */
-int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out);
+/* The MLP on host feature vectors (count x 10) -> predictions (count x 2):
+ * tensor_cores != 0 runs layers 1 and 2 as tcgen05.mma (bfloat16 operands in
+ * shared memory, FP32 accumulators in tensor memory), 0 on the CUDA cores
+ * (the same bfloat16 rounding).  Jumps use the tensor-core path. */
+int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out,
+                     int tensor_cores);
 
 /* Train the MLP on the GPU (hand-written forward, backward and Adam kernels):
  * samples are count x 12 floats (10 features, 2 targets), mean squared error,

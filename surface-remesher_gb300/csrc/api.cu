@@ -57,6 +57,7 @@ struct gcvt_ctx {
   // learned steps (gcvt_ctx_learning): histories, ids, features, predictions,
   // bfloat16-rounded MLP parameters
   int learning = 0, track_ids = 0, have_mlp = 0;
+  int mlp_tensor_cores = 1;  // MLP forward on tcgen05 (else CUDA cores)
   uint64_t *hist[2] = {};
   int *ids[2] = {};
   float *feat = nullptr, *pred = nullptr, *mlp_bf = nullptr;
@@ -856,7 +857,10 @@ int enqueue_jump(gcvt_ctx *c) {
   const int grid = 4 * 152;
   CK(launch_list(b, 0, c->stream));
   CK(launch_cells(b, 2, nullptr, c->stream, c->cell_grid));
-  CK(launch_mlp_infer(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, grid, c->stream));
+  if (c->mlp_tensor_cores)
+    CK(launch_mlp_tc(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, c->err, c->stream));
+  else
+    CK(launch_mlp_infer(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, grid, c->stream));
   CK(launch_apply(b, c->pred, grid, c->stream));
   CK(launch_gate_switch(c->st, n, c->stream));
   CK(launch_list(b, 0, c->stream));
@@ -949,26 +953,31 @@ int gcvt_ctx_iterate_learned(gcvt_ctx *c, int iterations, int jump_every, int *t
   return GCVT_OK;
 }
 
-int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out) {
+int gcvt_mlp_forward(const float *params, const float *feat, int count, float *out,
+                     int tensor_cores) {
   if (!params || (count > 0 && (!feat || !out)) || count < 0) return GCVT_ERR_ARGUMENT;
   if (count == 0) return GCVT_OK;
   const int np = mlp_param_count();
   float *d = nullptr;
-  const size_t floats = (size_t)2 * np + (size_t)count * 12 + 1;
+  const size_t floats = (size_t)2 * np + (size_t)count * 12 + 2;
   if (cudaMalloc(reinterpret_cast<void **>(&d), floats * sizeof(float)) != cudaSuccess)
     return GCVT_ERR_ALLOC;
   float *master = d, *pbf = d + np, *df = d + 2 * np, *dout = df + (size_t)count * 10;
-  int *dcount = reinterpret_cast<int *>(dout + (size_t)count * 2);
-  int rc = GCVT_OK;
+  int *dcount = reinterpret_cast<int *>(dout + (size_t)count * 2), *derr = dcount + 1;
+  int rc = GCVT_OK, herr = 0;
   if (cudaMemcpy(master, params, np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(df, feat, (size_t)count * 10 * sizeof(float), cudaMemcpyHostToDevice) !=
           cudaSuccess ||
       cudaMemcpy(dcount, &count, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(derr, 0, sizeof(int)) != cudaSuccess ||
       launch_round_params(master, pbf, nullptr) != cudaSuccess ||
-      launch_mlp_infer(df, dcount, pbf, dout, 4 * 152, nullptr) != cudaSuccess ||
+      (tensor_cores ? launch_mlp_tc(df, dcount, pbf, dout, derr, nullptr)
+                    : launch_mlp_infer(df, dcount, pbf, dout, 4 * 152, nullptr)) != cudaSuccess ||
       cudaMemcpy(out, dout, (size_t)count * 2 * sizeof(float), cudaMemcpyDeviceToHost) !=
-          cudaSuccess)
+          cudaSuccess ||
+      cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     rc = GCVT_ERR_CUDA;
+  if (herr) rc = GCVT_ERR_CUDA;
   cudaFree(d);
   return rc;
 }

@@ -140,6 +140,8 @@ int mlp_param_count();
 cudaError_t mlp_configure();
 cudaError_t launch_mlp_infer(const float *feat, const int *count, const float *params_bf,
                              float *pred, int grid, cudaStream_t s);
+cudaError_t launch_mlp_tc(const float *feat, const int *count, const float *params_bf,
+                          float *pred, int *err, cudaStream_t s);
 cudaError_t launch_apply(const LevelBufs &b, const float *pred, int grid, cudaStream_t s);
 cudaError_t launch_gate_switch(DevState *st, int n, cudaStream_t s);
 cudaError_t launch_gate_resolve(const LevelBufs &b, int grid, cudaStream_t s);

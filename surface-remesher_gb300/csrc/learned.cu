@@ -316,6 +316,246 @@ __global__ void k_round_params(const float *master, float *params_bf) {
   if (i < kMlpParams) params_bf[i] = bf(master[i]);
 }
 
+
+// ---- tensor-core forward: tcgen05.mma with accumulators in TMEM -----------
+//
+// One CTA of 128 threads takes tiles of 128 sites.  Layer 1 (K = 10, padded
+// to 16) and layer 2 (K = 64) are tcgen05.mma of kind f16 with bfloat16 A
+// (activations, one row per site) and B (weights, one row per output) in
+// shared memory in the no-swizzle K-major layout -- 8 x 8 core matrices of
+// 128 contiguous bytes, consecutive along K (LBO 128 B), rows of cores
+// KC * 128 B apart (SBO) -- and FP32 accumulators D (128 lanes x 64 columns)
+// in tensor memory.  Thread m reads row m of D with tcgen05.ld, adds the
+// bias, applies ReLU, rounds to bfloat16 and writes row m of the next A;
+// layer 3 (64 -> 2) runs on the CUDA cores from the same registers.
+
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcA1 = 0, kTcA2 = kTcA1 + kTcRows * 16 * 2, kTcB1 = kTcA2 + kTcRows * 64 * 2,
+                   kTcB2 = kTcB1 + 64 * 16 * 2, kTcP = kTcB2 + 64 * 64 * 2,
+                   kTcBar = kTcP + 264 * 4, kTcSlot = kTcBar + 8, kTcSmem = kTcSlot + 8;
+
+// byte offset of element (row, k) in a K-major no-swizzle operand with KC
+// core matrices along K
+__device__ __forceinline__ uint32_t core_off(int row, int k, int kc) {
+  return (uint32_t)((((row >> 3) * kc + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1, no swizzle
+}
+
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, M x N
+__host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t to_smem(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Bounded wait for phase `parity` of the mbarrier; false if it never came.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);  // a in the low half
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp_tc(const float *__restrict__ feat,
+                                                       const int *count,
+                                                       const float *__restrict__ params_bf,
+                                                       float *__restrict__ pred, int *err) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  const int m = threadIdx.x, warp = m >> 5;
+  const uint32_t base = to_smem(tsm);
+  float *P = reinterpret_cast<float *>(tsm + kTcP);  // b1[64], b2[64], W3[128], b3[2]
+  uint32_t *slot = reinterpret_cast<uint32_t *>(tsm + kTcSlot);
+  const uint32_t bar = base + kTcBar;
+  // weights as bfloat16 B operands: B1[n][k] = W1[k][n] (k < 10), B2[n][k] = W2[k][n]
+  for (int e = m; e < 64 * 16; e += kTcRows) {
+    const int nn = e / 16, k = e % 16;
+    const float w = k < kIn ? params_bf[kW1 + k * kHid + nn] : 0.f;
+    *reinterpret_cast<__nv_bfloat16 *>(tsm + kTcB1 + core_off(nn, k, 2)) = __float2bfloat16_rn(w);
+  }
+  for (int e = m; e < 64 * 64; e += kTcRows) {
+    const int nn = e / 64, k = e % 64;
+    *reinterpret_cast<__nv_bfloat16 *>(tsm + kTcB2 + core_off(nn, k, 8)) =
+        __float2bfloat16_rn(params_bf[kW2 + k * kHid + nn]);
+  }
+  for (int e = m; e < 64; e += kTcRows) {
+    P[e] = params_bf[kB1 + e];
+    P[64 + e] = params_bf[kB2 + e];
+  }
+  for (int e = m; e < 128; e += kTcRows) P[128 + e] = params_bf[kW3 + e];
+  if (m < 2) P[256 + m] = params_bf[kB3 + m];
+  if (m == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     to_smem(slot)),
+                 "r"(128u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t idesc = mma_idesc(128, 64);
+  const int ns = *count;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int tile = blockIdx.x; tile * kTcRows < ns && ok; tile += gridDim.x) {
+    const int i = tile * kTcRows + m;
+    // A1 row m: the features as bfloat16, zero beyond the 10th
+    float x[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = (i < ns && k < kIn) ? feat[(size_t)i * kIn + k] : 0.f;
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      *reinterpret_cast<uint4 *>(tsm + kTcA1 + core_off(m, 8 * c, 2)) =
+          make_uint4(pack_bf2(x[8 * c], x[8 * c + 1]), pack_bf2(x[8 * c + 2], x[8 * c + 3]),
+                     pack_bf2(x[8 * c + 4], x[8 * c + 5]), pack_bf2(x[8 * c + 6], x[8 * c + 7]));
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (m == 0) {
+      const uint64_t a = smem_desc(base + kTcA1, 128, 256), b = smem_desc(base + kTcB1, 128, 256);
+      asm volatile(
+          "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
+              tmem),
+          "l"(a), "l"(b), "r"(idesc), "r"(0u)
+          : "memory");
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       bar)
+                   : "memory");
+    }
+    ok = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(ok)) break;
+    tc_fence_after();
+    // layer 1 epilogue -> A2 row m
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(lane_base + 32 * half, v);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float h[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) h[q] = fmaxf(v[8 * c + q] + P[32 * half + 8 * c + q], 0.f);
+        *reinterpret_cast<uint4 *>(tsm + kTcA2 + core_off(m, 32 * half + 8 * c, 8)) =
+            make_uint4(pack_bf2(h[0], h[1]), pack_bf2(h[2], h[3]), pack_bf2(h[4], h[5]),
+                       pack_bf2(h[6], h[7]));
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (m == 0) {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const uint64_t a = smem_desc(base + kTcA2 + 256 * s, 128, 1024),
+                       b = smem_desc(base + kTcB2 + 256 * s, 128, 1024);
+        asm volatile(
+            "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(
+                tmem + 64),
+            "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)s)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       bar)
+                   : "memory");
+    }
+    ok = mbar_wait(bar, phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(ok)) break;
+    tc_fence_after();
+    // layer 2 epilogue and layer 3 on the CUDA cores
+    float o0 = P[256], o1 = P[257];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      tmem_ld32(lane_base + 64 + 32 * half, v);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int j = 32 * half + q;
+        const float h = bf(fmaxf(v[q] + P[64 + j], 0.f));
+        o0 = fmaf(h, P[128 + 2 * j], o0);
+        o1 = fmaf(h, P[128 + 2 * j + 1], o1);
+      }
+    }
+    if (i < ns) {
+      pred[2 * (size_t)i] = o0;
+      pred[2 * (size_t)i + 1] = o1;
+    }
+    tc_fence_before();
+    __syncthreads();  // A1, A2 and the accumulators are reused by the next tile
+    tc_fence_after();
+  }
+  if (!ok && m == 0) atomicOr(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128u));
+}
+
+cudaError_t launch_mlp_tc(const float *feat, const int *count, const float *params_bf,
+                          float *pred, int *err, cudaStream_t s) {
+  static bool configured[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!configured[dev]) {
+    if ((e = cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kTcSmem)) != cudaSuccess)
+      return e;
+    configured[dev] = true;
+  }
+  int sms = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+    return e;
+  // two CTAs per SM hold 256 of the 512 TMEM columns
+  k_mlp_tc<<<2 * sms, kTcRows, kTcSmem, s>>>(feat, count, params_bf, pred, err);
+  return cudaGetLastError();
+}
+
 int mlp_param_count() { return kMlpParams; }
 
 cudaError_t launch_mlp_infer(const float *feat, const int *count, const float *params_bf,

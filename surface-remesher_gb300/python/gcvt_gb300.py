@@ -83,7 +83,7 @@ SIGNATURES = {
     "gcvt_ctx_set_mlp": ([P, P, I], I),
     "gcvt_ctx_features": ([P, P, P, P, I, ctypes.POINTER(I)], I),
     "gcvt_ctx_iterate_learned": ([P, I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
-    "gcvt_mlp_forward": ([P, P, I, P], I),
+    "gcvt_mlp_forward": ([P, P, I, P, I], I),
     "gcvt_mlp_train": ([P, ctypes.c_longlong, P, I, I, ctypes.c_float, ctypes.c_ulonglong, P], I),
     "gcvt_ctx_set_tuning": ([P, ctypes.POINTER(Tuning)], I),
     "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
@@ -355,13 +355,13 @@ def mlp_init(seed=0):
     return p
 
 
-def mlp_forward(params, feat):
+def mlp_forward(params, feat, tensor_cores=True):
     lib = load_library()
     f = np.ascontiguousarray(feat, np.float32)
     p = np.ascontiguousarray(params, np.float32)
     out = np.empty((len(f), 2), np.float32)
-    _check(lib.gcvt_mlp_forward(p.ctypes.data, f.ctypes.data, len(f), out.ctypes.data),
-           "gcvt_mlp_forward")
+    _check(lib.gcvt_mlp_forward(p.ctypes.data, f.ctypes.data, len(f), out.ctypes.data,
+                                int(bool(tensor_cores))), "gcvt_mlp_forward")
     return out
 
 

@@ -28,17 +28,26 @@ def forward_numpy(p, f):
     return h2 @ W3 + b3
 
 
-def test_mlp_forward_matches_numpy(gcvt_lib, cuda_device):
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_mlp_forward_matches_numpy(gcvt_lib, cuda_device, tensor_cores):
     assert gcvt_lib.mlp_param_count() == 4994
     p = gcvt_lib.mlp_init(3)
     p[640:704] = 0.1
     f = np.random.default_rng(4).normal(0, 1.5, (5000, 10)).astype(np.float32)
-    got = gcvt_lib.mlp_forward(p, f)
+    got = gcvt_lib.mlp_forward(p, f, tensor_cores)
     want = forward_numpy(p, f)
     # FP32 accumulation vs FP64: the bfloat16 rounding of a hidden value can
     # flip on a tie-close sum, so compare with a loose bound on the few such
     assert np.median(np.abs(got - want)) < 1e-4
     assert np.mean(np.abs(got - want) > 1e-2 * (1 + np.abs(want))) < 0.01
+
+
+def test_tensor_core_forward_equals_cuda_cores(gcvt_lib, cuda_device):
+    p = gcvt_lib.mlp_init(9)
+    f = np.random.default_rng(10).normal(0, 1.0, (100003, 10)).astype(np.float32)
+    a = gcvt_lib.mlp_forward(p, f, True)
+    b = gcvt_lib.mlp_forward(p, f, False)
+    assert np.mean(np.abs(a - b) <= 1e-3 * (1 + np.abs(b))) > 0.99
 
 
 def test_training_fits_a_known_step(gcvt_lib, cuda_device):
