@@ -75,17 +75,20 @@ def support_pixels(rho):
     return int(((last - first + 1) * rows).sum())
 
 
-def jfa_line(n, ms, stats, peak):
+def jfa_line(n, ms, stats, peak, halo=16):
     """Jump-flooding labelling of the workload's sites: logical passes n/2 ..
-    1 plus 1, launches = passes >= 16 plus one fused tail (8, 4, 2, 1, 1);
-    algorithmic 8 B per pixel per launch (labels in and out)."""
+    1 plus 1; launches = one per step above halo/2 plus one fused tail (halo/2
+    .. 1, 1); algorithmic 8 B per pixel per launch (labels in and out)."""
     k, passes = 1, 1
     while 2 * k <= n // 2:
         k *= 2
     while k >= 1:
         passes += 1
         k //= 2
-    launches = passes - 5 + 1
+    tail = 1
+    while (1 << (tail - 1)) < halo:
+        tail += 1
+    launches = passes - tail + 1
     alg = 8.0 * n * n * launches
     return {"ms": ms, "logical_passes": passes, "launches": launches,
             "gpix_pass_per_s": n * n * passes / (ms / 1e3) / 1e9,
@@ -355,7 +358,7 @@ def run_ours(args):
                    "parallelism": "replicas x%d" % ws},
         "iter_per_s": ITERS * args.steps * ws / t_dev,
         "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1], "jfa_labelling": kms[2]},
-        "jfa": jfa_line(n, kms[2], jfa_stats, peak),
+        "jfa": jfa_line(n, kms[2], jfa_stats, peak, tuning["jfa_tail_halo"]),
         "tuning": tuning,
         "time_to_energy": tte,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

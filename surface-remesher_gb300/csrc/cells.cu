@@ -52,7 +52,7 @@
 
 namespace cvtgb {
 
-constexpr int kMaxCand = 32;  // candidate records per site; more: streamed
+constexpr int kMaxCand = 64;  // candidate records per site; more: streamed
 constexpr int kGroupsPerSlot = 64;
 
 __device__ __forceinline__ void tsum_c(float a, float b, float &s, float &e) {
