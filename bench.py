@@ -522,6 +522,21 @@ def run_batched(args):
     return 0
 
 
+def run_profile_jfa(repeats):
+    """The bench workload's jump-flooding labelling, `repeats` times (for ncu)."""
+    import torch
+    import gcvt_gb300 as G
+    from workloads import config_inputs
+    sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    ctx = G.Context(sites.shape[0])
+    ctx.load(sites, rho, mask)
+    ms = ctx.time_kernels(repeats)[2]
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_jfa": CONFIG, "repeats": repeats, "jfa_ms": ms}))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -535,9 +550,13 @@ def main():
                     help="only run ITERS Lloyd iterations of the workload (for ncu)")
     ap.add_argument("--config", default=CONFIG, choices=[CONFIG, "batched_64"],
                     help="batched_64: the batched-charts workload (its own JSON line)")
+    ap.add_argument("--profile-jfa", type=int, default=0, metavar="REPEATS",
+                    help="only run REPEATS jump-flooding labellings of the workload (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args.profile_case)
+    if args.profile_jfa:
+        return run_profile_jfa(args.profile_jfa)
     if args.warmup < 3:
         args.warmup = 3
     if args.config == "batched_64" and args.impl == "ours":

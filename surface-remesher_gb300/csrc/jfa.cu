@@ -8,10 +8,12 @@
 // The schedule is k = n/2, n/4, ..., 1 and one more step of 1 (for a side
 // that is not a power of two, from the largest power of two <= n/2).
 //
-//   * k > H/2: k_jfa_step, one launch per step, four pixels per thread: the
-//     nine neighbours of a 4-pixel group are three rows of three aligned
-//     16-byte words (k is a multiple of 4), so every load and the store is
-//     128-bit and a warp reads 512 contiguous bytes per row.
+//   * k > H/2: k_jfa_step, one launch per step, sixteen pixels per thread:
+//     four groups of four at (x0 + a k, y + b k), whose neighbours are 4 x 4
+//     aligned 16-byte words (k is a multiple of 4) -- 16 loads for 16
+//     pixels, every load and store 128-bit, a warp reading 512 contiguous
+//     bytes per row.  The nearest label is the smallest 64-bit key
+//     (distance, then x, then y).
 //   * k = H/2, ..., 1, 1: k_jfa_tail<H>, one launch (H = 8, 16 or 32, the
 //     fusion depth; 16 by default, the autotuner picks).  A block loads its
 //     64 x 64 tile with an H-pixel halo (96 x 96 labels, 36 KB, for H = 16)
@@ -29,7 +31,7 @@ namespace cvtgb {
 constexpr int kTile = 64;
 // Tail of halo H: steps H/2, H/4, ..., 1 and the extra 1 (they sum to H) on
 // a (64 + 2H)^2 region; H = 8, 16 or 32 (the fusion depth the autotuner picks).
-template <int H> constexpr int tail_reg() { return kTile + 2 * H; }
+template <int H> __host__ __device__ constexpr int tail_reg() { return kTile + 2 * H; }
 template <int H> constexpr unsigned tail_bytes() {
   return 2u * tail_reg<H>() * tail_reg<H>() * 4u + 64u;  // two buffers + mbarrier
 }
@@ -37,53 +39,76 @@ template <int H> constexpr unsigned tail_bytes() {
 __device__ __forceinline__ int lab_x(uint32_t v) { return (int)(int16_t)(v & 0xffffu); }
 __device__ __forceinline__ int lab_y(uint32_t v) { return (int)(int16_t)(v >> 16); }
 
-// Keep the better of best and c for pixel (x, y).
-__device__ __forceinline__ void consider(uint32_t c, int x, int y, uint32_t &best, int &bd) {
-  if (c == kMarkerWord) return;
-  const int cx = lab_x(c), cy = lab_y(c);
-  const int d = (cx - x) * (cx - x) + (cy - y) * (cy - y);
-  if (d < bd || (d == bd && (cx < lab_x(best) || (cx == lab_x(best) && cy < lab_y(best))))) {
-    best = c;
-    bd = d;
-  }
+// Comparison key of label c for pixel (x, y): squared distance in the high
+// word, the site's (x, y) in the low word (so ties go to the smaller x, then
+// y); no label: all ones.  The nearest label is the smallest key.
+__device__ __forceinline__ unsigned long long jkey(uint32_t c, int x, int y) {
+  const unsigned dx = (unsigned)(lab_x(c) - x), dy = (unsigned)(lab_y(c) - y);
+  const unsigned long long k =
+      ((unsigned long long)(dx * dx + dy * dy) << 32) | __byte_perm(c, 0, 0x1032);
+  return c == kMarkerWord ? ~0ull : k;
+}
+
+__device__ __forceinline__ uint32_t jlabel(unsigned long long k) {
+  return k == ~0ull ? kMarkerWord : __byte_perm((uint32_t)k, 0, 0x1032);
+}
+
+__device__ __forceinline__ unsigned long long kmin(unsigned long long a, unsigned long long b) {
+  return b < a ? b : a;
 }
 
 __device__ __forceinline__ uint32_t comp(const uint4 &v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// One step of offset k (a multiple of 4), four pixels per thread.
+// One step of offset k (a multiple of 4).  A thread takes the 2 x 2 groups of
+// four pixels at (x0 + a k, y + b k), a, b in {0, 1}, (x0, y) in the even
+// k-blocks: their nine neighbours each are 4 x 4 aligned 16-byte words, 16
+// loads for 16 pixels.
 __global__ void __launch_bounds__(256) k_jfa_step(const uint32_t *__restrict__ in,
                                                   uint32_t *__restrict__ out, int n, int k) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y;
-  if (q >= n / 4) return;
-  const int x0 = 4 * q;
+  const int kq = k / 4;
+  const int blocks = (n + 2 * k - 1) / (2 * k);  // k-blocks of even index
+  const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= blocks * kq) return;
+  const int yi = blockIdx.y;
+  const int x0 = (qi / kq) * 2 * k + (qi % kq) * 4;
+  const int y = (yi / k) * 2 * k + (yi % k);
   const uint4 none = make_uint4(kMarkerWord, kMarkerWord, kMarkerWord, kMarkerWord);
-  uint4 c[3][3];
+  uint4 c[4][4];
 #pragma unroll
-  for (int r = 0; r < 3; ++r) {
+  for (int r = 0; r < 4; ++r) {
     const int yy = y + (r - 1) * k;
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
+    for (int s = 0; s < 4; ++s) {
       const int xx = x0 + (s - 1) * k;
       c[r][s] = (yy >= 0 && yy < n && xx >= 0 && xx < n)
                     ? __ldg(reinterpret_cast<const uint4 *>(in + (size_t)yy * n + xx))
                     : none;
     }
   }
-  uint32_t res[4];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    uint32_t best = kMarkerWord;
-    int bd = 0x7fffffff;
+  for (int b = 0; b < 2; ++b) {
+    const int py = y + b * k;
+    if (py >= n) continue;
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int a = 0; a < 2; ++a) {
+      const int px = x0 + a * k;
+      if (px >= n) continue;
+      uint32_t res[4];
 #pragma unroll
-      for (int s = 0; s < 3; ++s) consider(comp(c[r][s], i), x0 + i, y, best, bd);
-    res[i] = best;
+      for (int i = 0; i < 4; ++i) {
+        unsigned long long best = ~0ull;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int s = 0; s < 3; ++s) best = kmin(best, jkey(comp(c[b + r][a + s], i), px + i, py));
+        res[i] = jlabel(best);
+      }
+      *reinterpret_cast<uint4 *>(out + (size_t)py * n + px) =
+          make_uint4(res[0], res[1], res[2], res[3]);
+    }
   }
-  *reinterpret_cast<uint4 *>(out + (size_t)y * n + x0) = make_uint4(res[0], res[1], res[2], res[3]);
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -146,16 +171,15 @@ __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtens
     for (int p = tid; p < w * w; p += blockDim.x) {
       const int i = h + p / w, j = h + p % w;  // buffer row, column
       const int gx = ox + j, gy = oy + i;
-      uint32_t best = kMarkerWord;
+      unsigned long long best = ~0ull;
       if (gx >= 0 && gy >= 0 && gx < n && gy < n) {
-        int bd = 0x7fffffff;
 #pragma unroll
         for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
           for (int dx = -1; dx <= 1; ++dx)
-            consider(cur[(i + dy * k) * kReg + j + dx * k], gx, gy, best, bd);
+            best = kmin(best, jkey(cur[(i + dy * k) * kReg + j + dx * k], gx, gy));
       }
-      nxt[i * kReg + j] = best;
+      nxt[i * kReg + j] = jlabel(best);
     }
     __syncthreads();
     uint32_t *t = cur;
@@ -263,7 +287,8 @@ cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **res
   int k = 1;
   while (2 * k <= n / 2) k *= 2;  // the largest power of two <= n/2
   for (; k > tail_halo / 2; k /= 2) {
-    const dim3 grid((unsigned)((n / 4 + 255) / 256), (unsigned)n);
+    const int blocks = (n + 2 * k - 1) / (2 * k);
+    const dim3 grid((unsigned)((blocks * (k / 4) + 255) / 256), (unsigned)(blocks * k));
     k_jfa_step<<<grid, 256, 0, s>>>(in, out, n, k);
     uint32_t *t = in;
     in = out;
