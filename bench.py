@@ -522,6 +522,75 @@ def run_batched(args):
     return 0
 
 
+def run_mesh(args):
+    """Mesh-driven density (256 x 256-vertex jittered disk mesh with a height
+    field, per-vertex area-ratio weights): rasterised to 2048^2 on the GPU,
+    65,536 sites drawn over it, 100 Lloyd iterations + labels per step."""
+    import torch
+    import gcvt_gb300 as G
+    from workloads import disk_sites, mesh_inputs
+    torch.cuda.set_device(0)
+    n, m, iters = 2048, 65536, 100
+    (pts, w, tris, scale), mask = mesh_inputs(256, n, seed=2)
+    lib = G.load_library()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    rho = G.rasterize(pts, w, tris, scale, n)  # warm-up
+    d_pts = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+    d_w = torch.from_numpy(np.ascontiguousarray(w)).cuda()
+    d_t = torch.from_numpy(np.ascontiguousarray(tris)).cuda()
+    d_rho = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    raster_ms = []
+    for _ in range(max(3, args.steps)):
+        torch.cuda.synchronize()
+        ev[0].record()
+        G._check(lib.gcvt_rasterize(d_pts.data_ptr(), d_w.data_ptr(), len(w), d_t.data_ptr(),
+                                    len(tris), d_rho.data_ptr(), float(scale), n, G.MEM_DEVICE),
+                 "gcvt_rasterize")
+        ev[1].record()
+        ev[1].synchronize()
+        raster_ms.append(ev[0].elapsed_time(ev[1]))
+    rho = d_rho.cpu().numpy()
+    sites = disk_sites(n, m, 3, rho)
+    stream = torch.cuda.Stream()
+    ctx = G.Context(n)
+    ctx.set_stream(stream.cuda_stream)
+    d_sites = torch.from_numpy(sites).cuda()
+    d_mask = torch.from_numpy(mask).cuda()
+    d_out = torch.empty_like(d_sites)
+
+    def step():
+        ctx.load(d_sites, d_rho, d_mask)
+        ctx.iterate(iters)
+        ctx.label(d_out)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        ms = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t = statistics.mean(ms)
+    print(json.dumps({
+        "metric": "Gpix-pass/s, mesh-driven density (2048^2 raster of a 256^2-vertex disk mesh), 65,536 sites, 100 iterations",
+        "value": n * n * (iters + 1) / (t / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 raster, f32+int16 Lloyd",
+        "data": "synthetic (seeded jittered disk mesh, height field, area-ratio weights)",
+        "config": {"workload": "mesh_2048", "n": n, "triangles": int(len(tris)),
+                   "vertices": int(len(w)), "sites": m, "iterations": iters},
+        "raster_ms": statistics.median(raster_ms),
+        "final_energy": ctx.info()["energy"]}))
+    ctx.close()
+    return 0
+
+
 def run_profile_jfa(repeats):
     """The bench workload's jump-flooding labelling, `repeats` times (for ncu)."""
     import torch
@@ -548,8 +617,9 @@ def main():
                     help="also time the reference's own kernels on this GPU")
     ap.add_argument("--profile-case", type=int, default=0, metavar="ITERS",
                     help="only run ITERS Lloyd iterations of the workload (for ncu)")
-    ap.add_argument("--config", default=CONFIG, choices=[CONFIG, "batched_64"],
-                    help="batched_64: the batched-charts workload (its own JSON line)")
+    ap.add_argument("--config", default=CONFIG, choices=[CONFIG, "batched_64", "mesh_2048"],
+                    help="batched_64 / mesh_2048: the batched-charts or mesh-driven workload "
+                         "(their own JSON lines)")
     ap.add_argument("--profile-jfa", type=int, default=0, metavar="REPEATS",
                     help="only run REPEATS jump-flooding labellings of the workload (for ncu)")
     args = ap.parse_args()
@@ -561,6 +631,8 @@ def main():
         args.warmup = 3
     if args.config == "batched_64" and args.impl == "ours":
         return run_batched(args)
+    if args.config == "mesh_2048" and args.impl == "ours":
+        return run_mesh(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -41,16 +41,17 @@ __device__ __forceinline__ int lab_y(uint32_t v) { return (int)(int16_t)(v >> 16
 
 // Comparison key of label c for pixel (x, y): squared distance in the high
 // word, the site's (x, y) in the low word (so ties go to the smaller x, then
-// y); no label: all ones.  The nearest label is the smallest key.
+// y).  The nearest label is the smallest key.  "No label" (MARKER, -32768 in
+// both halves) needs no special case: its squared distance from a pixel of a
+// grid of side <= 8192 lies in [2^31, 3.4e9], no overflow of 32 bits, and is
+// larger than any site's (< 2 * 8192^2).
 __device__ __forceinline__ unsigned long long jkey(uint32_t c, int x, int y) {
   const unsigned dx = (unsigned)(lab_x(c) - x), dy = (unsigned)(lab_y(c) - y);
-  const unsigned long long k =
-      ((unsigned long long)(dx * dx + dy * dy) << 32) | __byte_perm(c, 0, 0x1032);
-  return c == kMarkerWord ? ~0ull : k;
+  return ((unsigned long long)(dx * dx + dy * dy) << 32) | __byte_perm(c, 0, 0x1032);
 }
 
 __device__ __forceinline__ uint32_t jlabel(unsigned long long k) {
-  return k == ~0ull ? kMarkerWord : __byte_perm((uint32_t)k, 0, 0x1032);
+  return __byte_perm((uint32_t)k, 0, 0x1032);
 }
 
 __device__ __forceinline__ unsigned long long kmin(unsigned long long a, unsigned long long b) {
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtens
     for (int p = tid; p < w * w; p += blockDim.x) {
       const int i = h + p / w, j = h + p % w;  // buffer row, column
       const int gx = ox + j, gy = oy + i;
-      unsigned long long best = ~0ull;
+      unsigned long long best = ~0ull;  // outside the grid: no label
       if (gx >= 0 && gy >= 0 && gx < n && gy < n) {
 #pragma unroll
         for (int dy = -1; dy <= 1; ++dy)
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtens
           for (int dx = -1; dx <= 1; ++dx)
             best = kmin(best, jkey(cur[(i + dy * k) * kReg + j + dx * k], gx, gy));
       }
-      nxt[i * kReg + j] = jlabel(best);
+      nxt[i * kReg + j] = best == ~0ull ? kMarkerWord : jlabel(best);
     }
     __syncthreads();
     uint32_t *t = cur;
