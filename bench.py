@@ -577,6 +577,7 @@ def run_mesh(args):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
     t = statistics.mean(ms)
+    lift = lift_stage(ctx, n, args)
     print(json.dumps({
         "metric": "Gpix-pass/s, mesh-driven density (2048^2 raster of a 256^2-vertex disk mesh), 65,536 sites, 100 iterations",
         "value": n * n * (iters + 1) / (t / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
@@ -586,9 +587,68 @@ def run_mesh(args):
         "config": {"workload": "mesh_2048", "n": n, "triangles": int(len(tris)),
                    "vertices": int(len(w)), "sites": m, "iterations": iters},
         "raster_ms": statistics.median(raster_ms),
+        "lift": lift,
         "final_energy": ctx.info()["energy"]}))
     ctx.close()
     return 0
+
+
+def lift_stage(ctx, n, args):
+    """The stage after the CDT: the final sites, extracted as CDT input points
+    (delaunay.h:46-57), lifted onto the surface and the triangles filtered
+    (recover.h:98-157) by gcvt_lift, device buffers, CUDA events.  The CDT
+    itself is scipy's Delaunay on the host (outside the timing).  Beside it,
+    the oracle's single-thread restatement of recover() -- the reference's
+    O(queries x faces) scan -- timed on 400 queries and scaled to all."""
+    import torch
+    import gcvt_gb300 as G
+    from scipy.spatial import Delaunay
+    from workloads import disk_surface, raster_inputs
+    uv, xyz, tris = disk_surface(256, seed=2)
+    _, scale, left, lower = raster_inputs(uv, n)
+    pts = ctx.extract_points(scale, left, lower)
+    cdt = Delaunay(pts).simplices.astype(np.int32)
+    lib = G.load_library()
+    d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (uv, xyz, tris, pts, cdt)]
+    out = torch.empty((len(pts), 3), dtype=torch.float64, device="cuda")
+    face = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+    keep = torch.empty(len(cdt), dtype=torch.uint8, device="cuda")
+
+    def call():
+        G._check(lib.gcvt_lift(d[0].data_ptr(), d[1].data_ptr(), len(uv), d[2].data_ptr(),
+                               len(tris), d[3].data_ptr(), len(pts), 0, None, d[4].data_ptr(),
+                               len(cdt), out.data_ptr(), face.data_ptr(), keep.data_ptr(),
+                               G.MEM_DEVICE), "gcvt_lift")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    times = []
+    for r in range(max(3, args.warmup) + max(3, args.steps)):
+        torch.cuda.synchronize()
+        ev[0].record()
+        call()
+        ev[1].record()
+        ev[1].synchronize()
+        if r >= max(3, args.warmup):
+            times.append(ev[0].elapsed_time(ev[1]))
+    res = {"points": int(len(pts)), "faces": int(len(tris)), "cdt_triangles": int(len(cdt)),
+           "kept": int(keep.sum().item()), "located": int((face >= 0).sum().item()),
+           "lift_ms": statistics.median(times)}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        rng = np.random.default_rng(0)
+        sp = pts[rng.choice(len(pts), 200, replace=False)]
+        corners = pts[cdt[rng.choice(len(cdt), 200, replace=False)]].reshape(-1, 2)
+        t0 = time.perf_counter()
+        orc.lift(uv, xyz, tris, sp, threads=1)
+        t1 = time.perf_counter()
+        # the corners as constraint points (not located), their triangles' centroids located
+        orc.lift(uv, xyz, tris, corners, np.zeros(600, np.int32),
+                 np.arange(600, dtype=np.int32).reshape(200, 3), threads=1)
+        t2 = time.perf_counter()
+        res["cpu_baseline"] = {"kind": "port", "cores": 1,
+                               "sample": "200 points and 200 triangles, scaled to all",
+                               "ms": ((t1 - t0) * len(pts) + (t2 - t1) * len(cdt)) / 200 * 1e3}
+    return res
 
 
 def run_profile_jfa(repeats):

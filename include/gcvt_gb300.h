@@ -268,6 +268,36 @@ int gcvt_rasterize(const double *points, const double *weight, int num_point,
                    const int32_t *triangle, int num_tri, float *density, double scale, int n,
                    int mem);
 
+/* Lift parameter-space points onto the surface: recover() (recover.h:98-157).
+ * The mesh: num_vertex vertices with parameter-space coordinates uv
+ * (2 doubles each) and surface positions xyz (3 doubles each), num_tri faces
+ * (3 vertex indices each, listed in the order vertices_around_face visits
+ * them).  points: 2*num_points doubles, the CDT's input points -- the free
+ * points first, then num_fixed constraint points, which are the mesh vertices
+ * fixed_vertex[0..num_fixed) (delaunay.h:61-67).  For each free point: the
+ * first face in index order whose FP64 barycentric weights (recover.h:30-52)
+ * are all >= 0 (out_face, may be NULL) and the weighted sum of its vertices'
+ * xyz (out_xyz, 3 doubles per point); a point that no face holds keeps the
+ * previous point's face and weights as in the reference (out_face -1, out_xyz
+ * the nearest earlier located free point's, NaN when there is none).  A
+ * constraint point's out_xyz is its vertex's xyz (out_face -1).  keep[t]
+ * (num_cdt bytes) is 1 when the centroid of CDT triangle t (3 point indices
+ * in cdt) lies in a face, the reference's condition for emitting it.  Results
+ * equal the reference's bit for bit.  GCVT_ERR_ARGUMENT on an index out of
+ * range (the other outputs are then unspecified). */
+int gcvt_lift(const double *uv, const double *xyz, int num_vertex, const int32_t *triangle,
+              int num_tri, const double *points, int num_points, int num_fixed,
+              const int32_t *fixed_vertex, const int32_t *cdt, int num_cdt, double *out_xyz,
+              int32_t *out_face, uint8_t *keep, int mem);
+
+/* Per-vertex density weights: weighting_vertices_with_area (weighting.h:38-97).
+ * weight[v] = (sum of the surface areas of the faces at v) / (sum of their
+ * parameter-space areas), both summed in face order; ratios above 1e10 take
+ * the largest ratio that is not (0 when none is positive).  Same mesh arrays
+ * as gcvt_lift; weight: num_vertex doubles. */
+int gcvt_vertex_weights(const double *uv, const double *xyz, int num_vertex,
+                        const int32_t *triangle, int num_tri, double *weight, int mem);
+
 /* The same labelling for callers that cannot allocate device memory -- code
  * handed pre-allocated buffers by a host that owns all device memory, or a
  * loop that must not allocate after start-up.  No counterpart in the

@@ -8,6 +8,10 @@ Outputs:
   oracle/_ref/raster_ref.cubin     its own sources in the reference checkout
                                    (only where that checkout exists; the cubins
                                    are device code and travel with the repo)
+  oracle/_ref/librecover_ref.so -- ref_recover.cpp around the reference's own
+                                   source/recover.h and source/weighting.h (only
+                                   where the checkout exists; host code, so it
+                                   does not run on another architecture)
 
 The reference's gcvt.cu includes <helper_timer.h> from the CUDA Samples
 (gcvt.cu:27) without using it; an empty stand-in header is generated under
@@ -67,8 +71,24 @@ def build_reference_cubins():
     return [p for p in (out_g, out_r) if os.path.exists(p)]
 
 
+def build_reference_recover():
+    """The reference's recover.h / weighting.h behind ref_recover.cpp's
+    stand-ins for CGAL and Boost; None where the checkout is absent."""
+    src = os.path.join(REFERENCE, "source")
+    if not os.path.exists(os.path.join(src, "recover.h")):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    out = os.path.join(REF_OUT, "librecover_ref.so")
+    _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-I", src,
+          "-o", out, os.path.join(HERE, "ref_recover.cpp")])
+    return out
+
+
 def build_all():
     paths = [build_oracle()]
+    rr = build_reference_recover()
+    if rr:
+        paths.append(rr)
     try:
         paths.append(build_harness())
     except RuntimeError as e:  # no CUDA headers: the harness is optional

@@ -1012,6 +1012,153 @@ int orc_rasterize(const double *points, const double *weight, int num_point,
 }
 
 /* ============================================================================
+ * Lift (recover.h:30-157) and weighting (weighting.h:29-97).  Compiled with
+ * -ffp-contract=off: every product and sum is rounded on its own, as in the
+ * reference's host build.
+ * ==========================================================================*/
+
+static double dot2(double x1, double y1, double x2, double y2) { return x1 * x2 + y1 * y2; }
+
+/* barycentric (recover.h:30-52); w[0..2] = the caller's _w[0..2]. */
+static void lift_bary(double x1, double y1, double x2, double y2, double x3, double y3,
+                      double x0, double y0, double w[3]) {
+    double v0x = x2 - x1, v0y = y2 - y1;
+    double v1x = x3 - x1, v1y = y3 - y1;
+    double v2x = x0 - x1, v2y = y0 - y1;
+    double d00 = dot2(v0x, v0y, v0x, v0y);
+    double d01 = dot2(v0x, v0y, v1x, v1y);
+    double d11 = dot2(v1x, v1y, v1x, v1y);
+    double d20 = dot2(v2x, v2y, v0x, v0y);
+    double d21 = dot2(v2x, v2y, v1x, v1y);
+    double denom = d00 * d11 - d01 * d01;
+    if (denom == 0) { w[0] = w[1] = w[2] = -1; return; }
+    w[1] = (d11 * d20 - d01 * d21) / denom;
+    w[2] = (d00 * d21 - d01 * d20) / denom;
+    w[0] = 1.0 - w[1] - w[2];
+}
+
+/* locate (recover.h:64-85): first face, index order, all weights >= 0. */
+static int lift_locate(const double *uv, const int32_t *tri, int nt, double px, double py,
+                       double w[3]) {
+    for (int f = 0; f < nt; ++f) {
+        const int32_t *t = tri + 3 * f;
+        double bc[3];
+        lift_bary(uv[2 * t[0]], uv[2 * t[0] + 1], uv[2 * t[1]], uv[2 * t[1] + 1],
+                  uv[2 * t[2]], uv[2 * t[2] + 1], px, py, bc);
+        if (bc[0] < 0 || bc[1] < 0 || bc[2] < 0) continue;
+        w[0] = bc[0], w[1] = bc[1], w[2] = bc[2];
+        return f;
+    }
+    return -1;
+}
+
+int orc_lift(const double *uv, const double *xyz, int num_vertex, const int32_t *triangle,
+             int num_tri, const double *points, int num_points, int num_fixed,
+             const int32_t *fixed_vertex, const int32_t *cdt, int num_cdt, double *out_xyz,
+             int32_t *out_face, uint8_t *keep, int threads) {
+    if (num_vertex < 0 || num_tri < 0 || num_points < 0 || num_fixed < 0 || num_cdt < 0 ||
+        num_fixed > num_points)
+        return -1;
+    for (long i = 0; i < 3L * num_tri; ++i)
+        if (triangle[i] < 0 || triangle[i] >= num_vertex) return -1;
+    for (int i = 0; i < num_fixed; ++i)
+        if (fixed_vertex[i] < 0 || fixed_vertex[i] >= num_vertex) return -1;
+    for (long i = 0; i < 3L * num_cdt; ++i)
+        if (cdt[i] < 0 || cdt[i] >= num_points) return -1;
+    const int nfree = num_points - num_fixed;
+    int32_t *face = out_face ? out_face : (int32_t *)malloc(sizeof(int32_t) * (nfree + 1));
+    if (!face) return -2;
+#ifdef _OPENMP
+    int saved_threads = omp_get_max_threads();
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    /* recover.h:120-134: lift each free point with its face's vertices */
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < nfree; ++i) {
+        double w[3];
+        int f = lift_locate(uv, triangle, num_tri, points[2 * i], points[2 * i + 1], w);
+        face[i] = f;
+        if (f < 0) continue;
+        const int32_t *t = triangle + 3 * f;
+        for (int d = 0; d < 3; ++d) {
+            double s = 0.0;
+            for (int j = 0; j < 3; ++j) s += xyz[3 * t[j] + d] * w[j];
+            out_xyz[3 * i + d] = s;
+        }
+    }
+    /* recover.h:141-156: keep the triangles whose centroid locates */
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int t = 0; t < num_cdt; ++t) {
+        const int32_t *c = cdt + 3 * t;
+        double cx = (points[2 * c[0]] + points[2 * c[1]] + points[2 * c[2]]) / 3;
+        double cy = (points[2 * c[0] + 1] + points[2 * c[1] + 1] + points[2 * c[2] + 1]) / 3;
+        double w[3];
+        keep[t] = lift_locate(uv, triangle, num_tri, cx, cy, w) >= 0;
+    }
+#ifdef _OPENMP
+    omp_set_num_threads(saved_threads);
+#endif
+    /* an unlocated point reuses the last successful location */
+    int last = -1;
+    for (int i = 0; i < nfree; ++i) {
+        if (face[i] >= 0) { last = i; continue; }
+        for (int d = 0; d < 3; ++d) out_xyz[3 * i + d] = last >= 0 ? out_xyz[3 * last + d] : NAN;
+    }
+    /* recover.h:137-139: constraint points keep their vertex's position */
+    for (int k = 0; k < num_fixed; ++k) {
+        int i = nfree + k;
+        for (int d = 0; d < 3; ++d) out_xyz[3 * i + d] = xyz[3 * fixed_vertex[k] + d];
+        if (out_face) out_face[i] = -1;
+    }
+    if (!out_face) free(face);
+    return 0;
+}
+
+int orc_vertex_weights(const double *uv, const double *xyz, int num_vertex,
+                       const int32_t *triangle, int num_tri, double *weight) {
+    if (num_vertex < 0 || num_tri < 0) return -1;
+    for (long i = 0; i < 3L * num_tri; ++i)
+        if (triangle[i] < 0 || triangle[i] >= num_vertex) return -1;
+    double *a3 = (double *)calloc((size_t)num_vertex + 1, sizeof(double));
+    double *a2 = (double *)calloc((size_t)num_vertex + 1, sizeof(double));
+    uint8_t *over = (uint8_t *)calloc((size_t)num_vertex + 1, 1);
+    if (!a3 || !a2 || !over) { free(a3); free(a2); free(over); return -2; }
+    /* weighting.h:53-60: CGAL face_area of (source(h), target(h), target(next(h))) */
+    for (int f = 0; f < num_tri; ++f) {
+        const int32_t *t = triangle + 3 * f;
+        const double *p = xyz + 3 * t[2], *q = xyz + 3 * t[0], *r = xyz + 3 * t[1];
+        double dqx = q[0] - p[0], dqy = q[1] - p[1], dqz = q[2] - p[2];
+        double drx = r[0] - p[0], dry = r[1] - p[1], drz = r[2] - p[2];
+        double vx = dqy * drz - dqz * dry, vy = dqz * drx - dqx * drz, vz = dqx * dry - dqy * drx;
+        double area = sqrt((vx * vx + vy * vy + vz * vz) / 4);
+        for (int j = 0; j < 3; ++j) a3[t[j]] += area;
+    }
+    /* weighting.h:62-75: get_area (weighting.h:29-36) */
+    for (int f = 0; f < num_tri; ++f) {
+        const int32_t *t = triangle + 3 * f;
+        double ax = uv[2 * t[0]], ay = uv[2 * t[0] + 1];
+        double bx = uv[2 * t[1]] - ax, by = uv[2 * t[1] + 1] - ay;
+        double cx = uv[2 * t[2]] - ax, cy = uv[2 * t[2] + 1] - ay;
+        double area = fabs(bx * cy - cx * by) / 2.;
+        for (int j = 0; j < 3; ++j) a2[t[j]] += area;
+    }
+    /* weighting.h:77-92 */
+    double mx = 0;
+    for (int v = 0; v < num_vertex; ++v) {
+        double w = a3[v] / a2[v];
+        if (w > 1e10) { over[v] = 1; continue; }
+        weight[v] = w;
+        if (w > mx) mx = w;
+    }
+    for (int v = 0; v < num_vertex; ++v)
+        if (over[v]) weight[v] = mx;
+    free(a3); free(a2); free(over);
+    return 0;
+}
+
+/* ============================================================================
  * Seeding (gcvt.h:56-122).  Marsaglia's KISS-style generator with unsigned
  * long taken as 64 bits (LP64).
  * ==========================================================================*/

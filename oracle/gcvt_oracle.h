@@ -102,6 +102,24 @@ int orc_rasterize(const double *points, const double *weight, int num_point,
                   const int32_t *triangle, int num_tri, float *density,
                   double scale, int n, int threads);
 
+/* Lift and weighting (recover.h, weighting.h) --------------------------------*/
+
+/* Restatement of recover (recover.h:98-157) with locate (recover.h:64-85) and
+ * barycentric (recover.h:30-52), host arithmetic (no fused multiply-add):
+ * free points [0, num_points - num_fixed) are located by testing every face
+ * in index order; an unlocated point keeps the previous location (NaN lift
+ * when there is none); constraint points take xyz[fixed_vertex[k]]; keep[t]
+ * says whether CDT triangle t's centroid locates.  out_face may be NULL. */
+int orc_lift(const double *uv, const double *xyz, int num_vertex, const int32_t *triangle,
+             int num_tri, const double *points, int num_points, int num_fixed,
+             const int32_t *fixed_vertex, const int32_t *cdt, int num_cdt, double *out_xyz,
+             int32_t *out_face, uint8_t *keep, int threads);
+
+/* Restatement of weighting_vertices_with_area (weighting.h:38-97) with CGAL's
+ * face_area for the surface areas. */
+int orc_vertex_weights(const double *uv, const double *xyz, int num_vertex,
+                       const int32_t *triangle, int num_tri, double *weight);
+
 /* Seeding (gcvt.h:56-122) ----------------------------------------------------*/
 
 /* putConstrains + randomPoints with the reference's Marsaglia generator in its

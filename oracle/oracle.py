@@ -51,6 +51,10 @@ def lib():
         L.orc_rasterize.restype = I
         L.orc_seed_sites.argtypes = [P, P, P, I, I, ctypes.c_longlong]
         L.orc_seed_sites.restype = I
+        L.orc_lift.argtypes = [P, P, I, P, I, P, I, I, P, P, I, P, P, P, I]
+        L.orc_lift.restype = I
+        L.orc_vertex_weights.argtypes = [P, P, I, P, I, P]
+        L.orc_vertex_weights.restype = I
         _lib = L
     return _lib
 
@@ -140,6 +144,80 @@ def seed_sites(density, mask, num, seed=-1):
                               np.ascontiguousarray(mask, np.uint8).ctypes.data, num, n, seed),
          "orc_seed_sites")
     return v
+
+
+def _lift_args(uv, xyz, triangles, points, fixed, cdt):
+    uv = np.ascontiguousarray(uv, np.float64)
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    tri = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    pts = np.ascontiguousarray(points, np.float64).reshape(-1, 2)
+    fixed = np.ascontiguousarray(np.zeros(0) if fixed is None else fixed, np.int32).ravel()
+    cdt = np.ascontiguousarray(np.zeros((0, 3)) if cdt is None else cdt, np.int32).reshape(-1, 3)
+    return uv, xyz, tri, pts, fixed, cdt
+
+
+def lift(uv, xyz, triangles, points, fixed=None, cdt=None, threads=0):
+    """recover (recover.h:98-157) restated: (lifted xyz (P, 3), face (P,),
+    keep (C,) bool); the last len(fixed) points are the constraint points."""
+    uv, xyz, tri, pts, fixed, cdt = _lift_args(uv, xyz, triangles, points, fixed, cdt)
+    out = np.empty((len(pts), 3), np.float64)
+    face = np.empty(len(pts), np.int32)
+    keep = np.empty(len(cdt), np.uint8)
+    _chk(lib().orc_lift(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data, len(tri),
+                        pts.ctypes.data, len(pts), len(fixed), fixed.ctypes.data, cdt.ctypes.data,
+                        len(cdt), out.ctypes.data, face.ctypes.data, keep.ctypes.data, threads),
+         "orc_lift")
+    return out, face, keep.astype(bool)
+
+
+def vertex_weights(uv, xyz, triangles):
+    """weighting_vertices_with_area (weighting.h:38-97) restated."""
+    uv, xyz, tri, _, _, _ = _lift_args(uv, xyz, triangles, np.zeros((0, 2)), None, None)
+    w = np.empty(len(uv), np.float64)
+    _chk(lib().orc_vertex_weights(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data,
+                                  len(tri), w.ctypes.data), "orc_vertex_weights")
+    return w
+
+
+_recover_ref = None
+
+
+def recover_ref_available():
+    return os.path.exists(os.path.join(REF, "librecover_ref.so"))
+
+
+def _rr():
+    global _recover_ref
+    if _recover_ref is None:
+        R = ctypes.CDLL(os.path.join(REF, "librecover_ref.so"))
+        R.refr_recover.argtypes = [P, P, I, P, I, P, I, P, I, P, I, P, P]
+        R.refr_recover.restype = I
+        R.refr_weights.argtypes = [P, P, I, P, I, P]
+        R.refr_weights.restype = I
+        _recover_ref = R
+    return _recover_ref
+
+
+def ref_lift(uv, xyz, triangles, points, fixed=None, cdt=None):
+    """The reference's own recover() (recover.h, compiled by ref_recover.cpp):
+    (lifted xyz (P, 3), keep (C,) bool)."""
+    uv, xyz, tri, pts, fixed, cdt = _lift_args(uv, xyz, triangles, points, fixed, cdt)
+    out = np.empty((len(pts), 3), np.float64)
+    keep = np.empty(len(cdt), np.uint8)
+    _chk(_rr().refr_recover(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data, len(tri),
+                            pts.ctypes.data, len(pts), fixed.ctypes.data, len(fixed),
+                            cdt.ctypes.data, len(cdt), out.ctypes.data, keep.ctypes.data),
+         "refr_recover")
+    return out, keep.astype(bool)
+
+
+def ref_vertex_weights(uv, xyz, triangles):
+    """The reference's own weighting_vertices_with_area (weighting.h)."""
+    uv, xyz, tri, _, _, _ = _lift_args(uv, xyz, triangles, np.zeros((0, 2)), None, None)
+    w = np.empty(len(uv), np.float64)
+    _chk(_rr().refr_weights(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data, len(tri),
+                            w.ctypes.data), "refr_weights")
+    return w
 
 
 # ---- the reference's own kernels -------------------------------------------

@@ -152,6 +152,9 @@ cudaError_t launch_mlp_train_step(const float *samples, long long count, float *
                                   int batch, unsigned long long seed, int step, float lr,
                                   cudaStream_t s);
 cudaError_t launch_round_params(const float *master, float *params_bf, cudaStream_t s);
+// Exclusive scan of n counts into offset[0..n] (offset[n] = total) and a copy
+// in cursor[0..n-1]; one block, n <= 2^26.
+cudaError_t launch_scan(const int *count, int n, int *offset, int *cursor, cudaStream_t s);
 cudaError_t cells_configure();
 size_t list_blocks(int n);
 size_t cell_groups(int n);

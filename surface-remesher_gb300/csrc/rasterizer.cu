@@ -119,6 +119,12 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const int *count, int ntiles
   if (t == 1023) offset[ntiles] = part[1023];
 }
 
+cudaError_t launch_scan(const int *count, int n, int *offset, int *cursor, cudaStream_t s) {
+  if (n < 0 || n > 1024 * 65536) return cudaErrorInvalidValue;
+  k_tile_scan<<<1, 1024, 0, s>>>(count, n, offset, cursor);
+  return cudaGetLastError();
+}
+
 __global__ void k_tri_scatter(const int4 *__restrict__ tbox, int T, int n, int *cursor,
                               int *list) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;

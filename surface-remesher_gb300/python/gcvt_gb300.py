@@ -92,6 +92,8 @@ SIGNATURES = {
     "gcvt_batch_iterate": ([P, I], I),
     "gcvt_batch_run": ([P, I, P], I),
     "gcvt_centroidal_voronoi": ([P, P, P, I, I, I, I], I),
+    "gcvt_lift": ([P, P, I, P, I, P, I, I, P, P, I, P, P, P, I], I),
+    "gcvt_vertex_weights": ([P, P, I, P, I, P, I], I),
 }
 CPP_SYMBOLS = {"gCVT": "_Z4gCVTPsPfPbiii",
                "discretization_d": "_Z16discretization_dPdS_iPiiPfdi"}
@@ -430,6 +432,42 @@ def rasterize(points, weight, triangles, scale, n):
                               len(weight), _host_ptr(triangles, np.int32), len(triangles),
                               out.ctypes.data, float(scale), int(n), MEM_HOST), "gcvt_rasterize")
     return out
+
+
+def lift(uv, xyz, triangles, points, fixed=None, cdt=None):
+    """recover() (recover.h:98-157) on the GPU.  uv (V, 2) and xyz (V, 3)
+    float64 per mesh vertex, triangles (T, 3) int32, points (P, 2) float64 --
+    the free points, then len(fixed) constraint points whose mesh vertices
+    are `fixed` -- and cdt (C, 3) int32 triangles over the points.  Returns
+    (lifted xyz (P, 3) float64, face (P,) int32, keep (C,) bool)."""
+    lib = load_library()
+    uv = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    tri = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    pts = np.ascontiguousarray(points, np.float64).reshape(-1, 2)
+    fixed = np.ascontiguousarray(np.zeros(0) if fixed is None else fixed, np.int32).ravel()
+    cdt = np.ascontiguousarray(np.zeros((0, 3)) if cdt is None else cdt, np.int32).reshape(-1, 3)
+    out = np.empty((len(pts), 3), np.float64)
+    face = np.empty(len(pts), np.int32)
+    keep = np.empty(len(cdt), np.uint8)
+    _check(lib.gcvt_lift(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data, len(tri),
+                         pts.ctypes.data, len(pts), len(fixed), fixed.ctypes.data,
+                         cdt.ctypes.data, len(cdt), out.ctypes.data, face.ctypes.data,
+                         keep.ctypes.data, MEM_HOST), "gcvt_lift")
+    return out, face, keep.astype(bool)
+
+
+def vertex_weights(uv, xyz, triangles):
+    """weighting_vertices_with_area (weighting.h:38-97) on the GPU: (V,)
+    float64 area-ratio weights."""
+    lib = load_library()
+    uv = np.ascontiguousarray(uv, np.float64).reshape(-1, 2)
+    xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+    tri = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    w = np.empty(len(uv), np.float64)
+    _check(lib.gcvt_vertex_weights(uv.ctypes.data, xyz.ctypes.data, len(uv), tri.ctypes.data,
+                                   len(tri), w.ctypes.data, MEM_HOST), "gcvt_vertex_weights")
+    return w
 
 
 def sites_from_points(n, xs, ys):

@@ -105,17 +105,15 @@ def config_inputs(name, seed=1):
     return sites, rho, mask, c["iters"]
 
 
-def disk_mesh(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
-    """Triangulated unit-disk parameterisation with a height field.
+def disk_surface(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
+    """Triangulated unit-disk parameterisation of a height-field surface.
 
     A regular nv x nv grid on [0,1]^2 (two triangles per cell) keeps the
     triangles whose vertices all lie in the disk of centre (0.5, 0.5); vertices
-    get seeded Gaussian in-plane jitter of jitter x edge; the surface height is
-    z = 0.1 sum_j sin(f_j u + g_j v + phi_j), f, g ~ U(2, 20).  The per-vertex
-    density weight is the area ratio of weighting.h:79: sum of incident 3D face
-    areas / sum of incident UV face areas (ratios above 1e10 take the largest
-    finite ratio, weighting.h:80-92).
-    Returns (uv (V, 2) float64, weight (V,) float64, triangles (T, 3) int32)."""
+    get seeded Gaussian in-plane jitter of jitter x edge; the surface point of
+    parameter (u, v) is (u, v, z), z = 0.1 sum_j sin(f_j u + g_j v + phi_j),
+    f, g ~ U(2, 20).
+    Returns (uv (V, 2) float64, xyz (V, 3) float64, triangles (T, 3) int32)."""
     rng = np.random.default_rng(seed)
     h = 1.0 / (nv - 1)
     g = np.arange(nv) * h
@@ -137,14 +135,21 @@ def disk_mesh(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
     gg = rng.uniform(2, 20, waves)
     phi = rng.uniform(0, 2 * np.pi, waves)
     z = 0.1 * np.sin(np.outer(P[:, 0], f) + np.outer(P[:, 1], gg) + phi).sum(1)
-    P3 = np.concatenate([P, z[:, None]], 1)
-    e1 = P3[tris[:, 1]] - P3[tris[:, 0]]
-    e2 = P3[tris[:, 2]] - P3[tris[:, 0]]
+    return P, np.concatenate([P, z[:, None]], 1), tris.astype(np.int32)
+
+
+def area_weights(uv, xyz, tris):
+    """Per-vertex density weight, the area ratio of weighting.h:79: sum of
+    incident surface face areas / sum of incident parameter-space face areas
+    (ratios above 1e10 take the largest other ratio, weighting.h:80-92).
+    numpy arithmetic; the library's gcvt_vertex_weights is the exact form."""
+    e1 = xyz[tris[:, 1]] - xyz[tris[:, 0]]
+    e2 = xyz[tris[:, 2]] - xyz[tris[:, 0]]
     a3 = 0.5 * np.linalg.norm(np.cross(e1, e2), axis=1)
     u1, u2 = e1[:, :2], e2[:, :2]
     a2 = 0.5 * np.abs(u1[:, 0] * u2[:, 1] - u2[:, 0] * u1[:, 1])
-    s3 = np.zeros(len(P))
-    s2 = np.zeros(len(P))
+    s3 = np.zeros(len(uv))
+    s2 = np.zeros(len(uv))
     for k in range(3):
         np.add.at(s3, tris[:, k], a3)
         np.add.at(s2, tris[:, k], a2)
@@ -152,7 +157,14 @@ def disk_mesh(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
         w = s3 / s2
     finite = np.isfinite(w) & (w <= 1e10)
     w[~finite] = w[finite].max()
-    return P, w, tris.astype(np.int32)
+    return w
+
+
+def disk_mesh(nv=256, jitter=0.3, seed=2, waves=6, radius=0.48):
+    """disk_surface with its per-vertex area-ratio weights.
+    Returns (uv (V, 2) float64, weight (V,) float64, triangles (T, 3) int32)."""
+    uv, xyz, tris = disk_surface(nv, jitter, seed, waves, radius)
+    return uv, area_weights(uv, xyz, tris), tris
 
 
 def raster_inputs(P, n):
