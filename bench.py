@@ -131,6 +131,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, ws, device=None):
+    """The slowest replica's figures: the element-wise maximum over all ranks
+    (one all-reduce; with one rank the values as they are)."""
+    if ws == 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_rate(units_per_step, steps, ws, seconds):
+    """Whole-job throughput in G units per second: every replica processes
+    units_per_step per step, the job takes the slowest replica's seconds."""
+    return units_per_step * steps * ws / seconds / 1e9
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -335,13 +353,9 @@ def run_ours(args):
         _, jfa_stats = ctx.jfa_label(labels=False)
         kms = ctx.time_kernels(5)
         torch.cuda.synchronize(dev)
-    if ws > 1:
-        t = torch.tensor([t_dev, t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev, t_e2e = t.tolist()
-    passes = n * n * PASSES * args.steps * ws
-    value = passes / t_dev / 1e9
-    e2e = passes / t_e2e / 1e9
+    t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], ws, dev)
+    value = job_rate(n * n * PASSES, args.steps, ws, t_dev)
+    e2e = job_rate(n * n * PASSES, args.steps, ws, t_e2e)
     peak, peak_kind = measured_peak()
     support_px = support_pixels(rho)
     alg = (support_px * ALG_BYTES_PER_SUPPORT_PX + n * n * ALG_BYTES_PER_PX

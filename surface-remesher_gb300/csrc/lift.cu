@@ -10,7 +10,7 @@
 //   * skip   -- denominator exactly 0: the reference returns weights -1, so
 //               the face never matches;
 //   * local  -- finite, denominator > 0 and conditioning
-//               d00*d11/denom <= 2^24: binned by its bounding box enlarged by
+//               d00*d11/denom <= 2^20: binned by its bounding box enlarged by
 //               1e-6 of its width + height into a uniform grid over the faces;
 //   * global -- everything else (non-finite coordinates, negative
 //               denominator, ill-conditioned slivers, boxes over more than
@@ -22,10 +22,10 @@
 // (the reference's host build has no fused multiply-add), so the weights are
 // bit-identical.  Why the enlarged box cannot drop a match for a local face:
 // for a point at distance D outside the face, the rounding error of each
-// computed weight is at most about 16 u kappa |p - p1| / h (u = 2^-53, h the
+// computed weight is at most about 32 u kappa |p - p1| / h (u = 2^-53, h the
 // face's height over the weight's edge) while the exact weight is -D / h, so
-// a false "inside" needs D < 16 u kappa (D + L), L the face's size; with
-// kappa <= 2^24 that is D < 3e-8 L, well inside the 1e-6 margin.
+// a false "inside" needs D < 32 u kappa (D + L), L the face's size; with
+// kappa <= 2^20 that is D < 4e-9 L, far inside the 1e-6 margin.
 //
 // Points whose location fails keep the previous point's face and weights in
 // the reference (f_loc is not reset between calls, recover.h:120-134): such a
@@ -44,7 +44,7 @@ namespace cvtgb {
 
 namespace {
 
-constexpr double kMaxCond = 16777216.0;  // 2^24
+constexpr double kMaxCond = 1048576.0;  // 2^20
 constexpr double kMargin = 1e-6;
 constexpr int kMaxCellsPerFace = 1024;
 constexpr int kMaxGrid = 4096;

@@ -10,11 +10,18 @@
 //
 // GB300 version: triangles are binned into 16x16-pixel tiles by their
 // bounding boxes (count, scan, scatter); each pixel scans its tile's list,
-// rejects triangles whose slightly enlarged box misses it, runs the FP64
-// barycentric test -- the reference's expressions, with the fused
-// multiply-adds nvcc forms from them written out explicitly -- on the rest,
-// and keeps the smallest index that passes, which is the reference's first
-// hit.  The enlarged box keeps every triangle whose FP64 test could pass.
+// rejects triangles whose enlarged box misses it, runs the FP64 barycentric
+// test -- the reference's expressions, with the fused multiply-adds nvcc
+// forms from them written out explicitly -- on the rest, and keeps the
+// smallest index that passes, which is the reference's first hit.  Triangles
+// the boxes cannot place go to a global list every pixel tests: non-finite
+// coordinates (their weights are NaN and pass the test), a negative
+// denominator, a conditioning d00*d11/denom above 2^20 (slivers, whose
+// rounded weights can pass far outside the triangle), or a box over more
+// than 4096 tiles.  For the rest the box, enlarged by 1e-6 of its width +
+// height, keeps every pixel whose FP64 test can pass: the weights' rounding
+// errors are below 32 u kappa of the triangle's size (u = 2^-53), under 1e-8
+// of it at kappa <= 2^20.  A denominator of exactly 0 never passes.
 #include "gcvt_internal.cuh"
 #include "../../include/gcvt_gb300.h"
 
@@ -24,12 +31,25 @@
 namespace cvtgb {
 
 constexpr int kTile = 16;
+constexpr double kMaxCond = 1048576.0;  // 2^20
+constexpr int kMaxTilesPerTri = 4096;
 
 struct TriData {
   double x1, y1, x2, y2, x3, y3;  // vertex coordinates, copied from points[]
   int p1, p2, p3;                 // vertex indices (for the weights)
-  int pad;
+  int global;                     // 1: on the global list
 };
+
+// The point-independent terms of the test, as bary_inside computes them.
+__device__ __forceinline__ void tri_terms(const TriData &t, double &d00, double &d01,
+                                          double &d11, double &denom) {
+  const double v0x = __dsub_rn(t.x2, t.x1), v0y = __dsub_rn(t.y2, t.y1);
+  const double v1x = __dsub_rn(t.x3, t.x1), v1y = __dsub_rn(t.y3, t.y1);
+  d00 = __fma_rn(v0x, v0x, __dmul_rn(v0y, v0y));
+  d01 = __fma_rn(v0x, v1x, __dmul_rn(v0y, v1y));
+  d11 = __fma_rn(v1x, v1x, __dmul_rn(v1y, v1y));
+  denom = __fma_rn(d00, d11, -__dmul_rn(d01, d01));
+}
 
 // barycentric_coordinate (discretization.cu:32-55) with the reference's
 // operation order; returns the caller's (w1, w2, w3) after the reference's
@@ -56,38 +76,75 @@ __device__ __forceinline__ bool bary_inside(const TriData &t, double x0, double 
 
 __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restrict__ tri, int T,
                             double inv_scale, int n, TriData *td, int4 *tbox,
-                            int *tile_count) {
+                            int *tile_count, int *glist, int *gcount, int num_point,
+                            int *err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= T) return;
   TriData t;
   t.p1 = tri[3 * i];
   t.p2 = tri[3 * i + 1];
   t.p3 = tri[3 * i + 2];
+  if (t.p1 < 0 || t.p2 < 0 || t.p3 < 0 || t.p1 >= num_point || t.p2 >= num_point ||
+      t.p3 >= num_point) {
+    atomicOr(err, 1);
+    t.p1 = t.p2 = t.p3 = 0;
+    t.x1 = t.y1 = t.x2 = t.y2 = t.x3 = t.y3 = 0.0;  // denominator 0: never passes
+    t.global = 0;
+    td[i] = t;
+    tbox[i] = make_int4(1, 1, 0, 0);
+    return;
+  }
   t.x1 = pts[2 * t.p1];
   t.y1 = pts[2 * t.p1 + 1];
   t.x2 = pts[2 * t.p2];
   t.y2 = pts[2 * t.p2 + 1];
   t.x3 = pts[2 * t.p3];
   t.y3 = pts[2 * t.p3 + 1];
-  t.pad = 0;
-  td[i] = t;
-  // pixel box: pixels whose sample point lies in the triangle's box enlarged
-  // by one part in 2^20 of its size plus a pixel fraction
+  t.global = 0;
+  double d00, d01, d11, denom;
+  tri_terms(t, d00, d01, d11, denom);
   const double xmin = fmin(t.x1, fmin(t.x2, t.x3)), xmax = fmax(t.x1, fmax(t.x2, t.x3));
   const double ymin = fmin(t.y1, fmin(t.y2, t.y3)), ymax = fmax(t.y1, fmax(t.y2, t.y3));
-  const double mx = (xmax - xmin) * 1e-6 + 1e-9 / inv_scale;
-  const double my = (ymax - ymin) * 1e-6 + 1e-9 / inv_scale;
-  int x0 = (int)ceil((xmin - mx) * inv_scale), x1 = (int)floor((xmax + mx) * inv_scale);
-  int y0 = (int)ceil((ymin - my) * inv_scale), y1 = (int)floor((ymax + my) * inv_scale);
+  const bool finite = isfinite(t.x1) && isfinite(t.y1) && isfinite(t.x2) && isfinite(t.y2) &&
+                      isfinite(t.x3) && isfinite(t.y3) && isfinite(denom);
+  if (denom == 0) {  // never passes
+    td[i] = t;
+    tbox[i] = make_int4(1, 1, 0, 0);
+    return;
+  }
+  if (!finite || !(denom > 0) || !(d00 * d11 / denom <= kMaxCond)) {
+    t.global = 1;
+    td[i] = t;
+    tbox[i] = make_int4(0, 0, n - 1, n - 1);
+    glist[atomicAdd(gcount, 1)] = i;
+    return;
+  }
+  // pixel box: pixels whose sample point lies in the triangle's box enlarged
+  // by 1e-6 of its width + height plus a pixel fraction
+  const double m = ((xmax - xmin) + (ymax - ymin)) * 1e-6 + 1e-9 / inv_scale;
+  int x0 = (int)fmax(-1.0, ceil((xmin - m) * inv_scale));
+  int x1 = (int)fmin((double)n, floor((xmax + m) * inv_scale));
+  int y0 = (int)fmax(-1.0, ceil((ymin - m) * inv_scale));
+  int y1 = (int)fmin((double)n, floor((ymax + m) * inv_scale));
   x0 = max(x0, 0);
   y0 = max(y0, 0);
   x1 = min(x1, n - 1);
   y1 = min(y1, n - 1);
-  if (x0 > x1 || y0 > y1 || !(xmin == xmin) || !(ymin == ymin)) {
+  if (x0 > x1 || y0 > y1) {
+    td[i] = t;
     tbox[i] = make_int4(1, 1, 0, 0);  // empty
     return;
   }
   tbox[i] = make_int4(x0, y0, x1, y1);
+  const long long tiles =
+      (long long)(x1 / kTile - x0 / kTile + 1) * (long long)(y1 / kTile - y0 / kTile + 1);
+  if (tiles > kMaxTilesPerTri) {
+    t.global = 1;
+    td[i] = t;
+    glist[atomicAdd(gcount, 1)] = i;
+    return;
+  }
+  td[i] = t;
   const int nt = n / kTile;
   for (int ty = y0 / kTile; ty <= y1 / kTile; ++ty)
     for (int tx = x0 / kTile; tx <= x1 / kTile; ++tx) atomicAdd(&tile_count[ty * nt + tx], 1);
@@ -125,10 +182,10 @@ cudaError_t launch_scan(const int *count, int n, int *offset, int *cursor, cudaS
   return cudaGetLastError();
 }
 
-__global__ void k_tri_scatter(const int4 *__restrict__ tbox, int T, int n, int *cursor,
-                              int *list) {
+__global__ void k_tri_scatter(const TriData *__restrict__ td, const int4 *__restrict__ tbox, int T,
+                              int n, int *cursor, int *list) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= T) return;
+  if (i >= T || td[i].global) return;
   const int4 b = tbox[i];
   if (b.x > b.z) return;
   const int nt = n / kTile;
@@ -144,6 +201,8 @@ __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restri
                                                         const int4 *__restrict__ tbox,
                                                         const int *__restrict__ offset,
                                                         const int *__restrict__ list,
+                                                        const int *__restrict__ glist,
+                                                        const int *__restrict__ gcount,
                                                         const double *__restrict__ weight,
                                                         double scale, int n, float *density) {
   const int nt = n / kTile;
@@ -156,6 +215,20 @@ __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restri
   double bw1 = 0, bw2 = 0, bw3 = 0;
   for (int k = l0; k < l1; ++k) {
     const int i = list[k];
+    if (i >= best) continue;
+    const int4 b = __ldg(&tbox[i]);
+    if (tx < b.x || tx > b.z || ty < b.y || ty > b.w) continue;
+    double w1, w2, w3;
+    if (bary_inside(td[i], x, y, w1, w2, w3)) {
+      best = i;
+      bw1 = w1;
+      bw2 = w2;
+      bw3 = w3;
+    }
+  }
+  const int ng = *gcount;
+  for (int k = 0; k < ng; ++k) {
+    const int i = glist[k];
     if (i >= best) continue;
     const int4 b = __ldg(&tbox[i]);
     if (tx < b.x || tx > b.z || ty < b.y || ty > b.w) continue;
@@ -200,6 +273,8 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
   const int nt = n / kTile, ntiles = nt * nt;
   double *d_pts = nullptr, *d_w = nullptr;
   int *d_tri = nullptr, *d_cnt = nullptr, *d_off = nullptr, *d_cur = nullptr, *d_list = nullptr;
+  int *d_glist = nullptr, *d_scal = nullptr;  // global list; [0] its length, [1] error flag
+  int herr = 0;
   TriData *d_td = nullptr;
   int4 *d_box = nullptr;
   float *d_dens = nullptr;
@@ -225,9 +300,13 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
     RCK(cudaMalloc((void **)&d_cnt, (size_t)ntiles * sizeof(int)));
     RCK(cudaMalloc((void **)&d_off, (size_t)(ntiles + 1) * sizeof(int)));
     RCK(cudaMalloc((void **)&d_cur, (size_t)ntiles * sizeof(int)));
+    RCK(cudaMalloc((void **)&d_glist, (size_t)num_tri * sizeof(int) + 16));
+    RCK(cudaMalloc((void **)&d_scal, 2 * sizeof(int)));
+    RCK(cudaMemset(d_scal, 0, 2 * sizeof(int)));
     RCK(cudaMemset(d_cnt, 0, (size_t)ntiles * sizeof(int)));
     if (num_tri > 0) {
-      k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_box, d_cnt);
+      k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_box,
+                                                  d_cnt, d_glist, d_scal, num_point, d_scal + 1);
       RCK(cudaGetLastError());
     }
     k_tile_scan<<<1, 1024>>>(d_cnt, ntiles, d_off, d_cur);
@@ -235,11 +314,17 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
     RCK(cudaMemcpy(&total, d_off + ntiles, sizeof(int), cudaMemcpyDeviceToHost));
     RCK(cudaMalloc((void **)&d_list, (size_t)total * sizeof(int) + 16));
     if (num_tri > 0) {
-      k_tri_scatter<<<(num_tri + 255) / 256, 256>>>(d_box, num_tri, n, d_cur, d_list);
+      k_tri_scatter<<<(num_tri + 255) / 256, 256>>>(d_td, d_box, num_tri, n, d_cur, d_list);
       RCK(cudaGetLastError());
     }
-    k_raster<<<ntiles, kTile * kTile>>>(d_td, d_box, d_off, d_list, Wt, scale, n, D);
+    k_raster<<<ntiles, kTile * kTile>>>(d_td, d_box, d_off, d_list, d_glist, d_scal, Wt, scale,
+                                        n, D);
     RCK(cudaGetLastError());
+    RCK(cudaMemcpy(&herr, d_scal + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+      rc = GCVT_ERR_ARGUMENT;
+      goto done;
+    }
     if (mem == GCVT_MEM_HOST)
       RCK(cudaMemcpy(density, d_dens, (size_t)n * n * sizeof(float), cudaMemcpyDeviceToHost));
     RCK(cudaDeviceSynchronize());
@@ -255,6 +340,8 @@ done:
   cudaFree(d_off);
   cudaFree(d_cur);
   cudaFree(d_list);
+  cudaFree(d_glist);
+  cudaFree(d_scal);
   return rc;
 }
 

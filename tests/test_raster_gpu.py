@@ -49,3 +49,34 @@ def test_raster_edge_cases(gcvt_lib, cuda_device):
                           orc.rasterize(pts, w, T2, 1.0, n).view(np.int32))
     z = gcvt_lib.rasterize(pts, w, np.zeros((0, 3), np.int32), 1.0, n)
     assert (z == 0).all()
+
+
+def _same_f32(a, b):
+    nan = np.isnan(a)
+    return bool((nan == np.isnan(b)).all() and
+                (a[~nan].view(np.int32) == b[~nan].view(np.int32)).all())
+
+
+def test_raster_triangles_the_boxes_cannot_place(gcvt_lib, cuda_device):
+    """Slivers whose rounded weights pass outside them, nearly collinear and
+    negative-denominator triangles, a triangle larger than the tile limit, and
+    one with a NaN vertex (its weights are NaN, which pass the test, so it
+    takes every pixel no earlier triangle holds): all as the reference."""
+    n = 2048
+    rng = np.random.default_rng(8)
+    base = [[100.0, 100.0], [1900.0, 100.0], [1000.0, 100.0 + 1e-7],      # sliver
+            [200.0, 300.0], [1800.0, 300.0 + 1e-9], [1000.0, 300.0],      # near-collinear
+            [0.0, 0.0], [2047.0, 0.0], [0.0, 2047.0],                     # whole-grid
+            [np.nan, 50.0], [10.0, 20.0], [30.0, 40.0],                    # NaN vertex
+            [500.0, 500.0], [1500.0, 700.0], [900.0, 1600.0]]              # ordinary
+    pts = np.array(base, np.float64)
+    w = rng.uniform(0.5, 2.0, len(pts))
+    tris = np.array([[0, 1, 2], [3, 4, 5], [12, 13, 14], [6, 7, 8], [9, 10, 11]], np.int32)
+    for order in (tris, tris[::-1].copy(), tris[[4, 0, 1, 2, 3]].copy()):
+        got = gcvt_lib.rasterize(pts, w, order, 1.0, n)
+        want = orc.rasterize(pts, w, order, 1.0, n)
+        assert _same_f32(got, want)
+    bad = tris.copy()
+    bad[1, 2] = len(pts)
+    with pytest.raises(RuntimeError):
+        gcvt_lib.rasterize(pts, w, bad, 1.0, n)
