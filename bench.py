@@ -665,6 +665,41 @@ def lift_stage(ctx, n, args):
     return res
 
 
+def run_profile_lift(repeats):
+    """gcvt_lift alone, `repeats` times (for ncu): 65,536 points uniform in the
+    disk on the 256^2-vertex disk mesh, scipy's Delaunay of them as the CDT."""
+    import torch
+    import gcvt_gb300 as G
+    from scipy.spatial import Delaunay
+    from workloads import disk_surface
+    uv, xyz, tris = disk_surface(256, seed=2)
+    rng = np.random.default_rng(5)
+    r = 0.47 * np.sqrt(rng.random(65536))
+    a = rng.random(65536) * 2 * np.pi
+    pts = np.stack([0.5 + r * np.cos(a), 0.5 + r * np.sin(a)], 1)
+    cdt = Delaunay(pts).simplices.astype(np.int32)
+    lib = G.load_library()
+    d = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (uv, xyz, tris, pts, cdt)]
+    out = torch.empty((len(pts), 3), dtype=torch.float64, device="cuda")
+    face = torch.empty(len(pts), dtype=torch.int32, device="cuda")
+    keep = torch.empty(len(cdt), dtype=torch.uint8, device="cuda")
+    ms = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        ev[0].record()
+        G._check(lib.gcvt_lift(d[0].data_ptr(), d[1].data_ptr(), len(uv), d[2].data_ptr(),
+                               len(tris), d[3].data_ptr(), len(pts), 0, None, d[4].data_ptr(),
+                               len(cdt), out.data_ptr(), face.data_ptr(), keep.data_ptr(),
+                               G.MEM_DEVICE), "gcvt_lift")
+        ev[1].record()
+        ev[1].synchronize()
+        ms.append(ev[0].elapsed_time(ev[1]))
+    print(json.dumps({"profile_lift": {"points": len(pts), "faces": len(tris),
+                                       "triangles": len(cdt)}, "ms": ms}))
+    return 0
+
+
 def run_profile_jfa(repeats):
     """The bench workload's jump-flooding labelling, `repeats` times (for ncu)."""
     import torch
@@ -696,11 +731,15 @@ def main():
                          "(their own JSON lines)")
     ap.add_argument("--profile-jfa", type=int, default=0, metavar="REPEATS",
                     help="only run REPEATS jump-flooding labellings of the workload (for ncu)")
+    ap.add_argument("--profile-lift", type=int, default=0, metavar="REPEATS",
+                    help="only run REPEATS lifts of 65,536 points on the mesh (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args.profile_case)
     if args.profile_jfa:
         return run_profile_jfa(args.profile_jfa)
+    if args.profile_lift:
+        return run_profile_lift(args.profile_lift)
     if args.warmup < 3:
         args.warmup = 3
     if args.config == "batched_64" and args.impl == "ours":

@@ -152,6 +152,25 @@ cudaError_t launch_mlp_train_step(const float *samples, long long count, float *
                                   int batch, unsigned long long seed, int step, float lr,
                                   cudaStream_t s);
 cudaError_t launch_round_params(const float *master, float *params_bf, cudaStream_t s);
+// Grow-only device scratch for one call of a one-shot entry point; holds the
+// device's scratch lock for its lifetime (calls on a device serialise).
+// take() returns 256-byte aligned device memory valid until the Scratch is
+// destroyed, or nullptr when no memory can be had.
+class Scratch {
+ public:
+  Scratch();
+  ~Scratch();
+  Scratch(const Scratch &) = delete;
+  Scratch &operator=(const Scratch &) = delete;
+  void *take(size_t bytes);
+  template <class T> T *take(size_t count) { return static_cast<T *>(take(count * sizeof(T))); }
+
+ private:
+  void *pool_;
+  size_t block_, used_, total_;
+  bool ok_;
+};
+
 // Exclusive scan of n counts into offset[0..n] (offset[n] = total) and a copy
 // in cursor[0..n-1]; one block, n <= 2^26.
 cudaError_t launch_scan(const int *count, int n, int *offset, int *cursor, cudaStream_t s);

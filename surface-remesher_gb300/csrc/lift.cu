@@ -10,22 +10,26 @@
 //   * skip   -- denominator exactly 0: the reference returns weights -1, so
 //               the face never matches;
 //   * local  -- finite, denominator > 0 and conditioning
-//               d00*d11/denom <= 2^20: binned by its bounding box enlarged by
-//               1e-6 of its width + height into a uniform grid over the faces;
+//               kappa = d00*d11/denom <= 2^40: binned by its bounding box
+//               enlarged by max(1e-6, kappa 2^-45) of its width + height into
+//               a uniform grid over the faces;
 //   * global -- everything else (non-finite coordinates, negative
-//               denominator, ill-conditioned slivers, boxes over more than
-//               1024 cells): tested by every point.
-// A point scans its grid cell's list and the global list, keeps the smallest
-// face index whose test passes -- the reference's first hit -- and a point
-// with a non-finite coordinate tests every face in order.  The test is the
+//               denominator, kappa above 2^40, boxes over more than 1024
+//               cells): tested by every point.
+// A point scans its grid cell's list (sorted, so the first face that passes
+// ends the scan) and the global list, keeps the smallest face index whose
+// test passes -- the reference's first hit -- and a point with a non-finite
+// coordinate tests every face in order.  The test is the
 // reference's arithmetic with every product, sum and quotient rounded once
 // (the reference's host build has no fused multiply-add), so the weights are
 // bit-identical.  Why the enlarged box cannot drop a match for a local face:
 // for a point at distance D outside the face, the rounding error of each
 // computed weight is at most about 32 u kappa |p - p1| / h (u = 2^-53, h the
 // face's height over the weight's edge) while the exact weight is -D / h, so
-// a false "inside" needs D < 32 u kappa (D + L), L the face's size; with
-// kappa <= 2^20 that is D < 4e-9 L, far inside the 1e-6 margin.
+// a false "inside" needs D < 32 u kappa (D + L), L the face's size, i.e.
+// D < 2^-48 kappa L / (1 - 2^-48 kappa): at kappa <= 2^20 below 4e-9 L, far
+// inside the 1e-6 margin, and below the kappa 2^-45 margin by a factor 8 up
+// to kappa = 2^40.
 //
 // Points whose location fails keep the previous point's face and weights in
 // the reference (f_loc is not reset between calls, recover.h:120-134): such a
@@ -44,7 +48,7 @@ namespace cvtgb {
 
 namespace {
 
-constexpr double kMaxCond = 1048576.0;  // 2^20
+constexpr double kMaxCond = 1099511627776.0;  // 2^40
 constexpr double kMargin = 1e-6;
 constexpr int kMaxCellsPerFace = 1024;
 constexpr int kMaxGrid = 4096;
@@ -83,6 +87,32 @@ __device__ __forceinline__ bool face_test(const LiftFace &f, double px, double p
   return !(c < 0 || a < 0 || b < 0);
 }
 
+// RN(num / denom) < 0 for denom > 0, decided without dividing: num < 0 and
+// the quotient too large to round to -0 (|q| >= 2^-1074 when denom <= 1;
+// otherwise |num| >= denom 2^-1000 keeps it far from underflow).  False
+// means "divide to know".
+__device__ __forceinline__ bool quot_negative(double num, double denom) {
+  return num < 0 && (denom <= 1.0 || -num >= __dmul_rn(denom, 0x1p-1000));
+}
+
+// face_test for a face with a finite denominator > 0 and a finite point: the
+// same results, but a weight whose numerator already shows it negative
+// rejects the face before the two divisions (FP64 issue is scarce on GB300).
+__device__ __forceinline__ bool face_test_local(const LiftFace &f, double px, double py,
+                                                double &c, double &a, double &b) {
+  const double v2x = __dsub_rn(px, f.x1), v2y = __dsub_rn(py, f.y1);
+  const double d20 = dot_rn(v2x, v2y, f.v0x, f.v0y);
+  const double d21 = dot_rn(v2x, v2y, f.v1x, f.v1y);
+  const double na = __dsub_rn(__dmul_rn(f.d11, d20), __dmul_rn(f.d01, d21));
+  if (quot_negative(na, f.denom)) return false;
+  const double nb = __dsub_rn(__dmul_rn(f.d00, d21), __dmul_rn(f.d01, d20));
+  if (quot_negative(nb, f.denom)) return false;
+  a = __ddiv_rn(na, f.denom);
+  b = __ddiv_rn(nb, f.denom);
+  c = __dsub_rn(__dsub_rn(1.0, a), b);
+  return !(c < 0 || a < 0 || b < 0);
+}
+
 // Order-preserving 64-bit keys of doubles for atomic min / max.
 __device__ __forceinline__ long long dkey(double x) {
   const long long b = __double_as_longlong(x);
@@ -102,20 +132,19 @@ __device__ __forceinline__ int cell_y(const Grid &g, double y) {
   return min(g.gy - 1, (int)__dmul_rn(__dsub_rn(y, g.y0), g.iy));
 }
 
-// Per face: the precomputed test terms, the class, the enlarged box and the
-// union of the local faces' boxes (keys[0..3] = min x, min y, max x, max y).
-__global__ void k_lift_faces(const double *__restrict__ uv, int nv, const int *__restrict__ tri,
-                             int nt, LiftFace *faces, Box *ebox, unsigned char *kind,
-                             long long *keys, int *nlocal, int *err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nt) return;
+// Face i: its precomputed test terms, class and enlarged box; true (with the
+// box in e) for a local face.
+__device__ __forceinline__ bool classify_face(const double *__restrict__ uv, int nv,
+                                              const int *__restrict__ tri, int i,
+                                              LiftFace *faces, Box *ebox, unsigned char *kind,
+                                              int *err, Box &e) {
   const int t0 = tri[3 * i], t1 = tri[3 * i + 1], t2 = tri[3 * i + 2];
   LiftFace f{};
   if (t0 < 0 || t1 < 0 || t2 < 0 || t0 >= nv || t1 >= nv || t2 >= nv) {
     atomicOr(err, 1);
     faces[i] = f;  // denom 0: never matches
     kind[i] = 0;
-    return;
+    return false;
   }
   const double x1 = uv[2 * t0], y1 = uv[2 * t0 + 1];
   const double x2 = uv[2 * t1], y2 = uv[2 * t1 + 1];
@@ -133,7 +162,7 @@ __global__ void k_lift_faces(const double *__restrict__ uv, int nv, const int *_
   faces[i] = f;
   if (f.denom == 0) {
     kind[i] = 0;
-    return;
+    return false;
   }
   const double xmin = fmin(x1, fmin(x2, x3)), xmax = fmax(x1, fmax(x2, x3));
   const double ymin = fmin(y1, fmin(y2, y3)), ymax = fmax(y1, fmax(y2, y3));
@@ -143,22 +172,54 @@ __global__ void k_lift_faces(const double *__restrict__ uv, int nv, const int *_
   if (!finite || !(f.denom > 0) || !(cond <= kMaxCond)) {
     kind[i] = kGlobal;
     ebox[i] = Box{-INFINITY, -INFINITY, INFINITY, INFINITY};
-    return;
+    return false;
   }
-  const double m = kMargin * ((xmax - xmin) + (ymax - ymin));
-  const Box e = Box{xmin - m, ymin - m, xmax + m, ymax + m};
+  const double m = fmax(kMargin, cond * 0x1p-45) * ((xmax - xmin) + (ymax - ymin));
+  e = Box{xmin - m, ymin - m, xmax + m, ymax + m};
   if (!(isfinite(e.x) && isfinite(e.y) && isfinite(e.z) && isfinite(e.w))) {
     kind[i] = kGlobal;
     ebox[i] = Box{-INFINITY, -INFINITY, INFINITY, INFINITY};
-    return;
+    return false;
   }
   kind[i] = kLocal;
   ebox[i] = e;
-  atomicMin((long long *)&keys[0], dkey(e.x));
-  atomicMin((long long *)&keys[1], dkey(e.y));
-  atomicMax((long long *)&keys[2], dkey(e.z));
-  atomicMax((long long *)&keys[3], dkey(e.w));
-  atomicAdd(nlocal, 1);
+  return true;
+}
+
+__device__ __forceinline__ long long warp_min64(long long v) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ long long warp_max64(long long v) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Per face: the precomputed test terms, the class, the enlarged box and the
+// union of the local faces' boxes (keys[0..3] = min x, min y, max x, max y;
+// one atomic per warp).
+__global__ void __launch_bounds__(256) k_lift_faces(const double *__restrict__ uv, int nv,
+                                                    const int *__restrict__ tri, int nt,
+                                                    LiftFace *faces, Box *ebox,
+                                                    unsigned char *kind, long long *keys,
+                                                    int *nlocal, int *err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool local = false;
+  Box e{0, 0, 0, 0};
+  if (i < nt) local = classify_face(uv, nv, tri, i, faces, ebox, kind, err, e);
+  const unsigned lanes = __ballot_sync(0xffffffffu, local);
+  if (!lanes) return;
+  const long long k0 = warp_min64(local ? dkey(e.x) : LLONG_MAX);
+  const long long k1 = warp_min64(local ? dkey(e.y) : LLONG_MAX);
+  const long long k2 = warp_max64(local ? dkey(e.z) : LLONG_MIN);
+  const long long k3 = warp_max64(local ? dkey(e.w) : LLONG_MIN);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&keys[0], k0);
+    atomicMin(&keys[1], k1);
+    atomicMax(&keys[2], k2);
+    atomicMax(&keys[3], k3);
+    atomicAdd(nlocal, __popc(lanes));
+  }
 }
 
 // Local faces: count their cells, or move them to the global list when their
@@ -197,6 +258,23 @@ __global__ void k_lift_scatter(const Box *__restrict__ ebox,
     for (int cx = cx0; cx <= cx1; ++cx) list[atomicAdd(&cursor[cy * g.gx + cx], 1)] = i;
 }
 
+// Each cell's list in ascending face order (one thread per cell; lists are
+// a few faces long).
+__global__ void k_lift_sort(const int *__restrict__ offset, int ncell, int *list) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int l0 = offset[c], l1 = offset[c + 1];
+  for (int k = l0 + 1; k < l1; ++k) {
+    const int x = list[k];
+    int j = k - 1;
+    while (j >= l0 && list[j] > x) {
+      list[j + 1] = list[j];
+      --j;
+    }
+    list[j + 1] = x;
+  }
+}
+
 struct Locator {
   const LiftFace *faces;
   const Box *ebox;
@@ -218,14 +296,17 @@ struct Locator {
     }
     int best = INT_MAX;
     if (g.gx > 0 && px >= g.x0 && px <= g.x1 && py >= g.y0 && py <= g.y1) {
+      // the cell's faces in ascending order: the first that passes is the answer
       const int cell = cell_y(g, py) * g.gx + cell_x(g, px);
       const int l1 = offset[cell + 1];
       for (int k = offset[cell]; k < l1; ++k) {
         const int i = list[k];
-        if (i >= best) continue;
         const Box e = ebox[i];
         if (px < e.x || px > e.z || py < e.y || py > e.w) continue;
-        if (face_test(faces[i], px, py, wc, wa, wb)) best = i, c = wc, a = wa, b = wb;
+        if (face_test_local(faces[i], px, py, wc, wa, wb)) {
+          best = i, c = wc, a = wa, b = wb;
+          break;
+        }
       }
     }
     for (int k = 0; k < ngl; ++k) {
@@ -435,44 +516,43 @@ __global__ void k_vertex_fill(const unsigned char *__restrict__ over, int nv,
 
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
-struct DevBuf {
-  void *p = nullptr;
-  ~DevBuf() { cudaFree(p); }
-  template <class T> T *get() const { return (T *)p; }
-  cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes + 16); }
-};
-
 #define LCK(call)                                  \
   do {                                             \
     if ((call) != cudaSuccess) return GCVT_ERR_CUDA; \
   } while (0)
+#define TAKE(ptr, T, count)                                   \
+  do {                                                        \
+    if (!((ptr) = sc.take<T>((size_t)(count)))) return GCVT_ERR_ALLOC; \
+  } while (0)
 
 // Device-pointer core of gcvt_lift.
-int lift_device(const double *uv, const double *xyz, int nv, const int *tri, int nt,
+int lift_device(Scratch &sc, const double *uv, const double *xyz, int nv, const int *tri, int nt,
                 const double *pts, int np, int nfixed, const int *fixed_vertex, const int *cdt,
                 int nc, double *out_xyz, int *out_face, unsigned char *keep) {
-  DevBuf faces, ebox, kind, keys, cnt, off, cur, list, glist, scal, facebuf, blast;
-  LCK(faces.alloc((size_t)nt * sizeof(LiftFace)));
-  LCK(ebox.alloc((size_t)nt * sizeof(Box)));
-  LCK(kind.alloc((size_t)nt));
-  LCK(glist.alloc((size_t)nt * sizeof(int)));
-  LCK(keys.alloc(4 * sizeof(long long)));
-  LCK(scal.alloc(32));  // err, nlocal, gcount; list entries (64-bit) at byte 16
-  int *err = scal.get<int>(), *nlocal = err + 1, *gcount = err + 2;
-  unsigned long long *entries = (unsigned long long *)(scal.get<char>() + 16);
+  LiftFace *faces;
+  Box *ebox;
+  unsigned char *kind;
+  int *glist, *scal, *cnt, *off, *cur, *list, *face, *blast;
+  long long *keys;
+  TAKE(faces, LiftFace, nt);
+  TAKE(ebox, Box, nt);
+  TAKE(kind, unsigned char, nt);
+  TAKE(glist, int, nt);
+  TAKE(keys, long long, 4);
+  TAKE(scal, int, 8);  // err, nlocal, gcount; list entries (64-bit) at byte 16
+  int *err = scal, *nlocal = scal + 1, *gcount = scal + 2;
+  unsigned long long *entries = (unsigned long long *)(scal + 4);
   const long long init[4] = {LLONG_MAX, LLONG_MAX, LLONG_MIN, LLONG_MIN};
-  LCK(cudaMemcpy(keys.p, init, sizeof init, cudaMemcpyHostToDevice));
-  LCK(cudaMemset(scal.p, 0, 32));
+  LCK(cudaMemcpy(keys, init, sizeof init, cudaMemcpyHostToDevice));
+  LCK(cudaMemset(scal, 0, 32));
   if (nt > 0) {
-    k_lift_faces<<<blocks(nt, 256), 256>>>(uv, nv, tri, nt, faces.get<LiftFace>(),
-                                           ebox.get<Box>(), kind.get<unsigned char>(),
-                                           keys.get<long long>(), nlocal, err);
+    k_lift_faces<<<blocks(nt, 256), 256>>>(uv, nv, tri, nt, faces, ebox, kind, keys, nlocal, err);
     LCK(cudaGetLastError());
   }
   long long hk[4];
   int hs[4];
-  LCK(cudaMemcpy(hk, keys.p, sizeof hk, cudaMemcpyDeviceToHost));
-  LCK(cudaMemcpy(hs, scal.p, sizeof hs, cudaMemcpyDeviceToHost));
+  LCK(cudaMemcpy(hk, keys, sizeof hk, cudaMemcpyDeviceToHost));
+  LCK(cudaMemcpy(hs, scal, sizeof hs, cudaMemcpyDeviceToHost));
   Grid g{};
   if (hs[1] > 0) {
     g.x0 = dunkey(hk[0]);
@@ -488,13 +568,12 @@ int lift_device(const double *uv, const double *xyz, int nv, const int *tri, int
     g.iy = ey > 0 ? g.gy / ey : 0.0;
   }
   const int ncell = g.gx * g.gy;
-  LCK(cnt.alloc((size_t)ncell * sizeof(int)));
-  LCK(off.alloc((size_t)(ncell + 1) * sizeof(int)));
-  LCK(cur.alloc((size_t)ncell * sizeof(int)));
-  LCK(cudaMemset(cnt.p, 0, (size_t)ncell * sizeof(int)));
+  TAKE(cnt, int, ncell);
+  TAKE(off, int, ncell + 1);
+  TAKE(cur, int, ncell);
+  LCK(cudaMemset(cnt, 0, (size_t)ncell * sizeof(int)));
   if (nt > 0) {
-    k_lift_count<<<blocks(nt, 256), 256>>>(ebox.get<Box>(), kind.get<unsigned char>(), nt, g,
-                                           cnt.get<int>(), glist.get<int>(), gcount, entries);
+    k_lift_count<<<blocks(nt, 256), 256>>>(ebox, kind, nt, g, cnt, glist, gcount, entries);
     LCK(cudaGetLastError());
   }
   unsigned long long nentries = 0;
@@ -502,23 +581,20 @@ int lift_device(const double *uv, const double *xyz, int nv, const int *tri, int
   if (nentries > (unsigned long long)INT_MAX) return GCVT_ERR_SIZE;
   int total = 0;
   if (ncell > 0) {
-    LCK(launch_scan(cnt.get<int>(), ncell, off.get<int>(), cur.get<int>(), 0));
-    LCK(cudaMemcpy(&total, off.get<int>() + ncell, sizeof(int), cudaMemcpyDeviceToHost));
+    LCK(launch_scan(cnt, ncell, off, cur, 0));
+    LCK(cudaMemcpy(&total, off + ncell, sizeof(int), cudaMemcpyDeviceToHost));
   }
-  LCK(list.alloc((size_t)total * sizeof(int)));
+  TAKE(list, int, total);
   if (nt > 0 && ncell > 0) {
-    k_lift_scatter<<<blocks(nt, 256), 256>>>(ebox.get<Box>(), kind.get<unsigned char>(), nt,
-                                             g, cur.get<int>(), list.get<int>());
+    k_lift_scatter<<<blocks(nt, 256), 256>>>(ebox, kind, nt, g, cur, list);
+    LCK(cudaGetLastError());
+    k_lift_sort<<<blocks(ncell, 256), 256>>>(off, ncell, list);
     LCK(cudaGetLastError());
   }
-  LCK(cudaMemcpy(hs, scal.p, sizeof hs, cudaMemcpyDeviceToHost));
-  Locator L{faces.get<LiftFace>(), ebox.get<Box>(), off.get<int>(), list.get<int>(),
-            glist.get<int>(), hs[2], nt, g};
-  int *face = out_face;
-  if (!face) {
-    LCK(facebuf.alloc((size_t)np * sizeof(int)));
-    face = facebuf.get<int>();
-  }
+  LCK(cudaMemcpy(hs, scal, sizeof hs, cudaMemcpyDeviceToHost));
+  Locator L{faces, ebox, off, list, glist, hs[2], nt, g};
+  face = out_face;
+  if (!face) TAKE(face, int, np);
   const long long nq = (long long)np + nc;
   if (nq > 0) {
     k_lift_locate<<<blocks(nq, 128), 128>>>(L, xyz, nv, tri, pts, np, fixed_vertex, nfixed, cdt,
@@ -528,66 +604,63 @@ int lift_device(const double *uv, const double *xyz, int nv, const int *tri, int
   const int nfree = np - nfixed;
   if (nfree > 0) {
     const int nb = blocks(nfree, kScanBlock);
-    LCK(blast.alloc((size_t)nb * sizeof(int)));
-    k_lift_last<<<nb, kScanBlock>>>(face, nfree, blast.get<int>());
+    TAKE(blast, int, nb);
+    k_lift_last<<<nb, kScanBlock>>>(face, nfree, blast);
     LCK(cudaGetLastError());
-    k_lift_stale<<<nb, kScanBlock>>>(face, nfree, blast.get<int>(), out_xyz);
+    k_lift_stale<<<nb, kScanBlock>>>(face, nfree, blast, out_xyz);
     LCK(cudaGetLastError());
   }
-  LCK(cudaMemcpy(hs, scal.p, sizeof hs, cudaMemcpyDeviceToHost));
+  LCK(cudaMemcpy(hs, scal, sizeof hs, cudaMemcpyDeviceToHost));
   return hs[0] ? GCVT_ERR_ARGUMENT : GCVT_OK;
 }
 
-int weights_device(const double *uv, const double *xyz, int nv, const int *tri, int nt,
-                   double *weight) {
-  DevBuf area, cnt, off, cur, inc, over, scal;
-  LCK(area.alloc((size_t)nt * sizeof(double2)));
-  LCK(cnt.alloc((size_t)nv * sizeof(int)));
-  LCK(off.alloc((size_t)(nv + 1) * sizeof(int)));
-  LCK(cur.alloc((size_t)nv * sizeof(int)));
-  LCK(inc.alloc((size_t)nt * 3 * sizeof(int)));
-  LCK(over.alloc((size_t)nv));
-  LCK(scal.alloc(16));
-  int *err = scal.get<int>();
-  unsigned long long *mx = (unsigned long long *)(scal.get<char>() + 8);
-  LCK(cudaMemset(scal.p, 0, 16));  // mx starts at +0.0
-  LCK(cudaMemset(cnt.p, 0, (size_t)nv * sizeof(int)));
+int weights_device(Scratch &sc, const double *uv, const double *xyz, int nv, const int *tri,
+                   int nt, double *weight) {
+  double2 *area;
+  int *cnt, *off, *cur, *inc, *scal;
+  unsigned char *over;
+  TAKE(area, double2, nt);
+  TAKE(cnt, int, nv);
+  TAKE(off, int, nv + 1);
+  TAKE(cur, int, nv);
+  TAKE(inc, int, (size_t)nt * 3);
+  TAKE(over, unsigned char, nv);
+  TAKE(scal, int, 4);
+  int *err = scal;
+  unsigned long long *mx = (unsigned long long *)(scal + 2);
+  LCK(cudaMemset(scal, 0, 16));  // mx starts at +0.0
+  LCK(cudaMemset(cnt, 0, (size_t)nv * sizeof(int)));
   if (nt > 0) {
-    k_face_areas<<<blocks(nt, 256), 256>>>(uv, xyz, nv, tri, nt, area.get<double2>(),
-                                           cnt.get<int>(), err);
+    k_face_areas<<<blocks(nt, 256), 256>>>(uv, xyz, nv, tri, nt, area, cnt, err);
     LCK(cudaGetLastError());
   }
-  LCK(launch_scan(cnt.get<int>(), nv, off.get<int>(), cur.get<int>(), 0));
+  LCK(launch_scan(cnt, nv, off, cur, 0));
   if (nt > 0) {
-    k_vertex_faces<<<blocks(nt, 256), 256>>>(tri, nt, nv, cur.get<int>(), inc.get<int>());
+    k_vertex_faces<<<blocks(nt, 256), 256>>>(tri, nt, nv, cur, inc);
     LCK(cudaGetLastError());
   }
-  k_vertex_weight<<<blocks(nv, 256), 256>>>(off.get<int>(), inc.get<int>(), area.get<double2>(),
-                                            nv, weight, over.get<unsigned char>(), mx);
+  k_vertex_weight<<<blocks(nv, 256), 256>>>(off, inc, area, nv, weight, over, mx);
   LCK(cudaGetLastError());
-  k_vertex_fill<<<blocks(nv, 256), 256>>>(over.get<unsigned char>(), nv, mx, weight);
+  k_vertex_fill<<<blocks(nv, 256), 256>>>(over, nv, mx, weight);
   LCK(cudaGetLastError());
   int herr = 0;
   LCK(cudaMemcpy(&herr, err, sizeof herr, cudaMemcpyDeviceToHost));
   return herr ? GCVT_ERR_ARGUMENT : GCVT_OK;
 }
 
-// Host buffers: copy in, run, copy out.
-struct HostCopy {
-  DevBuf buf;
-  template <class T> int in(const T *h, size_t count, const T **d) {
-    if (buf.alloc(count * sizeof(T)) != cudaSuccess) return GCVT_ERR_CUDA;
-    if (count && cudaMemcpy(buf.p, h, count * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
-      return GCVT_ERR_CUDA;
-    *d = buf.get<T>();
-    return GCVT_OK;
-  }
-  template <class T> int out(size_t count, T **d) {
-    if (buf.alloc(count * sizeof(T)) != cudaSuccess) return GCVT_ERR_CUDA;
-    *d = buf.get<T>();
-    return GCVT_OK;
-  }
-};
+// Host buffers: copied into scratch, results copied back.
+template <class T> int copy_in(Scratch &sc, const T *h, size_t count, const T **d) {
+  T *p = sc.take<T>(count);
+  if (!p) return GCVT_ERR_ALLOC;
+  if (count && cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return GCVT_ERR_CUDA;
+  *d = p;
+  return GCVT_OK;
+}
+template <class T> int take_out(Scratch &sc, size_t count, T **d) {
+  *d = sc.take<T>(count);
+  return *d ? GCVT_OK : GCVT_ERR_ALLOC;
+}
 
 #define HCK(call)               \
   do {                          \
@@ -615,25 +688,25 @@ extern "C" int gcvt_lift(const double *uv, const double *xyz, int num_vertex,
   if ((long long)num_tri * 3 > INT_MAX || (long long)num_points * 3 > INT_MAX ||
       (long long)num_cdt * 3 > INT_MAX)
     return GCVT_ERR_SIZE;
+  Scratch sc;
   if (mem == GCVT_MEM_DEVICE)
-    return lift_device(uv, xyz, num_vertex, triangle, num_tri, points, num_points, num_fixed,
+    return lift_device(sc, uv, xyz, num_vertex, triangle, num_tri, points, num_points, num_fixed,
                        fixed_vertex, cdt, num_cdt, out_xyz, out_face, keep);
-  HostCopy c_uv, c_xyz, c_tri, c_pts, c_fix, c_cdt, c_out, c_face, c_keep;
   const double *d_uv = nullptr, *d_xyz = nullptr, *d_pts = nullptr;
   const int *d_tri = nullptr, *d_fix = nullptr, *d_cdt = nullptr;
   double *d_out = nullptr;
   int *d_face = nullptr;
   unsigned char *d_keep = nullptr;
-  HCK(c_uv.in(uv, (size_t)num_vertex * 2, &d_uv));
-  HCK(c_xyz.in(xyz, (size_t)num_vertex * 3, &d_xyz));
-  HCK(c_tri.in(triangle, (size_t)num_tri * 3, &d_tri));
-  HCK(c_pts.in(points, (size_t)num_points * 2, &d_pts));
-  HCK(c_fix.in(fixed_vertex, (size_t)num_fixed, &d_fix));
-  HCK(c_cdt.in(cdt, (size_t)num_cdt * 3, &d_cdt));
-  HCK(c_out.out((size_t)num_points * 3, &d_out));
-  HCK(c_face.out((size_t)num_points, &d_face));
-  HCK(c_keep.out((size_t)num_cdt, &d_keep));
-  const int rc = lift_device(d_uv, d_xyz, num_vertex, d_tri, num_tri, d_pts, num_points,
+  HCK(copy_in(sc, uv, (size_t)num_vertex * 2, &d_uv));
+  HCK(copy_in(sc, xyz, (size_t)num_vertex * 3, &d_xyz));
+  HCK(copy_in(sc, triangle, (size_t)num_tri * 3, &d_tri));
+  HCK(copy_in(sc, points, (size_t)num_points * 2, &d_pts));
+  HCK(copy_in(sc, fixed_vertex, (size_t)num_fixed, &d_fix));
+  HCK(copy_in(sc, cdt, (size_t)num_cdt * 3, &d_cdt));
+  HCK(take_out(sc, (size_t)num_points * 3, &d_out));
+  HCK(take_out(sc, (size_t)num_points, &d_face));
+  HCK(take_out(sc, (size_t)num_cdt, &d_keep));
+  const int rc = lift_device(sc, d_uv, d_xyz, num_vertex, d_tri, num_tri, d_pts, num_points,
                              num_fixed, d_fix, d_cdt, num_cdt, d_out, d_face, d_keep);
   if (rc != GCVT_OK) return rc;
   if (num_points &&
@@ -658,16 +731,17 @@ extern "C" int gcvt_vertex_weights(const double *uv, const double *xyz, int num_
     return GCVT_ERR_ARGUMENT;
   if ((long long)num_tri * 3 > INT_MAX) return GCVT_ERR_SIZE;
   if (num_vertex == 0) return GCVT_OK;
-  if (mem == GCVT_MEM_DEVICE) return weights_device(uv, xyz, num_vertex, triangle, num_tri, weight);
-  HostCopy c_uv, c_xyz, c_tri, c_w;
+  Scratch sc;
+  if (mem == GCVT_MEM_DEVICE)
+    return weights_device(sc, uv, xyz, num_vertex, triangle, num_tri, weight);
   const double *d_uv = nullptr, *d_xyz = nullptr;
   const int *d_tri = nullptr;
   double *d_w = nullptr;
-  HCK(c_uv.in(uv, (size_t)num_vertex * 2, &d_uv));
-  HCK(c_xyz.in(xyz, (size_t)num_vertex * 3, &d_xyz));
-  HCK(c_tri.in(triangle, (size_t)num_tri * 3, &d_tri));
-  HCK(c_w.out((size_t)num_vertex, &d_w));
-  const int rc = weights_device(d_uv, d_xyz, num_vertex, d_tri, num_tri, d_w);
+  HCK(copy_in(sc, uv, (size_t)num_vertex * 2, &d_uv));
+  HCK(copy_in(sc, xyz, (size_t)num_vertex * 3, &d_xyz));
+  HCK(copy_in(sc, triangle, (size_t)num_tri * 3, &d_tri));
+  HCK(take_out(sc, (size_t)num_vertex, &d_w));
+  const int rc = weights_device(sc, d_uv, d_xyz, num_vertex, d_tri, num_tri, d_w);
   if (rc != GCVT_OK) return rc;
   if (cudaMemcpy(weight, d_w, (size_t)num_vertex * sizeof(double), cudaMemcpyDeviceToHost) !=
       cudaSuccess)

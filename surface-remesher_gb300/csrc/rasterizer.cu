@@ -16,12 +16,16 @@
 // smallest index that passes, which is the reference's first hit.  Triangles
 // the boxes cannot place go to a global list every pixel tests: non-finite
 // coordinates (their weights are NaN and pass the test), a negative
-// denominator, a conditioning d00*d11/denom above 2^20 (slivers, whose
-// rounded weights can pass far outside the triangle), or a box over more
-// than 4096 tiles.  For the rest the box, enlarged by 1e-6 of its width +
-// height, keeps every pixel whose FP64 test can pass: the weights' rounding
-// errors are below 32 u kappa of the triangle's size (u = 2^-53), under 1e-8
-// of it at kappa <= 2^20.  A denominator of exactly 0 never passes.
+// denominator, a conditioning kappa = d00*d11/denom above 2^40 (near-flat
+// slivers, whose rounded weights can pass far outside the triangle), or a box
+// over more than 4096 tiles.  For the rest the box, enlarged by
+// max(1e-6, kappa 2^-45) of its width + height, keeps every pixel whose FP64
+// test can pass: a false hit at distance D needs D < 2^-48 kappa (D + L), L
+// the triangle's size (u = 2^-53), so under 4e-9 L at kappa <= 2^20 and a
+// factor 8 inside the margin up to kappa = 2^40.  A denominator of exactly 0
+// never passes.  Tile lists are sorted, so a pixel stops at its first hit,
+// and a weight whose numerator is already negative rejects a triangle before
+// the FP64 divisions.
 #include "gcvt_internal.cuh"
 #include "../../include/gcvt_gb300.h"
 
@@ -31,46 +35,71 @@
 namespace cvtgb {
 
 constexpr int kTile = 16;
-constexpr double kMaxCond = 1048576.0;  // 2^20
+constexpr double kMaxCond = 1099511627776.0;  // 2^40
 constexpr int kMaxTilesPerTri = 4096;
 
+// A triangle with the point-independent terms of barycentric_coordinate
+// (discretization.cu:32-55) precomputed as the kernel would compute them.
 struct TriData {
-  double x1, y1, x2, y2, x3, y3;  // vertex coordinates, copied from points[]
-  int p1, p2, p3;                 // vertex indices (for the weights)
-  int global;                     // 1: on the global list
+  double x1, y1, v0x, v0y, v1x, v1y, d00, d01, d11, denom;
+  int p1, p2, p3;  // vertex indices (for the weights)
+  int global;      // 1: on the global list
 };
 
-// The point-independent terms of the test, as bary_inside computes them.
-__device__ __forceinline__ void tri_terms(const TriData &t, double &d00, double &d01,
-                                          double &d11, double &denom) {
-  const double v0x = __dsub_rn(t.x2, t.x1), v0y = __dsub_rn(t.y2, t.y1);
-  const double v1x = __dsub_rn(t.x3, t.x1), v1y = __dsub_rn(t.y3, t.y1);
-  d00 = __fma_rn(v0x, v0x, __dmul_rn(v0y, v0y));
-  d01 = __fma_rn(v0x, v1x, __dmul_rn(v0y, v1y));
-  d11 = __fma_rn(v1x, v1x, __dmul_rn(v1y, v1y));
-  denom = __fma_rn(d00, d11, -__dmul_rn(d01, d01));
+__device__ __forceinline__ void tri_terms(double x1, double y1, double x2, double y2, double x3,
+                                          double y3, TriData &t) {
+  t.x1 = x1;
+  t.y1 = y1;
+  t.v0x = __dsub_rn(x2, x1);
+  t.v0y = __dsub_rn(y2, y1);
+  t.v1x = __dsub_rn(x3, x1);
+  t.v1y = __dsub_rn(y3, y1);
+  t.d00 = __fma_rn(t.v0x, t.v0x, __dmul_rn(t.v0y, t.v0y));
+  t.d01 = __fma_rn(t.v0x, t.v1x, __dmul_rn(t.v0y, t.v1y));
+  t.d11 = __fma_rn(t.v1x, t.v1x, __dmul_rn(t.v1y, t.v1y));
+  t.denom = __fma_rn(t.d00, t.d11, -__dmul_rn(t.d01, t.d01));
 }
 
-// barycentric_coordinate (discretization.cu:32-55) with the reference's
-// operation order; returns the caller's (w1, w2, w3) after the reference's
-// output-argument permutation.
+// barycentric_coordinate with the reference's operation order and the fused
+// multiply-adds nvcc forms in it; returns the caller's (w1, w2, w3) after the
+// reference's output-argument permutation.
 __device__ __forceinline__ bool bary_inside(const TriData &t, double x0, double y0, double &w1,
                                             double &w2, double &w3) {
-  const double v0x = __dsub_rn(t.x2, t.x1), v0y = __dsub_rn(t.y2, t.y1);
-  const double v1x = __dsub_rn(t.x3, t.x1), v1y = __dsub_rn(t.y3, t.y1);
   const double v2x = __dsub_rn(x0, t.x1), v2y = __dsub_rn(y0, t.y1);
-  const double d00 = __fma_rn(v0x, v0x, __dmul_rn(v0y, v0y));
-  const double d01 = __fma_rn(v0x, v1x, __dmul_rn(v0y, v1y));
-  const double d11 = __fma_rn(v1x, v1x, __dmul_rn(v1y, v1y));
-  const double d20 = __fma_rn(v2x, v0x, __dmul_rn(v2y, v0y));
-  const double d21 = __fma_rn(v2x, v1x, __dmul_rn(v2y, v1y));
-  const double denom = __fma_rn(d00, d11, -__dmul_rn(d01, d01));
-  if (denom == 0) return false;  // all weights -1 in the reference
-  const double a = __ddiv_rn(__fma_rn(d11, d20, -__dmul_rn(d01, d21)), denom);
-  const double b = __ddiv_rn(__fma_rn(d00, d21, -__dmul_rn(d01, d20)), denom);
-  w2 = a;                               // the reference's w1 argument slot
-  w3 = b;                               // w2 slot
-  w1 = __dsub_rn(__dsub_rn(1.0, a), b); // w3 slot: 1 - w1 - w2
+  const double d20 = __fma_rn(v2x, t.v0x, __dmul_rn(v2y, t.v0y));
+  const double d21 = __fma_rn(v2x, t.v1x, __dmul_rn(v2y, t.v1y));
+  if (t.denom == 0) return false;  // all weights -1 in the reference
+  const double a = __ddiv_rn(__fma_rn(t.d11, d20, -__dmul_rn(t.d01, d21)), t.denom);
+  const double b = __ddiv_rn(__fma_rn(t.d00, d21, -__dmul_rn(t.d01, d20)), t.denom);
+  w2 = a;                                // the reference's w1 argument slot
+  w3 = b;                                // w2 slot
+  w1 = __dsub_rn(__dsub_rn(1.0, a), b);  // w3 slot: 1 - w1 - w2
+  return !(w1 < 0 || w2 < 0 || w3 < 0);
+}
+
+// RN(num / denom) < 0 for denom > 0, decided without dividing (false: divide
+// to know): num < 0 and the quotient too large to round to -0.
+__device__ __forceinline__ bool quot_negative(double num, double denom) {
+  return num < 0 && (denom <= 1.0 || -num >= __dmul_rn(denom, 0x1p-1000));
+}
+
+// bary_inside for a finite triangle with denom > 0: same results, but a
+// weight whose numerator already shows it negative rejects the triangle
+// before the divisions (FP64 issue is scarce on GB300).
+__device__ __forceinline__ bool bary_inside_local(const TriData &t, double x0, double y0,
+                                                  double &w1, double &w2, double &w3) {
+  const double v2x = __dsub_rn(x0, t.x1), v2y = __dsub_rn(y0, t.y1);
+  const double d20 = __fma_rn(v2x, t.v0x, __dmul_rn(v2y, t.v0y));
+  const double d21 = __fma_rn(v2x, t.v1x, __dmul_rn(v2y, t.v1y));
+  const double na = __fma_rn(t.d11, d20, -__dmul_rn(t.d01, d21));
+  if (quot_negative(na, t.denom)) return false;
+  const double nb = __fma_rn(t.d00, d21, -__dmul_rn(t.d01, d20));
+  if (quot_negative(nb, t.denom)) return false;
+  const double a = __ddiv_rn(na, t.denom);
+  const double b = __ddiv_rn(nb, t.denom);
+  w2 = a;
+  w3 = b;
+  w1 = __dsub_rn(__dsub_rn(1.0, a), b);
   return !(w1 < 0 || w2 < 0 || w3 < 0);
 }
 
@@ -84,35 +113,31 @@ __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restric
   t.p1 = tri[3 * i];
   t.p2 = tri[3 * i + 1];
   t.p3 = tri[3 * i + 2];
+  t.global = 0;
   if (t.p1 < 0 || t.p2 < 0 || t.p3 < 0 || t.p1 >= num_point || t.p2 >= num_point ||
       t.p3 >= num_point) {
     atomicOr(err, 1);
     t.p1 = t.p2 = t.p3 = 0;
-    t.x1 = t.y1 = t.x2 = t.y2 = t.x3 = t.y3 = 0.0;  // denominator 0: never passes
-    t.global = 0;
+    tri_terms(0, 0, 0, 0, 0, 0, t);  // denominator 0: never passes
     td[i] = t;
     tbox[i] = make_int4(1, 1, 0, 0);
     return;
   }
-  t.x1 = pts[2 * t.p1];
-  t.y1 = pts[2 * t.p1 + 1];
-  t.x2 = pts[2 * t.p2];
-  t.y2 = pts[2 * t.p2 + 1];
-  t.x3 = pts[2 * t.p3];
-  t.y3 = pts[2 * t.p3 + 1];
-  t.global = 0;
-  double d00, d01, d11, denom;
-  tri_terms(t, d00, d01, d11, denom);
-  const double xmin = fmin(t.x1, fmin(t.x2, t.x3)), xmax = fmax(t.x1, fmax(t.x2, t.x3));
-  const double ymin = fmin(t.y1, fmin(t.y2, t.y3)), ymax = fmax(t.y1, fmax(t.y2, t.y3));
-  const bool finite = isfinite(t.x1) && isfinite(t.y1) && isfinite(t.x2) && isfinite(t.y2) &&
-                      isfinite(t.x3) && isfinite(t.y3) && isfinite(denom);
-  if (denom == 0) {  // never passes
+  const double x1 = pts[2 * t.p1], y1 = pts[2 * t.p1 + 1];
+  const double x2 = pts[2 * t.p2], y2 = pts[2 * t.p2 + 1];
+  const double x3 = pts[2 * t.p3], y3 = pts[2 * t.p3 + 1];
+  tri_terms(x1, y1, x2, y2, x3, y3, t);
+  const double xmin = fmin(x1, fmin(x2, x3)), xmax = fmax(x1, fmax(x2, x3));
+  const double ymin = fmin(y1, fmin(y2, y3)), ymax = fmax(y1, fmax(y2, y3));
+  const bool finite = isfinite(x1) && isfinite(y1) && isfinite(x2) && isfinite(y2) &&
+                      isfinite(x3) && isfinite(y3) && isfinite(t.denom);
+  if (t.denom == 0) {  // never passes
     td[i] = t;
     tbox[i] = make_int4(1, 1, 0, 0);
     return;
   }
-  if (!finite || !(denom > 0) || !(d00 * d11 / denom <= kMaxCond)) {
+  const double cond = t.d00 * t.d11 / t.denom;
+  if (!finite || !(t.denom > 0) || !(cond <= kMaxCond)) {
     t.global = 1;
     td[i] = t;
     tbox[i] = make_int4(0, 0, n - 1, n - 1);
@@ -120,24 +145,25 @@ __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restric
     return;
   }
   // pixel box: pixels whose sample point lies in the triangle's box enlarged
-  // by 1e-6 of its width + height plus a pixel fraction
-  const double m = ((xmax - xmin) + (ymax - ymin)) * 1e-6 + 1e-9 / inv_scale;
+  // by max(1e-6, kappa 2^-45) of its width + height plus a pixel fraction
+  const double m =
+      fmax(1e-6, cond * 0x1p-45) * ((xmax - xmin) + (ymax - ymin)) + 1e-9 / inv_scale;
   int x0 = (int)fmax(-1.0, ceil((xmin - m) * inv_scale));
-  int x1 = (int)fmin((double)n, floor((xmax + m) * inv_scale));
+  int x1p = (int)fmin((double)n, floor((xmax + m) * inv_scale));
   int y0 = (int)fmax(-1.0, ceil((ymin - m) * inv_scale));
-  int y1 = (int)fmin((double)n, floor((ymax + m) * inv_scale));
+  int y1p = (int)fmin((double)n, floor((ymax + m) * inv_scale));
   x0 = max(x0, 0);
   y0 = max(y0, 0);
-  x1 = min(x1, n - 1);
-  y1 = min(y1, n - 1);
-  if (x0 > x1 || y0 > y1) {
+  x1p = min(x1p, n - 1);
+  y1p = min(y1p, n - 1);
+  if (x0 > x1p || y0 > y1p) {
     td[i] = t;
     tbox[i] = make_int4(1, 1, 0, 0);  // empty
     return;
   }
-  tbox[i] = make_int4(x0, y0, x1, y1);
-  const long long tiles =
-      (long long)(x1 / kTile - x0 / kTile + 1) * (long long)(y1 / kTile - y0 / kTile + 1);
+  tbox[i] = make_int4(x0, y0, x1p, y1p);
+  const long long tiles = (long long)(x1p / kTile - x0 / kTile + 1) *
+                          (long long)(y1p / kTile - y0 / kTile + 1);
   if (tiles > kMaxTilesPerTri) {
     t.global = 1;
     td[i] = t;
@@ -146,8 +172,8 @@ __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restric
   }
   td[i] = t;
   const int nt = n / kTile;
-  for (int ty = y0 / kTile; ty <= y1 / kTile; ++ty)
-    for (int tx = x0 / kTile; tx <= x1 / kTile; ++tx) atomicAdd(&tile_count[ty * nt + tx], 1);
+  for (int ty = y0 / kTile; ty <= y1p / kTile; ++ty)
+    for (int tx = x0 / kTile; tx <= x1p / kTile; ++tx) atomicAdd(&tile_count[ty * nt + tx], 1);
 }
 
 // Exclusive scan of the tile counts, one block (tiles <= 1024 * 64).
@@ -196,7 +222,24 @@ __global__ void k_tri_scatter(const TriData *__restrict__ td, const int4 *__rest
     }
 }
 
-// One block per tile, one thread per pixel.
+// Each tile's list in ascending triangle order (one thread per tile).
+__global__ void k_tile_sort(const int *__restrict__ offset, int ntiles, int *list) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ntiles) return;
+  const int l0 = offset[c], l1 = offset[c + 1];
+  for (int k = l0 + 1; k < l1; ++k) {
+    const int x = list[k];
+    int j = k - 1;
+    while (j >= l0 && list[j] > x) {
+      list[j + 1] = list[j];
+      --j;
+    }
+    list[j + 1] = x;
+  }
+}
+
+// One block per tile, one thread per pixel; the tile's list is sorted, so the
+// first triangle that passes is the answer.
 __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restrict__ td,
                                                         const int4 *__restrict__ tbox,
                                                         const int *__restrict__ offset,
@@ -215,15 +258,15 @@ __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restri
   double bw1 = 0, bw2 = 0, bw3 = 0;
   for (int k = l0; k < l1; ++k) {
     const int i = list[k];
-    if (i >= best) continue;
     const int4 b = __ldg(&tbox[i]);
     if (tx < b.x || tx > b.z || ty < b.y || ty > b.w) continue;
     double w1, w2, w3;
-    if (bary_inside(td[i], x, y, w1, w2, w3)) {
+    if (bary_inside_local(td[i], x, y, w1, w2, w3)) {
       best = i;
       bw1 = w1;
       bw2 = w2;
       bw3 = w3;
+      break;
     }
   }
   const int ng = *gcount;
@@ -258,7 +301,7 @@ using namespace cvtgb;
 namespace {
 #define RCK(call)                                  \
   do {                                             \
-    if ((call) != cudaSuccess) { rc = GCVT_ERR_CUDA; goto done; } \
+    if ((call) != cudaSuccess) return GCVT_ERR_CUDA; \
   } while (0)
 }  // namespace
 
@@ -269,80 +312,58 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
   if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;
   if (num_point < 0 || num_tri < 0 || !(scale > 0)) return GCVT_ERR_ARGUMENT;
   if (n < kTile || n % kTile != 0 || n > 16384) return GCVT_ERR_SIZE;
-  int rc = GCVT_OK;
   const int nt = n / kTile, ntiles = nt * nt;
-  double *d_pts = nullptr, *d_w = nullptr;
-  int *d_tri = nullptr, *d_cnt = nullptr, *d_off = nullptr, *d_cur = nullptr, *d_list = nullptr;
-  int *d_glist = nullptr, *d_scal = nullptr;  // global list; [0] its length, [1] error flag
-  int herr = 0;
-  TriData *d_td = nullptr;
-  int4 *d_box = nullptr;
-  float *d_dens = nullptr;
-  int total = 0;
-  const cudaMemcpyKind h2d = mem == GCVT_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   if (ntiles > 1024 * 65536) return GCVT_ERR_SIZE;
+  Scratch sc;
+  const double *P = points, *Wt = weight;
+  const int *Tr = triangle;
+  float *D = density;
   if (mem == GCVT_MEM_HOST) {
-    RCK(cudaMalloc((void **)&d_pts, (size_t)num_point * 2 * sizeof(double) + 16));
-    RCK(cudaMalloc((void **)&d_w, (size_t)num_point * sizeof(double) + 16));
-    RCK(cudaMalloc((void **)&d_tri, (size_t)num_tri * 3 * sizeof(int) + 16));
-    RCK(cudaMalloc((void **)&d_dens, (size_t)n * n * sizeof(float)));
-    RCK(cudaMemcpy(d_pts, points, (size_t)num_point * 2 * sizeof(double), h2d));
-    RCK(cudaMemcpy(d_w, weight, (size_t)num_point * sizeof(double), h2d));
-    RCK(cudaMemcpy(d_tri, triangle, (size_t)num_tri * 3 * sizeof(int), h2d));
+    double *d_pts = sc.take<double>((size_t)num_point * 2), *d_w = sc.take<double>(num_point);
+    int *d_tri = sc.take<int>((size_t)num_tri * 3);
+    D = sc.take<float>((size_t)n * n);
+    if (!d_pts || !d_w || !d_tri || !D) return GCVT_ERR_ALLOC;
+    RCK(cudaMemcpy(d_pts, points, (size_t)num_point * 2 * sizeof(double), cudaMemcpyHostToDevice));
+    RCK(cudaMemcpy(d_w, weight, (size_t)num_point * sizeof(double), cudaMemcpyHostToDevice));
+    RCK(cudaMemcpy(d_tri, triangle, (size_t)num_tri * 3 * sizeof(int), cudaMemcpyHostToDevice));
+    P = d_pts;
+    Wt = d_w;
+    Tr = d_tri;
   }
-  {
-    const double *P = mem == GCVT_MEM_HOST ? d_pts : points;
-    const double *Wt = mem == GCVT_MEM_HOST ? d_w : weight;
-    const int *Tr = mem == GCVT_MEM_HOST ? d_tri : triangle;
-    float *D = mem == GCVT_MEM_HOST ? d_dens : density;
-    RCK(cudaMalloc((void **)&d_td, (size_t)num_tri * sizeof(TriData) + 16));
-    RCK(cudaMalloc((void **)&d_box, (size_t)num_tri * sizeof(int4) + 16));
-    RCK(cudaMalloc((void **)&d_cnt, (size_t)ntiles * sizeof(int)));
-    RCK(cudaMalloc((void **)&d_off, (size_t)(ntiles + 1) * sizeof(int)));
-    RCK(cudaMalloc((void **)&d_cur, (size_t)ntiles * sizeof(int)));
-    RCK(cudaMalloc((void **)&d_glist, (size_t)num_tri * sizeof(int) + 16));
-    RCK(cudaMalloc((void **)&d_scal, 2 * sizeof(int)));
-    RCK(cudaMemset(d_scal, 0, 2 * sizeof(int)));
-    RCK(cudaMemset(d_cnt, 0, (size_t)ntiles * sizeof(int)));
-    if (num_tri > 0) {
-      k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_box,
-                                                  d_cnt, d_glist, d_scal, num_point, d_scal + 1);
-      RCK(cudaGetLastError());
-    }
-    k_tile_scan<<<1, 1024>>>(d_cnt, ntiles, d_off, d_cur);
+  TriData *d_td = sc.take<TriData>(num_tri);
+  int4 *d_box = sc.take<int4>(num_tri);
+  int *d_cnt = sc.take<int>(ntiles), *d_off = sc.take<int>(ntiles + 1);
+  int *d_cur = sc.take<int>(ntiles), *d_glist = sc.take<int>(num_tri);
+  int *d_scal = sc.take<int>(2);  // global list length, error flag
+  if (!d_td || !d_box || !d_cnt || !d_off || !d_cur || !d_glist || !d_scal) return GCVT_ERR_ALLOC;
+  RCK(cudaMemset(d_scal, 0, 2 * sizeof(int)));
+  RCK(cudaMemset(d_cnt, 0, (size_t)ntiles * sizeof(int)));
+  if (num_tri > 0) {
+    k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_box,
+                                                d_cnt, d_glist, d_scal, num_point, d_scal + 1);
     RCK(cudaGetLastError());
-    RCK(cudaMemcpy(&total, d_off + ntiles, sizeof(int), cudaMemcpyDeviceToHost));
-    RCK(cudaMalloc((void **)&d_list, (size_t)total * sizeof(int) + 16));
-    if (num_tri > 0) {
-      k_tri_scatter<<<(num_tri + 255) / 256, 256>>>(d_td, d_box, num_tri, n, d_cur, d_list);
-      RCK(cudaGetLastError());
-    }
-    k_raster<<<ntiles, kTile * kTile>>>(d_td, d_box, d_off, d_list, d_glist, d_scal, Wt, scale,
-                                        n, D);
-    RCK(cudaGetLastError());
-    RCK(cudaMemcpy(&herr, d_scal + 1, sizeof(int), cudaMemcpyDeviceToHost));
-    if (herr) {
-      rc = GCVT_ERR_ARGUMENT;
-      goto done;
-    }
-    if (mem == GCVT_MEM_HOST)
-      RCK(cudaMemcpy(density, d_dens, (size_t)n * n * sizeof(float), cudaMemcpyDeviceToHost));
-    RCK(cudaDeviceSynchronize());
   }
-done:
-  cudaFree(d_pts);
-  cudaFree(d_w);
-  cudaFree(d_tri);
-  cudaFree(d_dens);
-  cudaFree(d_td);
-  cudaFree(d_box);
-  cudaFree(d_cnt);
-  cudaFree(d_off);
-  cudaFree(d_cur);
-  cudaFree(d_list);
-  cudaFree(d_glist);
-  cudaFree(d_scal);
-  return rc;
+  k_tile_scan<<<1, 1024>>>(d_cnt, ntiles, d_off, d_cur);
+  RCK(cudaGetLastError());
+  int total = 0;
+  RCK(cudaMemcpy(&total, d_off + ntiles, sizeof(int), cudaMemcpyDeviceToHost));
+  int *d_list = sc.take<int>(total);
+  if (!d_list) return GCVT_ERR_ALLOC;
+  if (num_tri > 0) {
+    k_tri_scatter<<<(num_tri + 255) / 256, 256>>>(d_td, d_box, num_tri, n, d_cur, d_list);
+    RCK(cudaGetLastError());
+    k_tile_sort<<<(ntiles + 255) / 256, 256>>>(d_off, ntiles, d_list);
+    RCK(cudaGetLastError());
+  }
+  k_raster<<<ntiles, kTile * kTile>>>(d_td, d_box, d_off, d_list, d_glist, d_scal, Wt, scale, n,
+                                      D);
+  RCK(cudaGetLastError());
+  int herr = 0;
+  RCK(cudaMemcpy(&herr, d_scal + 1, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return GCVT_ERR_ARGUMENT;
+  if (mem == GCVT_MEM_HOST)
+    RCK(cudaMemcpy(density, D, (size_t)n * n * sizeof(float), cudaMemcpyDeviceToHost));
+  return GCVT_OK;
 }
 
 // The reference's entry point (discretization.h:66, discretization.cu:87):

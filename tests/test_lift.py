@@ -166,3 +166,33 @@ def test_gpu_lift_device_memory_and_errors(gcvt_lib):
         gcvt_lib.vertex_weights(uv, xyz, bad)
     empty, eface, ekeep = gcvt_lib.lift(uv, xyz, tris, np.zeros((0, 2)))
     assert empty.shape == (0, 3) and ekeep.shape == (0,)
+
+
+@pytest.mark.gpu
+def test_gpu_lift_slivers_equal_oracle(gcvt_lib, oracle):
+    """Flat triangles from conditioning 1e2 to 1e20 (binned with widened boxes,
+    or tested by every point), queried on and around them."""
+    rng = np.random.default_rng(21)
+    uv, tris = [], []
+    for k, h in enumerate(10.0 ** -np.arange(1, 11)):
+        y0 = 0.05 + 0.09 * k
+        base = len(uv)
+        a, b = np.array([0.1, y0]), np.array([0.9, y0 + 1e-3 * k])
+        c = a + (0.5 + 0.01 * k) * (b - a) + np.array([0.0, h])   # h above the long edge
+        uv += [a.tolist(), b.tolist(), c.tolist()]
+        tris.append([base, base + 1, base + 2])
+        tris.append([base + 1, base, base + 2])   # the same sliver, other orientation
+    uv = np.array(uv)
+    xyz = np.concatenate([uv, rng.normal(0, 1, (len(uv), 1))], 1)
+    tris = np.array(tris, np.int32)
+    near = []
+    for t in tris[::2]:
+        a, b, c = uv[t]
+        s = rng.random((300, 2))
+        near.append(a + s[:, :1] * (b - a) + s[:, 1:] * (c - a) * rng.uniform(-2, 3, (300, 1)))
+        near.append(a + rng.random((100, 1)) * (b - a))          # on the long edge
+    pts = np.concatenate(near + [rng.uniform(0, 1, (500, 2))])
+    want, wface, _ = oracle.lift(uv, xyz, tris, pts)
+    got, face, _ = gcvt_lib.lift(uv, xyz, tris, pts)
+    assert np.array_equal(face, wface)
+    assert same_f64(got, want)

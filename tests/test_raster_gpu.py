@@ -80,3 +80,32 @@ def test_raster_triangles_the_boxes_cannot_place(gcvt_lib, cuda_device):
     bad[1, 2] = len(pts)
     with pytest.raises(RuntimeError):
         gcvt_lib.rasterize(pts, w, bad, 1.0, n)
+
+
+def test_raster_slivers_across_conditioning(gcvt_lib, cuda_device):
+    """Flat triangles whose height goes from 1e-1 to 1e-10 pixels (conditioning
+    up to about 1e26), both orientations, over a regular background mesh."""
+    n = 256
+    rng = np.random.default_rng(12)
+    pts, tris = [], []
+    for k, h in enumerate(10.0 ** -np.arange(1, 11)):
+        y0 = 10.0 + 23.0 * k
+        b = len(pts)
+        a, c = np.array([5.0, y0]), np.array([250.0, y0 + 0.37 * k])
+        m = a + (0.45 + 0.01 * k) * (c - a) + np.array([0.0, h])   # h above the long edge
+        pts += [a.tolist(), c.tolist(), m.tolist()]
+        tris += [[b, b + 1, b + 2], [b + 1, b, b + 2]]
+    b = len(pts)
+    g = np.linspace(0, 255, 9)
+    X, Y = np.meshgrid(g, g)
+    pts += np.stack([X.ravel(), Y.ravel()], 1).tolist()
+    for r in range(8):
+        for c in range(8):
+            a = b + r * 9 + c
+            tris += [[a, a + 1, a + 10], [a, a + 10, a + 9]]
+    pts = np.array(pts, np.float64)
+    tris = np.array(tris, np.int32)
+    w = rng.uniform(0.5, 2.0, len(pts))
+    got = gcvt_lib.rasterize(pts, w, tris, 1.0, n)
+    want = orc.rasterize(pts, w, tris, 1.0, n)
+    assert _same_f32(got, want)
