@@ -103,12 +103,64 @@ __device__ __forceinline__ bool bary_inside_local(const TriData &t, double x0, d
   return !(w1 < 0 || w2 < 0 || w3 < 0);
 }
 
+// An FP32 pre-test that rejects a pixel clearly outside a triangle before the
+// FP64 test, for triangles with conditioning <= 2^20 (sgn = 0: no pre-test).
+// In pixel units, r = q - P1, edge functions E0 = v0 x r, E1 = (v1 - v0) x
+// (r - v0), E2 = (-v1) x (r - v1), all >= 0 inside a counter-clockwise
+// triangle (sgn folds the orientation).  With M the largest coordinate
+// magnitude, L the longest edge and |r| <= 3 L inside the triangle's box, the
+// FP32 error of each E_k is below L (2^-22 M + 2^-19 L) (rounded coordinates
+// and edge vectors, three roundings in the products); so sgn E_k < -t with
+// t = L (2^-21 M + 2^-16 L) means E_k < -2^-17 L^2 exactly: the pixel lies
+// more than 2^-17 L outside edge k, far beyond the FP64 test's own error
+// there (2^-48 kappa (|r| + L) <= 2^-26 L), so the FP64 weight of the
+// opposite vertex is negative and the reference's test fails too.
+struct TriPre {
+  float p1x, p1y, v0x, v0y, v1x, v1y, t, sgn;
+};
+
+__device__ __forceinline__ bool pre_outside(const TriPre &q, int tx, int ty) {
+  if (q.sgn == 0.f) return false;
+  const float rx = (float)tx - q.p1x, ry = (float)ty - q.p1y;
+  const float e0 = q.v0x * ry - q.v0y * rx;
+  const float e1 = (q.v1x - q.v0x) * (ry - q.v0y) - (q.v1y - q.v0y) * (rx - q.v0x);
+  const float e2 = q.v1y * (rx - q.v1x) - q.v1x * (ry - q.v1y);
+  return q.sgn * e0 < -q.t || q.sgn * e1 < -q.t || q.sgn * e2 < -q.t;
+}
+
+__device__ __forceinline__ TriPre make_pre(const TriData &t, double inv_scale, int n,
+                                           double cond) {
+  TriPre q{0, 0, 0, 0, 0, 0, 0, 0};
+  if (!(cond <= 1048576.0)) return q;
+  const double cr = t.v0x * t.v1y - t.v0y * t.v1x;
+  if (!(cr != 0.0) || !isfinite(cr)) return q;
+  const double p1x = t.x1 * inv_scale, p1y = t.y1 * inv_scale;
+  const double ax = t.v0x * inv_scale, ay = t.v0y * inv_scale;
+  const double bx = t.v1x * inv_scale, by = t.v1y * inv_scale;
+  const double l0 = sqrt(ax * ax + ay * ay), l2 = sqrt(bx * bx + by * by);
+  const double l1 = sqrt((bx - ax) * (bx - ax) + (by - ay) * (by - ay));
+  const double L = fmax(l0, fmax(l1, l2));
+  const double M = fmax((double)n, fmax(fabs(p1x), fabs(p1y)) + 4.0 * L);
+  if (!(L >= 1e-9 && M <= 1e9)) return q;  // keep FP32 away from over/underflow
+  const double thr = L * (0x1p-21 * M + 0x1p-16 * L) * 1.0625;
+  q.p1x = (float)p1x;
+  q.p1y = (float)p1y;
+  q.v0x = (float)ax;
+  q.v0y = (float)ay;
+  q.v1x = (float)bx;
+  q.v1y = (float)by;
+  q.t = (float)thr;
+  q.sgn = cr > 0 ? 1.f : -1.f;
+  return q;
+}
+
 __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restrict__ tri, int T,
-                            double inv_scale, int n, TriData *td, int4 *tbox,
+                            double inv_scale, int n, TriData *td, TriPre *tpre, int4 *tbox,
                             int *tile_count, int *glist, int *gcount, int num_point,
                             int *err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= T) return;
+  tpre[i] = TriPre{0, 0, 0, 0, 0, 0, 0, 0};
   TriData t;
   t.p1 = tri[3 * i];
   t.p2 = tri[3 * i + 1];
@@ -171,6 +223,7 @@ __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restric
     return;
   }
   td[i] = t;
+  tpre[i] = make_pre(t, inv_scale, n, cond);
   const int nt = n / kTile;
   for (int ty = y0 / kTile; ty <= y1p / kTile; ++ty)
     for (int tx = x0 / kTile; tx <= x1p / kTile; ++tx) atomicAdd(&tile_count[ty * nt + tx], 1);
@@ -241,6 +294,7 @@ __global__ void k_tile_sort(const int *__restrict__ offset, int ntiles, int *lis
 // One block per tile, one thread per pixel; the tile's list is sorted, so the
 // first triangle that passes is the answer.
 __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restrict__ td,
+                                                        const TriPre *__restrict__ tpre,
                                                         const int4 *__restrict__ tbox,
                                                         const int *__restrict__ offset,
                                                         const int *__restrict__ list,
@@ -260,6 +314,7 @@ __global__ void __launch_bounds__(kTile *kTile) k_raster(const TriData *__restri
     const int i = list[k];
     const int4 b = __ldg(&tbox[i]);
     if (tx < b.x || tx > b.z || ty < b.y || ty > b.w) continue;
+    if (pre_outside(tpre[i], tx, ty)) continue;
     double w1, w2, w3;
     if (bary_inside_local(td[i], x, y, w1, w2, w3)) {
       best = i;
@@ -331,15 +386,16 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
     Tr = d_tri;
   }
   TriData *d_td = sc.take<TriData>(num_tri);
+  TriPre *d_pre = sc.take<TriPre>(num_tri);
   int4 *d_box = sc.take<int4>(num_tri);
   int *d_cnt = sc.take<int>(ntiles), *d_off = sc.take<int>(ntiles + 1);
   int *d_cur = sc.take<int>(ntiles), *d_glist = sc.take<int>(num_tri);
   int *d_scal = sc.take<int>(2);  // global list length, error flag
-  if (!d_td || !d_box || !d_cnt || !d_off || !d_cur || !d_glist || !d_scal) return GCVT_ERR_ALLOC;
+  if (!d_td || !d_pre || !d_box || !d_cnt || !d_off || !d_cur || !d_glist || !d_scal) return GCVT_ERR_ALLOC;
   RCK(cudaMemset(d_scal, 0, 2 * sizeof(int)));
   RCK(cudaMemset(d_cnt, 0, (size_t)ntiles * sizeof(int)));
   if (num_tri > 0) {
-    k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_box,
+    k_tri_setup<<<(num_tri + 255) / 256, 256>>>(P, Tr, num_tri, 1.0 / scale, n, d_td, d_pre, d_box,
                                                 d_cnt, d_glist, d_scal, num_point, d_scal + 1);
     RCK(cudaGetLastError());
   }
@@ -355,7 +411,7 @@ extern "C" int gcvt_rasterize(const double *points, const double *weight, int nu
     k_tile_sort<<<(ntiles + 255) / 256, 256>>>(d_off, ntiles, d_list);
     RCK(cudaGetLastError());
   }
-  k_raster<<<ntiles, kTile * kTile>>>(d_td, d_box, d_off, d_list, d_glist, d_scal, Wt, scale, n,
+  k_raster<<<ntiles, kTile * kTile>>>(d_td, d_pre, d_box, d_off, d_list, d_glist, d_scal, Wt, scale, n,
                                       D);
   RCK(cudaGetLastError());
   int herr = 0;
