@@ -200,10 +200,11 @@ __global__ void k_tri_setup(const double *__restrict__ pts, const int *__restric
   // by max(1e-6, kappa 2^-45) of its width + height plus a pixel fraction
   const double m =
       fmax(1e-6, cond * 0x1p-45) * ((xmax - xmin) + (ymax - ymin)) + 1e-9 / inv_scale;
-  int x0 = (int)fmax(-1.0, ceil((xmin - m) * inv_scale));
-  int x1p = (int)fmin((double)n, floor((xmax + m) * inv_scale));
-  int y0 = (int)fmax(-1.0, ceil((ymin - m) * inv_scale));
-  int y1p = (int)fmin((double)n, floor((ymax + m) * inv_scale));
+  // (clamped to [-1, n] before the conversion to int)
+  int x0 = (int)fmin((double)n, fmax(-1.0, ceil((xmin - m) * inv_scale)));
+  int x1p = (int)fmin((double)n, fmax(-1.0, floor((xmax + m) * inv_scale)));
+  int y0 = (int)fmin((double)n, fmax(-1.0, ceil((ymin - m) * inv_scale)));
+  int y1p = (int)fmin((double)n, fmax(-1.0, floor((ymax + m) * inv_scale)));
   x0 = max(x0, 0);
   y0 = max(y0, 0);
   x1p = min(x1p, n - 1);
