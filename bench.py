@@ -27,6 +27,10 @@ Metric: Gpix-pass/s = n^2 x labelling passes / second, 101 passes per step
 oracle's OpenMP restatement of gcvt.cu, all threads) on a bounded sample of
 the same workload, in the same unit.
 Multi-GPU: independent replicas, one per rank (weak scaling).
+Other workloads, each with its own JSON line: --config plain_8192 (8192^2,
+64 Gaussians, 1,048,576 sites, 100 iterations; the same contract),
+--config batched_64 (64 charts of 256^2-2048^2 iterated together),
+--config mesh_2048 (a mesh rasterised to 2048^2, then Lloyd, then the lift).
 """
 import argparse
 import json
@@ -45,10 +49,18 @@ for _p in (os.path.join(PKG, "python"), PKG):
 import numpy as np  # noqa: E402
 
 CONFIG = "plain_4096"
+PLAIN = ("plain_4096", "plain_8192")  # the plain Lloyd workloads bench.py runs
 SEED = 1
 ITERS = 100
 PASSES = ITERS + 1
 METRIC = "Gpix-pass/s, plain Lloyd CVT (gCVT loop), 4096^2 grid, 262,144 sites, 100 iterations"
+
+
+def metric_of(workload, n, nsites):
+    if workload == CONFIG:
+        return METRIC
+    return "Gpix-pass/s, plain Lloyd CVT (gCVT loop), %d^2 grid, %s sites, 100 iterations" % (
+        n, format(nsites, ","))
 UNIT = "Gpix-pass/s"
 # Algorithmic bytes of one Lloyd iteration (k_list + k_cell<0>): the density
 # once over its row support (4 B per support pixel: every such pixel belongs
@@ -64,6 +76,10 @@ ALG_BYTES_PER_SITE = 24.0
 # from the ncu capture summarised in profiles/cell_kernel_plain_4096.md:
 # k_list 1,493,248 + 693,248, k_cell 33,864,960 + 18,889,984 bytes.
 NCU_TRAFFIC_BYTES = 54941440
+# the same capture on the 8192^2 / 1,048,576-site workload (iteration 31,
+# profiles/cell_kernel_plain_8192.md): k_list 13,138,176 + 3,403,520, k_cell
+# 265,760,256 + 77,200,896 bytes
+NCU_TRAFFIC = {"plain_4096": NCU_TRAFFIC_BYTES, "plain_8192": 359502848}
 
 
 def support_pixels(rho):
@@ -209,7 +225,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline_sample(sites, rho, mask, target_s=10.0):
+def cpu_baseline_sample(sites, rho, mask, target_s=10.0, workload=CONFIG):
     """The oracle's OpenMP restatement of the reference's Lloyd loop (faithful
     FP32 mode, all host threads) on a bounded sample: as many iterations of
     the 4096^2 workload as fit in about target_s seconds."""
@@ -226,8 +242,8 @@ def cpu_baseline_sample(sites, rho, mask, target_s=10.0):
     # k iterations + the final labelling pass
     value = n * n * (k + 1) / dt / 1e9
     return {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d Lloyd iterations + final labelling of the 4096^2 / 262,144-site "
-                      "workload, faithful FP32 restatement of gcvt.cu, %.1f s" % (k, dt)}
+            "sample": "%d Lloyd iterations + final labelling of the %s workload, faithful FP32 "
+                      "restatement of gcvt.cu, %.1f s" % (k, workload, dt)}
 
 
 def run_reference(args):
@@ -237,7 +253,8 @@ def run_reference(args):
     from workloads import config_inputs
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
-    sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    workload = args.config if args.config in PLAIN else CONFIG
+    sites, rho, mask, _ = config_inputs(workload, seed=SEED)
     n = sites.shape[0]
     iters_per_step = 2
     for _ in range(args.warmup):
@@ -248,11 +265,12 @@ def run_reference(args):
     dt = time.perf_counter() - t
     value = n * n * (iters_per_step + 1) * args.steps / dt / 1e9
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "impl": "reference", "value": value, "unit": UNIT, "n_gpus": ws,
+        "metric": metric_of(workload, n, int((sites[..., 0] != -32768).sum())),
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+int16",
         "data": "synthetic (seeded Gaussian density on a disk, uniform sites)",
-        "config": {"workload": CONFIG, "n": n, "sites": int((sites[..., 0] != -32768).sum()),
+        "config": {"workload": workload, "n": n, "sites": int((sites[..., 0] != -32768).sum()),
                    "sample_iterations_per_step": iters_per_step},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                          "sample": "%d Lloyd iterations + final labelling per step, faithful "
@@ -273,7 +291,8 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    sites, rho, mask, iters = config_inputs(CONFIG, seed=SEED)
+    workload = args.config if args.config in PLAIN else CONFIG
+    sites, rho, mask, iters = config_inputs(workload, seed=SEED)
     assert iters == ITERS
     n = sites.shape[0]
     nsites = int((sites[..., 0] != -32768).sum())
@@ -362,12 +381,13 @@ def run_ours(args):
            + nsites * ALG_BYTES_PER_SITE)
     achieved = alg / (iter_ms / 1e3) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "metric": metric_of(workload, n, nsites), "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+int16",
         "data": "synthetic (seeded Gaussian density on a disk, uniform sites)",
-        "config": {"workload": CONFIG, "n": n, "sites": nsites, "iterations": ITERS,
+        "config": {"workload": workload, "n": n, "sites": nsites, "iterations": ITERS,
                    "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
                    "parallelism": "replicas x%d" % ws},
         "iter_per_s": ITERS * args.steps * ws / t_dev,
@@ -376,7 +396,7 @@ def run_ours(args):
         "tuning": tuning,
         "time_to_energy": tte,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
+                     "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(workload),
                      "peak_source": peak_kind,
                      "kernel": "k_list + k_cell<0> (one Lloyd iteration, iterations 2-100)",
                      "algorithmic_bytes": alg},
@@ -395,7 +415,7 @@ def run_ours(args):
     }
     if rank == 0:
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask)
+            line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask, workload=workload)
         if args.reference_gpu:
             line["reference_gpu"] = reference_gpu(sites, rho, mask)
         print(json.dumps(line))
@@ -421,14 +441,14 @@ def reference_gpu(sites, rho, mask):
                     "excludes its per-call allocation and copies, total_ms includes them"}
 
 
-def run_profile_case(iterations):
+def run_profile_case(iterations, workload=CONFIG):
     """The bench workload for ncu captures: load once, then `iterations` Lloyd
     iterations as the bench runs them (CUDA graphs of k_list + k_cell), timed
     as a whole with CUDA events on the context's stream."""
     import torch
     import gcvt_gb300 as G
     from workloads import config_inputs
-    sites, rho, mask, _ = config_inputs(CONFIG, seed=SEED)
+    sites, rho, mask, _ = config_inputs(workload, seed=SEED)
     stream = torch.cuda.Stream()
     ctx = G.Context(sites.shape[0])
     ctx.set_stream(stream.cuda_stream)
@@ -439,7 +459,7 @@ def run_profile_case(iterations):
     ctx.iterate(iterations)
     e1.record(stream)
     e1.synchronize()
-    print(json.dumps({"profile_case": CONFIG, "iterations": iterations,
+    print(json.dumps({"profile_case": workload, "iterations": iterations,
                       "lloyd_ms_per_iteration": e0.elapsed_time(e1) / iterations,
                       "energy": ctx.info()["energy"]}))
     ctx.close()
@@ -726,7 +746,8 @@ def main():
                     help="also time the reference's own kernels on this GPU")
     ap.add_argument("--profile-case", type=int, default=0, metavar="ITERS",
                     help="only run ITERS Lloyd iterations of the workload (for ncu)")
-    ap.add_argument("--config", default=CONFIG, choices=[CONFIG, "batched_64", "mesh_2048"],
+    ap.add_argument("--config", default=CONFIG,
+                    choices=list(PLAIN) + ["batched_64", "mesh_2048"],
                     help="batched_64 / mesh_2048: the batched-charts or mesh-driven workload "
                          "(their own JSON lines)")
     ap.add_argument("--profile-jfa", type=int, default=0, metavar="REPEATS",
@@ -735,7 +756,8 @@ def main():
                     help="only run REPEATS lifts of 65,536 points on the mesh (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
-        return run_profile_case(args.profile_case)
+        return run_profile_case(args.profile_case,
+                                args.config if args.config in PLAIN else CONFIG)
     if args.profile_jfa:
         return run_profile_jfa(args.profile_jfa)
     if args.profile_lift:
