@@ -17,7 +17,7 @@ constexpr int kNoneAbove = -32768;  // "no site above" in the column summaries
 constexpr int kNoneBelow = 32767;   // "no site below"
 constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 for
                                     // every entry of gcvt.cu:842-847
-constexpr int kRowsPerBlock = 4;    // rows (one warp each) per row-pass block
+constexpr int kRowsPerBlock = 1;    // rows (one warp each) per row-pass block
 constexpr int kListWords = 2048;   // bitmap words per site-list block
 constexpr int kMinN = 256;   // n must be a multiple of 256 (S = n/32 >= 8)
 constexpr int kMaxN = 8192;  // row-pass shared memory: 4 rows x 32 KB at 8192
