@@ -196,11 +196,11 @@ int ensure_cover(gcvt_ctx *c, int n, int level) {
   const LevelBufs b = level_bufs(c, n, level);
   CK(launch_summary(b, 0, c->stream));
   CK(launch_rows(b, 0, c->stream));
-  CK(launch_cover(b, c->stream));
+  CK(cudaMemsetAsync(c->hint, 0, (size_t)n * n, c->stream));
+  CK(launch_cover(b, c->stream));  // also each site's first window (hint)
   CK(launch_count(b, c->stream));
   const size_t nlb = list_blocks(n);
   CK(cudaMemsetAsync(c->counts[(c->st_host->cur + 1) % 3], 0, nlb * sizeof(unsigned), c->stream));
-  CK(cudaMemsetAsync(c->hint, 0, (size_t)n * n, c->stream));
   if (c->learning && level == 0) {  // no moves yet; ids = list positions
     CK(cudaMemsetAsync(c->hist[c->st_host->hist_cur], 0, (size_t)n * n * sizeof(uint64_t),
                        c->stream));

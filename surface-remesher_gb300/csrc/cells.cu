@@ -826,9 +826,29 @@ __global__ void __launch_bounds__(256) k_count(LevelBufs a) {
 
 // Covering bound from a label grid: cover = ceil(sqrt(max |p - label(p)|^2))
 // over the pixels of the density's row support.  One block per row.
+// hint[pid] = max(hint[pid], b) on the byte inside its 32-bit word.  Each
+// failed compare-and-swap means another byte of the word grew, so the loop is
+// short; past the limit the hint just stays lower (a wider first window).
+__device__ __forceinline__ void hint_max(uint8_t *hint, size_t pid, unsigned b) {
+  unsigned *word = reinterpret_cast<unsigned *>(hint + (pid & ~(size_t)3));
+  const int sh = (int)(pid & 3) * 8;
+  unsigned old = *reinterpret_cast<volatile unsigned *>(word);
+  for (int k = 0; k < 64 && ((old >> sh) & 0xffu) < b; ++k) {
+    const unsigned prev = atomicCAS(word, old, (old & ~(0xffu << sh)) | (b << sh));
+    if (prev == old) break;
+    old = prev;
+  }
+}
+
+// Covering bound of a label grid (max over density pixels of the squared
+// distance to their site), and each site's first window: 2 R + slack with R
+// the largest distance from the site to a density pixel of its cell (hint at
+// the site pixel, zeroed before), so the first iteration after a load needs
+// no window retries.
 __global__ void __launch_bounds__(256) k_cover(LevelBufs a) {
   const int n = a.n, y = blockIdx.x;
   const int2 yr = *a.sup_range;
+  const unsigned slack = (unsigned)a.st->hint_slack;
   unsigned m = 0;
   if (y >= yr.x && y < yr.y) {
     const int2 s = a.support[y];
@@ -837,13 +857,19 @@ __global__ void __launch_bounds__(256) k_cover(LevelBufs a) {
       const uint32_t v = row[x];
       const int lx = (int16_t)(v & 0xffffu), ly = (int16_t)(v >> 16);
       if (lx == kMarker) continue;  // no site at all
-      m = max(m, (unsigned)((x - lx) * (x - lx) + (y - ly) * (y - ly)));
+      const unsigned d2 = (unsigned)((x - lx) * (x - lx) + (y - ly) * (y - ly));
+      m = max(m, d2);
+      // ceil(sqrt(d2)) from a float square root, one integer correction up
+      unsigned r = (unsigned)sqrtf((float)d2);
+      if (r * r < d2) ++r;
+      const unsigned b = min(2u * r + slack, 255u);
+      const size_t pid = (size_t)ly * n + lx;
+      if (a.hint[pid] < b) hint_max(a.hint, pid, b);
     }
   }
   m = __reduce_max_sync(0xffffffffu, m);
   if ((threadIdx.x & 31) == 0 && m) atomicMax(&a.st->cover_acc, m);
 }
-
 __global__ void k_cover_finish(LevelBufs a) {
   DevState *st = a.st;
   st->cover = min(isqrt_ceil((int)st->cover_acc), 2 * a.n);
