@@ -688,12 +688,14 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   const size_t wbytes = bits_words(n) * sizeof(uint64_t), cbytes = list_blocks(n) * sizeof(unsigned);
   const size_t hbytes = (size_t)n * n;
   const size_t total = 3 * wbytes + 3 * cbytes + hbytes + sizeof(DevState);
-  unsigned char *save = nullptr;
-  if (cudaMalloc(reinterpret_cast<void **>(&save), total) != cudaSuccess) return GCVT_ERR_ALLOC;
+  unsigned char *save = nullptr;  // [0, total): the state to return to; [total, 2 total): the base
+  if (cudaMalloc(reinterpret_cast<void **>(&save), 2 * total) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
   DevState saved_host = *c->st_host;
   const int saved_valid = c->cover_valid;
+  size_t slot = 0;  // which copy copy_state uses
   auto copy_state = [&](bool to_save) -> int {
-    size_t off = 0;
+    size_t off = slot;
     auto mv = [&](void *p, size_t bytes) {
       const cudaError_t e = cudaMemcpyAsync(to_save ? save + off : p, to_save ? p : save + off,
                                             bytes, cudaMemcpyDeviceToDevice, c->stream);
@@ -710,7 +712,7 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   int sms = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   gcvt_tuning best = {0, c->hint_slack, c->jfa_halo, 1e30f, 1e30f};
-  const int per_sm[3] = {16, 24, 32}, slack[3] = {1, 2, 3};
+  const int slack[3] = {1, 2, 3};
   const int keep_grid = c->cell_grid, keep_slack = c->hint_slack;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
       cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
@@ -719,8 +721,31 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   if (!rc) rc = start_level(c, n, 0, 0x7fffffff, 0x7fffffff);
   if (!rc) rc = pull_state(c);
   if (!rc) rc = copy_state(true);
-  // Lloyd kernel: grid x hint slack, iterations 2-4 after the same start
-  for (int gi = 0; gi < 3 && !rc; ++gi)
+  // the base of the search: 16 iterations on, where most of a run's
+  // iterations look like (the first few after a load are heavier)
+  if (!rc) {
+    const LevelBufs lb = level_bufs(c, n, 0);
+    for (int it = 0; it < 16 && !rc; ++it)
+      if (launch_list(lb, 1, c->stream) != cudaSuccess ||
+          launch_cells(lb, 0, nullptr, c->stream) != cudaSuccess)
+        rc = GCVT_ERR_CUDA;
+  }
+  if (!rc) rc = pull_state(c);
+  slot = total;
+  if (!rc) rc = copy_state(true);
+  // Lloyd grids: 16, 24 and 32 blocks (warps) per SM, and the block counts
+  // that make the 32-site groups an exact number of waves (k groups per
+  // warp: no half-empty last wave)
+  int per_sm[12] = {16, 24, 32}, ngrid = 3;
+  const int groups = (c->st_host->snap_count + 31) / 32;
+  for (int k = 1; k <= 8 && sms > 0; ++k) {
+    const int b = (groups + k * sms - 1) / (k * sms);
+    bool seen = b < 12 || b > 32;
+    for (int q = 0; q < ngrid; ++q) seen = seen || per_sm[q] == b;
+    if (!seen && ngrid < 12) per_sm[ngrid++] = b;
+  }
+  // each: grid x hint slack, three iterations from the same base
+  for (int gi = 0; gi < ngrid && !rc; ++gi)
     for (int si = 0; si < 3 && !rc; ++si) {
       if ((rc = copy_state(false))) break;
       c->st_host->hint_slack = slack[si];
@@ -749,6 +774,7 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
       cudaMalloc(reinterpret_cast<void **>(&c->jfa),
                  2 * (size_t)c->n_max * c->n_max * sizeof(uint32_t) + 64) != cudaSuccess)
     rc = GCVT_ERR_ALLOC;
+  slot = 0;
   if (!rc) rc = copy_state(false);
   const int halos[3] = {8, 16, 32};
   for (int hi = 0; hi < 3 && !rc; ++hi) {
