@@ -18,8 +18,8 @@ Metric: Gpix-pass/s = n^2 x labelling passes / second, 101 passes per step
   e2e   : the same through the C ABI with pinned host buffers: host->device
           copies of sites, density and mask and the device->host copy of the
           label grid inside every timed step.
-  roofline: one Lloyd iteration, the launch pair k_list + k_cell<0> (88 % +
-          4 % of the step's device time): algorithmic bytes per iteration /
+  roofline: one Lloyd iteration, the launch pair k_list + k_cell<0> (89.5 % +
+          3.9 % of the run's device time): algorithmic bytes per iteration /
           its mean duration over iterations 2-100 of the timed steps (CUDA
           events on the launching stream around them) against the measured
           HBM copy bandwidth.
