@@ -849,26 +849,34 @@ __global__ void __launch_bounds__(256) k_cover(LevelBufs a) {
   const int n = a.n, y = blockIdx.x;
   const int2 yr = *a.sup_range;
   const unsigned slack = (unsigned)a.st->hint_slack;
+  const int lane = threadIdx.x & 31;
   unsigned m = 0;
   if (y >= yr.x && y < yr.y) {
     const int2 s = a.support[y];
     const uint32_t *row = a.labels + (size_t)y * n;
-    for (int x = s.x + threadIdx.x; x < s.y; x += blockDim.x) {
-      const uint32_t v = row[x];
+    // 32 consecutive pixels per warp step: the lanes holding one site's label
+    // (runs along the row) reduce together, one of them updates the hint
+    for (int base = s.x + (int)(threadIdx.x & ~31u); base < s.y; base += blockDim.x) {
+      const int x = base + lane;
+      const uint32_t v = x < s.y ? row[x] : kMarkerWord;
       const int lx = (int16_t)(v & 0xffffu), ly = (int16_t)(v >> 16);
-      if (lx == kMarker) continue;  // no site at all
-      const unsigned d2 = (unsigned)((x - lx) * (x - lx) + (y - ly) * (y - ly));
+      const bool site = lx != kMarker;
+      const unsigned d2 = site ? (unsigned)((x - lx) * (x - lx) + (y - ly) * (y - ly)) : 0u;
       m = max(m, d2);
-      // ceil(sqrt(d2)) from a float square root, one integer correction up
-      unsigned r = (unsigned)sqrtf((float)d2);
-      if (r * r < d2) ++r;
-      const unsigned b = min(2u * r + slack, 255u);
-      const size_t pid = (size_t)ly * n + lx;
-      if (a.hint[pid] < b) hint_max(a.hint, pid, b);
+      const unsigned grp = __match_any_sync(0xffffffffu, site ? v : kMarkerWord);
+      const unsigned g2 = __reduce_max_sync(grp, d2);
+      if (site && lane == __ffs(grp) - 1) {
+        // ceil(sqrt(g2)) from a float square root, one integer correction up
+        unsigned r = (unsigned)sqrtf((float)g2);
+        if (r * r < g2) ++r;
+        const unsigned b = min(2u * r + slack, 255u);
+        const size_t pid = (size_t)ly * n + lx;
+        if (a.hint[pid] < b) hint_max(a.hint, pid, b);
+      }
     }
   }
   m = __reduce_max_sync(0xffffffffu, m);
-  if ((threadIdx.x & 31) == 0 && m) atomicMax(&a.st->cover_acc, m);
+  if (lane == 0 && m) atomicMax(&a.st->cover_acc, m);
 }
 __global__ void k_cover_finish(LevelBufs a) {
   DevState *st = a.st;
