@@ -49,18 +49,18 @@ for _p in (os.path.join(PKG, "python"), PKG):
 import numpy as np  # noqa: E402
 
 CONFIG = "plain_4096"
-PLAIN = ("plain_4096", "plain_8192")  # the plain Lloyd workloads bench.py runs
+PLAIN = ("plain_4096", "plain_8192", "plain_1024")  # the plain Lloyd workloads bench.py runs
 SEED = 1
 ITERS = 100
 PASSES = ITERS + 1
 METRIC = "Gpix-pass/s, plain Lloyd CVT (gCVT loop), 4096^2 grid, 262,144 sites, 100 iterations"
 
 
-def metric_of(workload, n, nsites):
+def metric_of(workload, n, nsites, iters=ITERS):
     if workload == CONFIG:
         return METRIC
-    return "Gpix-pass/s, plain Lloyd CVT (gCVT loop), %d^2 grid, %s sites, 100 iterations" % (
-        n, format(nsites, ","))
+    return "Gpix-pass/s, plain Lloyd CVT (gCVT loop), %d^2 grid, %s sites, %d iterations" % (
+        n, format(nsites, ","), iters)
 UNIT = "Gpix-pass/s"
 # Algorithmic bytes of one Lloyd iteration (k_list + k_cell<0>): the density
 # once over its row support (4 B per support pixel: every such pixel belongs
@@ -79,7 +79,7 @@ NCU_TRAFFIC_BYTES = 54941440
 # the same capture on the 8192^2 / 1,048,576-site workload (iteration 31,
 # profiles/cell_kernel_plain_8192.md): k_list 13,138,176 + 3,403,520, k_cell
 # 265,760,256 + 77,200,896 bytes
-NCU_TRAFFIC = {"plain_4096": NCU_TRAFFIC_BYTES, "plain_8192": 359502848}
+NCU_TRAFFIC = {"plain_4096": NCU_TRAFFIC_BYTES, "plain_8192": 359502848, "plain_1024": None}
 
 
 def support_pixels(rho):
@@ -225,7 +225,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline_sample(sites, rho, mask, target_s=10.0, workload=CONFIG):
+def cpu_baseline_sample(sites, rho, mask, target_s=10.0, workload=CONFIG, iters=ITERS):
     """The oracle's OpenMP restatement of the reference's Lloyd loop (faithful
     FP32 mode, all host threads) on a bounded sample: as many iterations of
     the 4096^2 workload as fit in about target_s seconds."""
@@ -235,7 +235,7 @@ def cpu_baseline_sample(sites, rho, mask, target_s=10.0, workload=CONFIG):
     t = time.perf_counter()
     orc.gcvt(sites, rho, mask, 1, 1, mode=orc.FAITHFUL, fixed_iters=1)
     t1 = time.perf_counter() - t
-    k = int(max(1, min(ITERS, target_s / max(t1, 1e-3))))
+    k = int(max(1, min(iters, target_s / max(t1, 1e-3))))
     t = time.perf_counter()
     orc.gcvt(sites, rho, mask, 1, k, mode=orc.FAITHFUL, fixed_iters=k)
     dt = time.perf_counter() - t
@@ -293,7 +293,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     workload = args.config if args.config in PLAIN else CONFIG
     sites, rho, mask, iters = config_inputs(workload, seed=SEED)
-    assert iters == ITERS
+    passes = iters + 1
     n = sites.shape[0]
     nsites = int((sites[..., 0] != -32768).sum())
     stream = torch.cuda.Stream(device=dev)
@@ -309,7 +309,7 @@ def run_ours(args):
     ctx = G.Context(n)
     ctx.set_stream(stream.cuda_stream)
 
-    loop_ms = []  # iterations 2..ITERS of each timed device step
+    loop_ms = []  # iterations 2..iters of each timed device step
 
     def step_device(record=False):
         ctx.load(d_sites, d_rho, d_mask)
@@ -317,7 +317,7 @@ def run_ours(args):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        ctx.iterate(ITERS - 1)
+        ctx.iterate(iters - 1)
         b.record(stream)
         ctx.label(d_out)
         if record:
@@ -326,7 +326,7 @@ def run_ours(args):
     def step_host():
         ctx.load(h_sites, h_rho, h_mask)
         ctx.iterate(1)
-        ctx.iterate(ITERS - 1)
+        ctx.iterate(iters - 1)
         ctx.label(h_out)
 
     def barrier():
@@ -359,7 +359,7 @@ def run_ours(args):
             step_device()
         with ClockSampler(local) as clk:
             t_dev = timed(lambda: step_device(True), args.steps)
-        iter_ms = statistics.mean(a.elapsed_time(b) for a, b in loop_ms) / (ITERS - 1)
+        iter_ms = statistics.mean(a.elapsed_time(b) for a, b in loop_ms) / (iters - 1)
         info = ctx.info()  # state after the last timed step's 100 iterations
         for _ in range(max(1, args.warmup // 2)):
             step_host()
@@ -373,24 +373,24 @@ def run_ours(args):
         kms = ctx.time_kernels(5)
         torch.cuda.synchronize(dev)
     t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], ws, dev)
-    value = job_rate(n * n * PASSES, args.steps, ws, t_dev)
-    e2e = job_rate(n * n * PASSES, args.steps, ws, t_e2e)
+    value = job_rate(n * n * passes, args.steps, ws, t_dev)
+    e2e = job_rate(n * n * passes, args.steps, ws, t_e2e)
     peak, peak_kind = measured_peak()
     support_px = support_pixels(rho)
     alg = (support_px * ALG_BYTES_PER_SUPPORT_PX + n * n * ALG_BYTES_PER_PX
            + nsites * ALG_BYTES_PER_SITE)
     achieved = alg / (iter_ms / 1e3) / 1e9
     line = {
-        "metric": metric_of(workload, n, nsites), "value": value, "unit": UNIT, "n_gpus": ws,
+        "metric": metric_of(workload, n, nsites, iters), "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+int16",
         "data": "synthetic (seeded Gaussian density on a disk, uniform sites)",
-        "config": {"workload": workload, "n": n, "sites": nsites, "iterations": ITERS,
-                   "passes_per_step": PASSES, "l2": "flushed (256 MB write) before each step",
+        "config": {"workload": workload, "n": n, "sites": nsites, "iterations": iters,
+                   "passes_per_step": passes, "l2": "flushed (256 MB write) before each step",
                    "parallelism": "replicas x%d" % ws},
-        "iter_per_s": ITERS * args.steps * ws / t_dev,
+        "iter_per_s": iters * args.steps * ws / t_dev,
         "kernel_ms": {"lloyd_iteration": iter_ms, "label_pass": kms[1], "jfa_labelling": kms[2]},
         "jfa": jfa_line(n, kms[2], jfa_stats, peak, tuning["jfa_tail_halo"]),
         "tuning": tuning,
@@ -409,15 +409,16 @@ def run_ours(args):
         # iterate(1) and iterate(ITERS - 1) as graphs of ten (k_list, k_cell)
         # pairs, launches past the last iteration returning at once; final
         # labelling (column summaries, rows)
-        "gpu_launches": args.steps * (3 + 5 + 2 * 10 * (1 + (ITERS - 1 + 9) // 10) + 2),
+        "gpu_launches": args.steps * (3 + 5 + 2 * 10 * (1 + (iters - 1 + 9) // 10) + 2),
         "clocks": clk.summary(),
         "final_energy": info["energy"],
     }
     if rank == 0:
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask, workload=workload)
+            line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask, workload=workload,
+                                                       iters=iters)
         if args.reference_gpu:
-            line["reference_gpu"] = reference_gpu(sites, rho, mask)
+            line["reference_gpu"] = reference_gpu(sites, rho, mask, iters)
         print(json.dumps(line))
     ctx.close()
     if ws > 1:
@@ -425,7 +426,7 @@ def run_ours(args):
     return 0
 
 
-def reference_gpu(sites, rho, mask):
+def reference_gpu(sites, rho, mask, iters=ITERS):
     """The reference's own kernels (compiled from its sources into
     oracle/_ref/gcvt_ref.cubin) under gcvt.cu's loop on the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -434,11 +435,11 @@ def reference_gpu(sites, rho, mask):
         return {"unavailable": "reference cubin not built"}
     n = sites.shape[0]
     orc.ref_gcvt(sites, rho, mask, 1, 10, fixed_iters=10)
-    _, info = orc.ref_gcvt(sites, rho, mask, 1, ITERS, fixed_iters=ITERS)
-    return {"value": n * n * PASSES / (info["loop_ms"] / 1e3) / 1e9, "unit": UNIT,
+    _, info = orc.ref_gcvt(sites, rho, mask, 1, iters, fixed_iters=iters)
+    return {"value": n * n * (iters + 1) / (info["loop_ms"] / 1e3) / 1e9, "unit": UNIT,
             "loop_ms": info["loop_ms"], "total_ms": info["total_ms"],
-            "what": "gcvt.cu kernels on this GPU, 100 iterations + final labelling; loop_ms "
-                    "excludes its per-call allocation and copies, total_ms includes them"}
+            "what": "gcvt.cu kernels on this GPU, %d iterations + final labelling; loop_ms "
+                    "excludes its per-call allocation and copies, total_ms includes them" % iters}
 
 
 def run_profile_case(iterations, workload=CONFIG):
@@ -549,6 +550,18 @@ def run_batched(args):
         "same_energies_as_solo": same,
         "clocks": clk.summary(),
     }
+    if args.reference_gpu:  # 64 gCVT calls of the reference's kernels, one per chart
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        if orc.ref_available():
+            loop = total = 0.0
+            for sites, rho, mask in charts:
+                _, info = orc.ref_gcvt(sites, rho, mask, 1, iters, fixed_iters=iters)
+                loop += info["loop_ms"]
+                total += info["total_ms"]
+            line["reference_gpu"] = {"loop_ms": loop, "total_ms": total,
+                                     "value": px * (iters + 1) / (loop / 1e3) / 1e9,
+                                     "what": "the reference's gCVT kernels, one call per chart"}
     print(json.dumps(line))
     batch.close()
     for c in ctxs:
@@ -612,6 +625,23 @@ def run_mesh(args):
             ms.append(e0.elapsed_time(e1))
     t = statistics.mean(ms)
     lift = lift_stage(ctx, n, args)
+    ref = None
+    if args.reference_gpu:  # the reference's rasteriser and gCVT kernels on this mesh
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        if orc.ref_available():
+            # the reference tests every triangle at every pixel: timed on the
+            # 64^2-vertex mesh (its cost grows with the triangle count) and
+            # scaled to this one
+            (p64, w64, t64, s64), _ = mesh_inputs(64, n, seed=2)
+            ref_rho, ref_ms = orc.ref_rasterize(p64, w64, t64, s64, n)
+            ours64 = G.rasterize(p64, w64, t64, s64, n)
+            _, info = orc.ref_gcvt(sites, rho, mask, 1, iters, fixed_iters=iters)
+            ref = {"raster_ms_64": ref_ms, "triangles_64": int(len(t64)),
+                   "raster_ms_scaled": ref_ms * len(tris) / len(t64),
+                   "same_density_64": bool(np.array_equal(ref_rho.view(np.int32),
+                                                          ours64.view(np.int32))),
+                   "loop_ms": info["loop_ms"], "total_ms": info["total_ms"]}
     print(json.dumps({
         "metric": "Gpix-pass/s, mesh-driven density (2048^2 raster of a 256^2-vertex disk mesh), 65,536 sites, 100 iterations",
         "value": n * n * (iters + 1) / (t / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
@@ -622,6 +652,7 @@ def run_mesh(args):
                    "vertices": int(len(w)), "sites": m, "iterations": iters},
         "raster_ms": statistics.median(raster_ms),
         "lift": lift,
+        "reference_gpu": ref,
         "final_energy": ctx.info()["energy"]}))
     ctx.close()
     return 0
