@@ -21,7 +21,9 @@
 // outside the disc can beat s there (|p - t| > W - R >= R); otherwise the
 // window grows (W <- min(2R + 1, 2W)) and the cell is redone; a window
 // covering the grid is exact by construction.  The starting W of a site is
-// the hint its predecessor left at its pixel (2R + 2 of the cell it had).
+// the hint at its pixel: 2R + slack of the cell the site that moved there
+// had, or, after a load, of its own cell in the level start's label grid
+// (k_cover).
 //
 // Rows are visited outward from s.  A row may hold no pixel of the cell while
 // a row further out does (a sliver narrower than a pixel), so the walk ends
