@@ -58,6 +58,9 @@ typedef struct {
     int jfa_tail_halo;      /* jump flooding: steps <= halo/2 fused in one launch (8/16/32) */
     float lloyd_ms;         /* autotune: best time of one Lloyd iteration (ms)           */
     float jfa_ms;           /* autotune: best time of one jump-flooding labelling (ms)   */
+    int cell_mode;          /* Lloyd cells: 0 = one site per warp up to 8192 sites, else
+                               one per lane; 1 = one per lane; 2 = one per warp (up to
+                               8192 sites, and not while learned steps are enabled)     */
 } gcvt_tuning;
 
 /* Human-readable text of a status code. */

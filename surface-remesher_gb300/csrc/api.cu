@@ -54,6 +54,9 @@ struct gcvt_ctx {
   int cell_grid = 0;
   int hint_slack = 2;
   int jfa_halo = 16;
+  int cell_mode = 0;            // 0 auto, 1 one site per lane, 2 one site per warp
+  float4 *sitev = nullptr;      // one site per warp: kWarpSites site values
+  unsigned *gcnt = nullptr;     //   and kWarpSites / 32 group counters
   // learned steps (gcvt_ctx_learning): histories, ids, features, predictions,
   // bfloat16-rounded MLP parameters
   int learning = 0, track_ids = 0, have_mlp = 0;
@@ -104,6 +107,11 @@ LevelBufs level_bufs(gcvt_ctx *c, int n, int level) {
   b.gslot = c->gslot;
   b.sslot = c->sslot;
   b.scnt = c->scnt;
+  // one site per warp when the sites are too few to fill the GPU one per lane
+  if (c->cell_mode == 2 || (c->cell_mode == 0 && c->sites <= kWarpSites)) {
+    b.sitev = c->sitev;
+    b.gcnt = c->gcnt;
+  }
   if (c->learning && level == 0) {
     b.hist[0] = c->hist[0];
     b.hist[1] = c->hist[1];
@@ -411,10 +419,13 @@ int gcvt_ctx_create(int n_max, gcvt_ctx **out) {
   ok = ok && dal(&c->gslot, groups * sizeof(float4));
   ok = ok && dal(&c->sslot, slots * sizeof(float4));
   ok = ok && dal(&c->scnt, slots * sizeof(unsigned));
+  ok = ok && dal(&c->sitev, kWarpSites * sizeof(float4));
+  ok = ok && dal(&c->gcnt, (kWarpSites / 32) * sizeof(unsigned));
   ok = ok && dal(&c->colcnt, ((size_t)n_max + 1) * sizeof(unsigned));
   ok = ok && dal(&c->err, 2 * sizeof(int));
   if (!ok) return fail(GCVT_ERR_ALLOC);
-  if (cudaMemsetAsync(c->scnt, 0, slots * sizeof(unsigned), c->stream) != cudaSuccess)
+  if (cudaMemsetAsync(c->scnt, 0, slots * sizeof(unsigned), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->gcnt, 0, (kWarpSites / 32) * sizeof(unsigned), c->stream) != cudaSuccess)
     return fail(GCVT_ERR_CUDA);
   if (cudaMallocHost(reinterpret_cast<void **>(&c->st_host), sizeof(DevState)) != cudaSuccess)
     return fail(GCVT_ERR_ALLOC);
@@ -451,6 +462,8 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->gslot);
   cudaFree(c->sslot);
   cudaFree(c->scnt);
+  cudaFree(c->sitev);
+  cudaFree(c->gcnt);
   cudaFree(c->colcnt);
   cudaFree(c->jfa);
   for (int k = 0; k < 2; ++k) {
@@ -660,17 +673,19 @@ int gcvt_ctx_set_tuning(gcvt_ctx *c, const gcvt_tuning *t) {
   if (!c || !t) return GCVT_ERR_ARGUMENT;
   if (t->cell_blocks_per_sm < 0 || t->cell_blocks_per_sm > 32 || t->hint_slack < 0 ||
       t->hint_slack > 64 || (t->jfa_tail_halo != 8 && t->jfa_tail_halo != 16 &&
-                             t->jfa_tail_halo != 32))
+                             t->jfa_tail_halo != 32) ||
+      t->cell_mode < 0 || t->cell_mode > 2)
     return GCVT_ERR_ARGUMENT;
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
     return GCVT_ERR_CUDA;
   const int grid = t->cell_blocks_per_sm * sms;
-  if (grid != c->cell_grid && c->chunk_exec) {  // the captured grid changes
-    cudaGraphExecDestroy(c->chunk_exec);
+  if ((grid != c->cell_grid || t->cell_mode != c->cell_mode) && c->chunk_exec) {
+    cudaGraphExecDestroy(c->chunk_exec);  // the captured launches change
     c->chunk_exec = nullptr;
   }
   c->cell_grid = grid;
+  c->cell_mode = t->cell_mode;
   c->hint_slack = t->hint_slack;
   c->jfa_halo = t->jfa_tail_halo;
   return GCVT_OK;
@@ -711,9 +726,9 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   };
   int sms = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  gcvt_tuning best = {0, c->hint_slack, c->jfa_halo, 1e30f, 1e30f};
+  gcvt_tuning best = {0, c->hint_slack, c->jfa_halo, 1e30f, 1e30f, c->cell_mode};
   const int slack[3] = {1, 2, 3};
-  const int keep_grid = c->cell_grid, keep_slack = c->hint_slack;
+  const int keep_grid = c->cell_grid, keep_slack = c->hint_slack, keep_mode = c->cell_mode;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
       cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     rc = GCVT_ERR_CUDA;
@@ -744,12 +759,17 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
     for (int q = 0; q < ngrid; ++q) seen = seen || per_sm[q] == b;
     if (!seen && ngrid < 12) per_sm[ngrid++] = b;
   }
-  // each: grid x hint slack, three iterations from the same base
+  // cells one site per lane, and (few sites, no learned-step state) one per warp
+  const int modes[2] = {1, 2};
+  const int nmode = (c->sites <= kWarpSites && !c->learning) ? 2 : 1;
+  // each: mode x grid x hint slack, three iterations from the same base
+  for (int mi = 0; mi < nmode && !rc; ++mi)
   for (int gi = 0; gi < ngrid && !rc; ++gi)
     for (int si = 0; si < 3 && !rc; ++si) {
       if ((rc = copy_state(false))) break;
       c->st_host->hint_slack = slack[si];
       if ((rc = push_state(c))) break;
+      c->cell_mode = modes[mi];
       const LevelBufs lb = level_bufs(c, n, 0);
       const int grid = per_sm[gi] * sms;
       float ms = 0.f;
@@ -767,8 +787,10 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
         best.lloyd_ms = ms / 3;
         best.cell_blocks_per_sm = per_sm[gi];
         best.hint_slack = slack[si];
+        best.cell_mode = modes[mi];
       }
     }
+  c->cell_mode = keep_mode;
   // jump flooding: fusion depth
   if (!rc && !c->jfa &&
       cudaMalloc(reinterpret_cast<void **>(&c->jfa),
@@ -810,6 +832,7 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
   if (rc) {
     c->cell_grid = keep_grid;
     c->hint_slack = keep_slack;
+    c->cell_mode = keep_mode;
     return rc;
   }
   rc = gcvt_ctx_set_tuning(c, &best);

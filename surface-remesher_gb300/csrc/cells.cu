@@ -198,6 +198,34 @@ __device__ __forceinline__ RowPair row_bounds2(const int2 *rec, int cnt, bool ov
   return p;
 }
 
+// FP32 sums of one chunk [u0, u1] (at most 16 pixels) of a row: density,
+// x-moment and x^2-moment relative to the site.
+__device__ __forceinline__ void chunk_sums(const float *__restrict__ row, int u0, int u1,
+                                           float &rw, float &rx, float &rq) {
+  rw = 0.f, rx = 0.f, rq = 0.f;
+  float dx = (float)u0;
+#pragma unroll 4
+  for (int u = u0; u <= u1; ++u) {
+    const float rho = __ldg(row + u);
+    const float t = __fmul_rn(dx, rho);
+    rw = __fadd_rn(rw, rho);
+    rx = __fadd_rn(rx, t);
+    rq = __fmaf_rn(t, dx, rq);
+    dx = __fadd_rn(dx, 1.0f);
+  }
+}
+
+// A chunk of row v (fv = v, fv2 = v^2) folded into the two-float cell sums.
+__device__ __forceinline__ void fold_chunk(CellSums &c, float rw, float rx, float rq, float fv,
+                                           float fv2) {
+  dfa(c.wh, c.wl, rw, 0.f);
+  dfa(c.xh, c.xl, rx, 0.f);
+  dfa_scaled(c.yh, c.yl, fv, rw, 0.f);
+  float qh = rq, ql = 0.f;
+  dfa_scaled(qh, ql, fv2, rw, 0.f);
+  dfa(c.eh, c.el, qh, ql);
+}
+
 // Sums of row v = [da, db] (relative columns) into c: FP32 over chunks of at
 // most 16 pixels (relative error below 16 ulp of the chunk), chunks folded
 // into the two-float cell sums.
@@ -205,43 +233,57 @@ __device__ __forceinline__ void row_sums(const float *__restrict__ row, int da, 
                                          CellSums &c) {
   const float fv = (float)v, fv2 = (float)(v * v);
   for (int u0 = da; u0 <= db; u0 += 16) {
-    const int u1 = min(db, u0 + 15);
-    float rw = 0.f, rx = 0.f, rq = 0.f;
-    float dx = (float)u0;
-#pragma unroll 4
-    for (int u = u0; u <= u1; ++u) {
-      const float rho = __ldg(row + u);
-      const float t = __fmul_rn(dx, rho);
-      rw = __fadd_rn(rw, rho);
-      rx = __fadd_rn(rx, t);
-      rq = __fmaf_rn(t, dx, rq);
-      dx = __fadd_rn(dx, 1.0f);
-    }
-    dfa(c.wh, c.wl, rw, 0.f);
-    dfa(c.xh, c.xl, rx, 0.f);
-    dfa_scaled(c.yh, c.yl, fv, rw, 0.f);
-    float qh = rq, ql = 0.f;
-    dfa_scaled(qh, ql, fv2, rw, 0.f);
-    dfa(c.eh, c.el, qh, ql);
+    float rw, rx, rq;
+    chunk_sums(row, u0, min(db, u0 + 15), rw, rx, rq);
+    fold_chunk(c, rw, rx, rq, fv, fv2);
   }
 }
 
-// Row v of the cell with bounds [lo, hi]: clip to the density support and
-// the covering disc, sum it, track R2.
-__device__ __forceinline__ void take_row(const LevelBufs &a, int n, int sx, int sy, int rb2, int v,
-                                         int lo, int hi, int &R2, CellSums &c) {
-  const int y = sy + v;
-  const int2 s = a.support[y];
-  int da = max(lo, s.x - sx), db = min(hi, s.y - 1 - sx);
-  if (da > db) return;
+// The pixels [da, db] of row v the cell with bounds [lo, hi] sums: clipped to
+// the density support and the covering disc; false when none.
+__device__ __forceinline__ bool row_span(const LevelBufs &a, int sx, int sy, int rb2, int v,
+                                         int lo, int hi, int &da, int &db) {
+  const int2 s = a.support[sy + v];
+  da = max(lo, s.x - sx), db = min(hi, s.y - 1 - sx);
+  if (da > db) return false;
   if (max(da * da, db * db) + v * v > rb2) {  // clip to the covering disc
     const int hx = isqrt_floor(rb2 - v * v);
     da = max(da, -hx);
     db = min(db, hx);
-    if (da > db) return;
+    if (da > db) return false;
   }
+  return true;
+}
+
+// Row v of the cell with bounds [lo, hi]: its span, R2, its sums.
+__device__ __forceinline__ void take_row(const LevelBufs &a, int n, int sx, int sy, int rb2, int v,
+                                         int lo, int hi, int &R2, CellSums &c) {
+  int da, db;
+  if (!row_span(a, sx, sy, rb2, v, lo, hi, da, db)) return;
   R2 = max(R2, max(da * da, db * db) + v * v);
-  row_sums(a.density + (size_t)y * n + sx, da, db, v, c);
+  row_sums(a.density + (size_t)(sy + v) * n + sx, da, db, v, c);
+}
+
+// A site in s's own column at row offset B != 0: s keeps the rows strictly on
+// its side of the mirror row, and the mirror row (B even) if the band rule
+// says so.
+__device__ __forceinline__ void same_column_limit(int B, int sy, int &vmin, int &vmax) {
+  if (B > 0) {
+    int m = (B - 1) >> 1;
+    if (!(B & 1) && (((sy + B) >> 6) != ((sy + B / 2) >> 6))) m = B / 2;
+    vmax = min(vmax, m);
+  } else {
+    int m = -((-B - 1) >> 1);
+    if (!(B & 1) && ((sy >> 6) == ((sy + B / 2) >> 6))) m = B / 2;
+    vmin = max(vmin, m);
+  }
+}
+
+// The record {K, S | D << 16} of candidate t = s + (A, B), A != 0, K = A^2 + B^2
+// (|S|, |D| <= 2 (n - 1) fit 16 bits).
+__device__ __forceinline__ int2 make_rec(int A, int B, int K) {
+  const int S = A > 0 ? 2 * B : -2 * B;
+  return make_int2(A > 0 ? K : -K, (int)(((unsigned)S & 0xffffu) | ((unsigned)(2 * A) << 16)));
 }
 
 // The sites of one bitmap word (column offset A, bit i at row offset B0 + i)
@@ -256,27 +298,14 @@ __device__ __forceinline__ void gather_word(uint64_t w, int A, int B0, int sy, l
     const int K = A * A + B * B;
     if (K == 0 || (long long)K > Wc) continue;  // s itself; outside the disc
     if (A == 0) {
-      // same column: s keeps the rows strictly on its side of the mirror row,
-      // and the mirror row (B even) if the band rule says so
-      if (B > 0) {
-        int m = (B - 1) >> 1;
-        if (!(B & 1) && (((sy + B) >> 6) != ((sy + B / 2) >> 6))) m = B / 2;
-        vmax = min(vmax, m);
-      } else {
-        int m = -((-B - 1) >> 1);
-        if (!(B & 1) && ((sy >> 6) == ((sy + B / 2) >> 6))) m = B / 2;
-        vmin = max(vmin, m);
-      }
+      same_column_limit(B, sy, vmin, vmax);
       continue;
     }
     if (cnt >= kMaxCand) {
       ovf = true;
       continue;
     }
-    // |S|, |D| <= 2 (n - 1) fit 16 bits
-    const int S = A > 0 ? 2 * B : -2 * B;
-    rec[cnt++] = make_int2(A > 0 ? K : -K,
-                           (int)(((unsigned)S & 0xffffu) | ((unsigned)(2 * A) << 16)));
+    rec[cnt++] = make_rec(A, B, K);
   }
 }
 
@@ -499,63 +528,51 @@ __device__ __forceinline__ void site_features(const LevelBufs &a, const IterView
 // and the group's share of the energy reduction; the warp that completes the
 // chart's last 64-group runs its schedule.  MODE 1: moments only, written as
 // doubles (W, X, Y, E) at each site pixel of out4 (four n*n planes).
-template <int MODE>
-__device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, int lane,
-                           double *out4) {
+// The move of listed site e at (sx, sy) with cell sums cs (gcvt.cu:753-781):
+// the over-relaxed centroid rounded to float, then to a pixel; fixed sites
+// and zero-density targets stay.  The site goes into the next bitmap (the
+// first to set a bit counts it for the next list), leaves its window hint and
+// (learned steps) its move history and id at its new pixel.  Returns the
+// move's squared length.
+__device__ __forceinline__ unsigned move_site(const LevelBufs &a, const IterView &v, uint32_t e,
+                                              int sx, int sy, const CellSums &cs) {
   const int n = a.n;
-  float eh = 0.f, el = 0.f;
-  unsigned r2 = 0, mv = 0;
-  const int idx = (int)g * 32 + lane;
-  if (idx < v.nsites) {
-    const uint32_t e = a.list[idx];
-    const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
-    const size_t pid = (size_t)sy * n + sx;
-    const int h = a.hint[pid];
-    const CellSums cs = cell_sums(a, v.bits, n, sx, sy, h ? h : v.W0, v.rb);
-    if (MODE == 1) {
-      const size_t nn = (size_t)n * n;
-      const double Wd = (double)cs.wh + (double)cs.wl;
-      out4[pid] = Wd;
-      out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
-      out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
-      out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
-    } else if (MODE == 2 || MODE == 3) {  // learned jump: energy, features or hints
-      dfa(eh, el, cs.eh, cs.el);
-      r2 = (unsigned)cs.r2;
-      if (MODE == 2) site_features(a, v, idx, sx, sy);
-      else a.hint[pid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
-    } else {
-      dfa(eh, el, cs.eh, cs.el);
-      const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
-      const float cy = cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl);
-      const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)sx), v.omega, (float)sx), 0.5f);
-      const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)sy), v.omega, (float)sy), 0.5f);
-      int nx = min(max(__float2int_rz(fx), 0), n - 1);
-      int ny = min(max(__float2int_rz(fy), 0), n - 1);
-      if ((e & 0x8000u) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = sx; ny = sy; }
-      r2 = (unsigned)cs.r2;
-      mv = (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy));
-      const size_t widx = (size_t)(ny / kBand) * n + nx;
-      const unsigned long long bit = 1ull << (ny % kBand);
-      const unsigned long long old =
-          atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
-      if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
-      const size_t npid = (size_t)ny * n + nx;
-      a.hint[npid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
-      if (a.hist[0]) {  // this move becomes the newest of the site's last four
-        const int mx = min(max(nx - sx, -127), 127), my = min(max(ny - sy, -127), 127);
-        a.hist[v.hc ^ 1][npid] = (a.hist[v.hc][pid] << 16) | (uint64_t)(uint8_t)mx |
-                                 ((uint64_t)(uint8_t)my << 8);
-      }
-      if (a.ids[0]) a.ids[v.hc ^ 1][npid] = a.ids[v.hc][pid];
-    }
+  const size_t pid = (size_t)sy * n + sx;
+  const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
+  const float cy = cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl);
+  const float fx = __fadd_rn(__fmaf_rn(__fsub_rn(cx, (float)sx), v.omega, (float)sx), 0.5f);
+  const float fy = __fadd_rn(__fmaf_rn(__fsub_rn(cy, (float)sy), v.omega, (float)sy), 0.5f);
+  int nx = min(max(__float2int_rz(fx), 0), n - 1);
+  int ny = min(max(__float2int_rz(fy), 0), n - 1);
+  if ((e & 0x8000u) || a.density[(size_t)ny * n + nx] == 0.0f) { nx = sx; ny = sy; }
+  const unsigned mv = (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy));
+  const size_t widx = (size_t)(ny / kBand) * n + nx;
+  const unsigned long long bit = 1ull << (ny % kBand);
+  const unsigned long long old =
+      atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
+  if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
+  const size_t npid = (size_t)ny * n + nx;
+  a.hint[npid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+  if (a.hist[0]) {  // this move becomes the newest of the site's last four
+    const int mx = min(max(nx - sx, -127), 127), my = min(max(ny - sy, -127), 127);
+    a.hist[v.hc ^ 1][npid] = (a.hist[v.hc][pid] << 16) | (uint64_t)(uint8_t)mx |
+                             ((uint64_t)(uint8_t)my << 8);
   }
-  __syncwarp();
-  if (MODE == 1) return;
+  if (a.ids[0]) a.ids[v.hc ^ 1][npid] = a.ids[v.hc][pid];
+  return mv;
+}
+
+// The energy reduction after group g (lane i holds site 32 g + i's energy
+// two-float, max cell radius^2 and move^2): group total -> slot; the warp
+// finishing the last group of a 64-group reduces the 64 slots; the warp
+// finishing the last 64-group totals them and runs the schedule (MODE 0) or
+// the learned jump's gate (MODE 2, 3).
+template <int MODE>
+__device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v, unsigned g,
+                                           int lane, float eh, float el, unsigned r2,
+                                           unsigned mv) {
   DevState *st = a.st;
   warp_reduce(eh, el, r2, mv);
-  // group total -> slot; the warp finishing the last group of a 64-group
-  // reduces the 64 slots; the warp finishing the last 64-group totals them
   int last = 0;
   const unsigned sg = g / kGroupsPerSlot;
   const unsigned sbase = sg * kGroupsPerSlot;
@@ -597,8 +614,265 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
   warp_reduce(eh, el, r2, mv);
   if (lane == 0) {
     const double E = ((double)eh + (double)el) * st->energy_scale;
-    if (MODE == 0) run_schedule(st, E, r2, mv, n, v.cur);
+    if (MODE == 0) run_schedule(st, E, r2, mv, a.n, v.cur);
     else gate_pass_done<MODE>(st, E);
+  }
+}
+
+// Group g of a chart (32 listed sites, one per lane).  MODE 0: cells, moves,
+// and the group's share of the energy reduction.  MODE 1: moments only,
+// written as doubles (W, X, Y, E) at each site pixel of out4 (four n*n
+// planes).  MODE 2, 3: the learned jump's passes.
+template <int MODE>
+__device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, int lane,
+                           double *out4) {
+  const int n = a.n;
+  float eh = 0.f, el = 0.f;
+  unsigned r2 = 0, mv = 0;
+  const int idx = (int)g * 32 + lane;
+  if (idx < v.nsites) {
+    const uint32_t e = a.list[idx];
+    const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
+    const size_t pid = (size_t)sy * n + sx;
+    const int h = a.hint[pid];
+    const CellSums cs = cell_sums(a, v.bits, n, sx, sy, h ? h : v.W0, v.rb);
+    if (MODE == 1) {
+      const size_t nn = (size_t)n * n;
+      const double Wd = (double)cs.wh + (double)cs.wl;
+      out4[pid] = Wd;
+      out4[nn + pid] = (double)sx * Wd + ((double)cs.xh + (double)cs.xl);
+      out4[2 * nn + pid] = (double)sy * Wd + ((double)cs.yh + (double)cs.yl);
+      out4[3 * nn + pid] = (double)cs.eh + (double)cs.el;
+    } else {
+      dfa(eh, el, cs.eh, cs.el);
+      r2 = (unsigned)cs.r2;
+      if (MODE == 2) site_features(a, v, idx, sx, sy);
+      else if (MODE == 3) a.hint[pid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+      else mv = move_site(a, v, e, sx, sy, cs);
+    }
+  }
+  __syncwarp();
+  if (MODE == 1) return;
+  group_tail<MODE>(a, v, g, lane, eh, el, r2, mv);
+}
+
+// ---------------------------------------------------------------------------
+// One site per warp, for problems with fewer sites than the GPU holds warps
+// (a lane-per-site group then runs one site's whole cell serially, and only
+// a few groups exist).  The same cell and the same sums, bit for bit: the
+// candidates are gathered by the lanes into shared memory, the rows of the
+// walk are bounded and summed one per lane, 32 at a time, and lane 0 folds
+// the rows' chunk sums into the cell sums in the lane-per-site order.  The
+// energy reduction keeps its groups: each site's contribution waits in
+// LevelBufs::sitev, and the warp finishing a group's last site reduces it.
+// ---------------------------------------------------------------------------
+
+constexpr int kWarpChunks = 4;  // chunk sums per row kept in shared memory
+
+struct WarpScratch {
+  int2 rec[kMaxCand];
+  float part[32][kWarpChunks][3];  // per row (lane): chunk sums rw, rx, rq
+  int2 span[32];                   // per row: summed pixels [da, db]
+};
+
+__device__ CellSums cell_sums_warp(const LevelBufs &a, const uint64_t *__restrict__ bits, int n,
+                                   int sx, int sy, int W, int rb, int lane, WarpScratch &ws) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int2 yr = *a.sup_range;
+  const int vlo_sup = max(yr.x, sy - rb) - sy, vhi_sup = min(yr.y - 1, sy + rb) - sy;
+  const int rb2 = rb * rb;
+  W = max(1, min(W, 2 * rb));
+  CellSums c;
+  for (;;) {
+    const int x0 = max(0, sx - W), x1 = min(n - 1, sx + W);
+    const int y0 = max(0, sy - W), y1 = min(n - 1, sy + W);
+    const bool whole = x0 == 0 && y0 == 0 && x1 == n - 1 && y1 == n - 1;
+    const int b0 = y0 >> 6, b1 = y1 >> 6, nb = b1 - b0 + 1, ncol = x1 - x0 + 1;
+    const long long W2 = (long long)W * W;
+    const long long Wc = whole ? (1ll << 62) : W2;
+    // candidates: lanes over the window's (column, band) words, records
+    // compacted into shared memory in word order
+    int cnt = 0;
+    int vmin = vlo_sup, vmax = vhi_sup;
+    for (int t0 = 0; t0 < ncol * nb; t0 += 32) {
+      const int t = t0 + lane;
+      uint64_t w = 0ull;
+      int A = 0, B0 = 0;
+      if (t < ncol * nb) {
+        const int x = x0 + t / nb, b = b0 + t % nb;
+        w = __ldg(bits + (size_t)b * n + x) & row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63));
+        A = x - sx;
+        B0 = 64 * b - sy;
+      }
+      int mine = 0;
+      for (uint64_t q = w; q; q &= q - 1ull) {
+        const int B = B0 + __ffsll((long long)q) - 1;
+        const int K = A * A + B * B;
+        if (K == 0 || (long long)K > Wc) continue;
+        if (A == 0) same_column_limit(B, sy, vmin, vmax);
+        else ++mine;
+      }
+      int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += u;
+      }
+      int pos = cnt + incl - mine;
+      if (mine) {
+        for (uint64_t q = w; q; q &= q - 1ull) {
+          const int B = B0 + __ffsll((long long)q) - 1;
+          const int K = A * A + B * B;
+          if (K == 0 || (long long)K > Wc || A == 0) continue;
+          if (pos < kMaxCand) ws.rec[pos] = make_rec(A, B, K);
+          ++pos;
+        }
+      }
+      cnt += __shfl_sync(kFull, incl, 31);
+    }
+    vmin = __reduce_max_sync(kFull, vmin);
+    vmax = __reduce_min_sync(kFull, vmax);
+    const bool ovf = cnt > kMaxCand;
+    __syncwarp();
+    const bool fast = 2 * W2 + 2 * (long long)W * rb < (1ll << 23);
+    c = CellSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};  // lane 0 accumulates
+    int R2 = 0;
+    // rows outward from s, up from v = 0 then down from v = -1, 32 per step
+    // (one per lane); the walk ends at its first row with lo > hi + 1
+    for (int dir = 1; dir >= -1; dir -= 2) {
+      const int vend = dir > 0 ? vmax : vmin;
+      const int vstart = dir > 0 ? max(0, vmin) : min(-1, vmax);
+      for (int base = vstart; dir > 0 ? base <= vend : base >= vend; base += 32 * dir) {
+        const int vr = base + dir * lane;
+        const bool inr = dir > 0 ? vr <= vend : vr >= vend;
+        int lo = -sx, hi = n - 1 - sx;
+        if (inr) {
+          if (!ovf) {
+            for (int k = 0; k < cnt; ++k) {
+              const int2 r = ws.rec[k];
+              const int S = (int)(int16_t)((unsigned)r.y & 0xffffu);
+              const int D = (int)(int16_t)((unsigned)r.y >> 16);
+              const int aD = abs(D);
+              const int N = r.x - S * vr;
+              const int q = fast ? floordiv_r(N, aD, rcp_approx((float)aD))
+                                 : floordiv_est(N, aD, 0.f, false);
+              if (D > 0) hi = min(hi, q);
+              else lo = max(lo, q + 1);
+            }
+          } else {
+            for (int x = x0; x <= x1; ++x)
+              for (int b = b0; b <= b1; ++b) {
+                uint64_t w = __ldg(bits + (size_t)b * n + x) &
+                             row_mask(max(y0 - 64 * b, 0), min(y1 - 64 * b, 63));
+                while (w) {
+                  const int i = __ffsll((long long)w) - 1;
+                  w &= w - 1ull;
+                  const int A = x - sx, B = 64 * b + i - sy;
+                  const int K = A * A + B * B;
+                  if (K == 0 || (long long)K > Wc) continue;
+                  constrain_rel(A, B, vr, lo, hi);
+                }
+              }
+          }
+        }
+        const unsigned sb = __ballot_sync(kFull, !inr || lo > hi + 1);
+        const int f = sb ? __ffs(sb) - 1 : 32;  // rows 0 .. f-1 of this step are walked
+        int da = 1, db = 0;
+        if (lane < f && lo <= hi && row_span(a, sx, sy, rb2, vr, lo, hi, da, db)) {
+          R2 = max(R2, max(da * da, db * db) + vr * vr);
+          const float *row = a.density + (size_t)(sy + vr) * n + sx;
+          int k = 0;
+          for (int u0 = da; u0 <= db && k < kWarpChunks; u0 += 16, ++k)
+            chunk_sums(row, u0, min(db, u0 + 15), ws.part[lane][k][0], ws.part[lane][k][1],
+                       ws.part[lane][k][2]);
+        }
+        ws.span[lane] = make_int2(da, db);
+        __syncwarp();
+        if (lane == 0) {
+          for (int r = 0; r < f; ++r) {
+            const int2 sp = ws.span[r];
+            if (sp.x > sp.y) continue;
+            const int vv = base + dir * r;
+            const float fv = (float)vv, fv2 = (float)(vv * vv);
+            const float *row = a.density + (size_t)(sy + vv) * n + sx;
+            int k = 0;
+            for (int u0 = sp.x; u0 <= sp.y; u0 += 16, ++k) {
+              float rw, rx, rq;
+              if (k < kWarpChunks) {
+                rw = ws.part[r][k][0];
+                rx = ws.part[r][k][1];
+                rq = ws.part[r][k][2];
+              } else {
+                chunk_sums(row, u0, min(sp.y, u0 + 15), rw, rx, rq);
+              }
+              fold_chunk(c, rw, rx, rq, fv, fv2);
+            }
+          }
+        }
+        __syncwarp();
+        if (f < 32) break;
+      }
+    }
+    R2 = __reduce_max_sync(kFull, R2);
+    if (lane == 0) c.r2 = R2;
+    if (whole || 4 * (long long)R2 <= W2) return c;
+    W = min(min(2 * isqrt_ceil(R2) + 1, 2 * W), 2 * rb);
+  }
+}
+
+// One Lloyd iteration, one listed site per warp from a site ticket.
+__global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
+  __shared__ WarpScratch ws;
+  DevState *st = a.st;
+  if (st->snap_stopped) return;
+  const int lane = threadIdx.x;
+  const IterView v = iter_view(a);
+  clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
+  if (v.ngroups == 0) {  // no sites: the schedule still advances
+    if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, v.cur);
+    return;
+  }
+  if (v.nsites > kWarpSites) {  // more sites than LevelBufs::sitev holds: per lane
+    for (;;) {
+      unsigned g = 0;
+      if (lane == 0) g = atomicAdd(&st->ticket, 1u);
+      g = __shfl_sync(0xffffffffu, g, 0);
+      if (g >= v.ngroups) return;
+      cell_group<0>(a, v, g, lane, nullptr);
+    }
+  }
+  const int n = a.n;
+  for (;;) {
+    unsigned idx = 0;
+    if (lane == 0) idx = atomicAdd(&st->ticket, 1u);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= (unsigned)v.nsites) break;
+    const uint32_t e = a.list[idx];
+    const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
+    const int h = a.hint[(size_t)sy * n + sx];
+    const CellSums cs = cell_sums_warp(a, v.bits, n, sx, sy, h ? h : v.W0, v.rb, lane, ws);
+    const unsigned g = idx / 32;
+    int last = 0;
+    if (lane == 0) {
+      float eh = 0.f, el = 0.f;
+      dfa(eh, el, cs.eh, cs.el);
+      const unsigned mv = move_site(a, v, e, sx, sy, cs);
+      a.sitev[idx] = make_float4(eh, el, __uint_as_float((unsigned)cs.r2), __uint_as_float(mv));
+      __threadfence();
+      const unsigned gsize = min(32u, (unsigned)v.nsites - g * 32);
+      last = atomicAdd(a.gcnt + g, 1u) == gsize - 1;
+    }
+    if (!__shfl_sync(0xffffffffu, last, 0)) continue;
+    // the group's last site: its values in lane order, then the usual tail
+    __threadfence();
+    float eh = 0.f, el = 0.f;
+    unsigned r2 = 0, mv = 0;
+    if (g * 32 + lane < (unsigned)v.nsites) {
+      const float4 q = __ldcg(a.sitev + g * 32 + lane);
+      eh = q.x, el = q.y, r2 = __float_as_uint(q.z), mv = __float_as_uint(q.w);
+    }
+    if (lane == 0) a.gcnt[g] = 0u;
+    group_tail<0>(a, v, g, lane, eh, el, r2, mv);
   }
 }
 
@@ -911,6 +1185,7 @@ cudaError_t launch_count(const LevelBufs &b, cudaStream_t s) {
 
 // Persistent grid of the Lloyd kernel: every warp that fits, per device.
 static int g_cell_grid[64] = {};
+static int g_warp_grid[64] = {};  // k_cell_warp: its own carveout and occupancy
 
 cudaError_t cells_configure() {
   int dev = 0;
@@ -951,6 +1226,16 @@ cudaError_t cells_configure() {
       return e;
     per0 = min(per0, per);
   }
+  // one site per warp: its shared scratch (candidates, chunk sums) needs about
+  // 3.3 KB per block with the reserved 1 KB
+  int perw = 0;
+  if ((e = cudaFuncSetAttribute(k_cell_warp, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                50)) != cudaSuccess)
+    return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perw, k_cell_warp, 32, 0)) !=
+      cudaSuccess)
+    return e;
+  g_warp_grid[dev] = sms * max(1, perw);
   g_cell_grid[dev] = sms * max(1, min(per0, per1));
   return cudaSuccess;
 }
@@ -986,6 +1271,10 @@ cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cud
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
   if (grid <= 0 || grid > g_cell_grid[dev]) grid = g_cell_grid[dev];
+  if (moments_only == 0 && b.sitev && b.gcnt && !b.hist[0]) {
+    k_cell_warp<<<min(grid, g_warp_grid[dev]), 32, 0, s>>>(b);
+    return cudaGetLastError();
+  }
   switch (moments_only) {
     case 1: k_cell<1><<<grid, 32, 0, s>>>(b, out4); break;
     case 2: k_cell<2><<<grid, 32, 0, s>>>(b, out4); break;

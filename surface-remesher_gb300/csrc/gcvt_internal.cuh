@@ -18,6 +18,7 @@ constexpr int kNoneBelow = 32767;   // "no site below"
 constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 for
                                     // every entry of gcvt.cu:842-847
 constexpr int kRowsPerBlock = 1;    // rows (one warp each) per row-pass block
+constexpr int kWarpSites = 8192;    // one site per warp up to this many sites
 constexpr int kListWords = 2048;   // bitmap words per site-list block
 constexpr int kMinN = 256;   // n must be a multiple of 256 (S = n/32 >= 8)
 constexpr int kMaxN = 8192;  // row-pass shared memory: 4 rows x 32 KB at 8192
@@ -97,6 +98,11 @@ struct LevelBufs {
   uint64_t *hist[2];
   int *ids[2];
   float *feat;
+  // one site per warp (small problems): per listed site its energy two-float,
+  // cell radius^2 and move^2 until its group is reduced; per group the sites
+  // done (null: lane-per-site only)
+  float4 *sitev;
+  unsigned *gcnt;
 };
 
 __device__ __forceinline__ const uint64_t *cur_bits(const LevelBufs &a) {
@@ -113,6 +119,8 @@ cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, 
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_list(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_count(const LevelBufs &b, cudaStream_t s);
+// MODE 0 runs one site per warp when b.sitev and b.gcnt are set (and no
+// learned-step state is), else one site per lane.
 cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s,
                          int grid = 0);
 int cells_default_grid();

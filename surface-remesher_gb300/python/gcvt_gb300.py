@@ -38,7 +38,7 @@ class GcvtError(RuntimeError):
 class Tuning(ctypes.Structure):
     _fields_ = [("cell_blocks_per_sm", ctypes.c_int), ("hint_slack", ctypes.c_int),
                 ("jfa_tail_halo", ctypes.c_int), ("lloyd_ms", ctypes.c_float),
-                ("jfa_ms", ctypes.c_float)]
+                ("jfa_ms", ctypes.c_float), ("cell_mode", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -245,8 +245,9 @@ class Context:
         _check(self.lib.gcvt_ctx_autotune(self.h, ctypes.byref(t)), "gcvt_ctx_autotune")
         return t.as_dict()
 
-    def set_tuning(self, cell_blocks_per_sm=0, hint_slack=2, jfa_tail_halo=16):
-        t = Tuning(int(cell_blocks_per_sm), int(hint_slack), int(jfa_tail_halo), 0.0, 0.0)
+    def set_tuning(self, cell_blocks_per_sm=0, hint_slack=2, jfa_tail_halo=16, cell_mode=0):
+        t = Tuning(int(cell_blocks_per_sm), int(hint_slack), int(jfa_tail_halo), 0.0, 0.0,
+                   int(cell_mode))
         _check(self.lib.gcvt_ctx_set_tuning(self.h, ctypes.byref(t)), "gcvt_ctx_set_tuning")
 
     def learning(self, enable=True, track_ids=False):
