@@ -209,6 +209,18 @@ int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
 int gcvt_ctx_extract_points(gcvt_ctx *ctx, double scale, double left, double lower, double *xy,
                             int capacity, int *count, int mem);
 
+/* The Delaunay triangulation of the current free sites (the points of
+ * gcvt_ctx_extract_points, same order), computed on the GPU: the Delaunay
+ * half of the CDT stage (main.cpp:229-236, gDel2D's GpuDel::compute on
+ * delaunayInput's points) without the constraint points and segments.  Sites are lattice points, so the
+ * predicates are exact integers; four or more co-circular sites are split by
+ * a fixed symbolic perturbation (rank y * n + x).  Writes min(count,
+ * capacity) triangles (3 point indices each, counter-clockwise) to
+ * triangles and their number to *count; capacity 0 only counts.  Fewer than
+ * three sites, or all collinear: no triangles.  GCVT_ERR_INPUT when a site
+ * has more than 64 Delaunay neighbours. */
+int gcvt_ctx_delaunay(gcvt_ctx *ctx, int32_t *triangles, int capacity, int *count, int mem);
+
 /* ---- batches: many charts, one launch pair per iteration ---------------
  * No reference counterpart: the reference runs one chart per gCVT call.  A
  * batch groups loaded contexts (any mix of sizes, one device); its

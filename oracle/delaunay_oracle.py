@@ -1,0 +1,177 @@
+"""Delaunay checks for lattice sites (TEST INFRASTRUCTURE ONLY).
+
+Only tests/ use this module.  Two parts:
+
+* check(points, tris): restates gDel2D's DelaunayChecker
+  (gDel2D/DelaunayChecker.cpp:27-87 checkEuler, :99-144 checkAdjacency,
+  :146-169 checkOrientation, :171-213 checkDelaunay) in exact integer
+  arithmetic, plus the coverage the reference's checker leaves implicit: the
+  triangles tile the sites' convex hull (their areas sum to the hull's) and
+  every site is a vertex, so the count is 2V - h - 2 (h: sites on the hull).
+* sos_triangulation(points, n): the one Delaunay triangulation that the
+  symbolic perturbation z(q) = |q|^2 + delta(q) picks (delta infinitesimal,
+  infinitely larger for a larger rank y n + x), by brute force over all
+  triples -- small point sets only.
+
+Points are (x, y) lattice coordinates below 2^13, so every determinant fits
+in int64 when taken relative to one of its points.
+"""
+import itertools
+
+import numpy as np
+
+
+def _orient(a, b, c):
+    return (int(b[0]) - int(a[0])) * (int(c[1]) - int(a[1])) - \
+        (int(b[1]) - int(a[1])) * (int(c[0]) - int(a[0]))
+
+
+def _incircle(p, a, b, d):
+    """> 0 when d is strictly inside the circle through p, a, b (CCW)."""
+    r = [(int(q[0]) - int(d[0]), int(q[1]) - int(d[1])) for q in (p, a, b)]
+    m0 = r[1][0] * r[2][1] - r[1][1] * r[2][0]
+    m1 = r[0][0] * r[2][1] - r[0][1] * r[2][0]
+    m2 = r[0][0] * r[1][1] - r[0][1] * r[1][0]
+    z = [x * x + y * y for x, y in r]
+    return z[0] * m0 - z[1] * m1 + z[2] * m2, (m0, m1, m2)
+
+
+def _incircle_many(p, a, b, d):
+    """Vectorised _incircle over the rows of d (int64)."""
+    r0 = p[None, :] - d
+    r1 = a[None, :] - d
+    r2 = b[None, :] - d
+    m0 = r1[:, 0] * r2[:, 1] - r1[:, 1] * r2[:, 0]
+    m1 = r0[:, 0] * r2[:, 1] - r0[:, 1] * r2[:, 0]
+    m2 = r0[:, 0] * r1[:, 1] - r0[:, 1] * r1[:, 0]
+    z0 = (r0 * r0).sum(1)
+    z1 = (r1 * r1).sum(1)
+    z2 = (r2 * r2).sum(1)
+    return z0 * m0 - z1 * m1 + z2 * m2, m0, m1, m2
+
+
+def hull_size(points):
+    """Sites on the boundary of their convex hull (corners and edge points)."""
+    pts = sorted(set(map(tuple, np.asarray(points).tolist())))
+    if len(pts) < 3:
+        return len(pts), []
+
+    def chain(seq):
+        h = []
+        for q in seq:
+            while len(h) >= 2 and _orient(h[-2], h[-1], q) <= 0:
+                h.pop()
+            h.append(q)
+        return h
+    lower, upper = chain(pts), chain(pts[::-1])
+    corners = lower[:-1] + upper[:-1]
+    if len(corners) < 3:
+        return 0, []
+    on = 0
+    for q in pts:
+        for i in range(len(corners)):
+            a, b = corners[i], corners[(i + 1) % len(corners)]
+            if _orient(a, b, q) == 0 and min(a[0], b[0]) <= q[0] <= max(a[0], b[0]) and \
+                    min(a[1], b[1]) <= q[1] <= max(a[1], b[1]):
+                on += 1
+                break
+    return on, corners
+
+
+def check(points, tris):
+    """Raise AssertionError unless tris is a Delaunay triangulation of points
+    (integer (V, 2)); returns a dict of the counts."""
+    pts = np.asarray(points, np.int64)
+    tris = np.asarray(tris, np.int64).reshape(-1, 3)
+    v = len(pts)
+    h, corners = hull_size(pts)
+    if len(corners) < 3:  # collinear or fewer than three sites
+        assert len(tris) == 0, "triangles of collinear sites"
+        return {"vertices": 0, "edges": 0, "triangles": 0, "hull": 0}
+    assert len(tris) == 2 * v - h - 2, f"{len(tris)} triangles, expected {2 * v - h - 2}"
+    assert tris.min() >= 0 and tris.max() < v, "index out of range"
+    # checkOrientation: every triangle counter-clockwise, none flat
+    a, b, c = pts[tris[:, 0]], pts[tris[:, 1]], pts[tris[:, 2]]
+    o = (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
+    assert (o > 0).all(), f"{int((o <= 0).sum())} triangles not counter-clockwise"
+    # coverage: twice the areas sum to twice the hull's area
+    hull2 = sum(_orient(corners[0], corners[i], corners[i + 1]) for i in range(1, len(corners) - 1))
+    assert int(o.sum()) == hull2, "triangles do not tile the hull"
+    # checkAdjacency: each directed edge once; an edge's two triangles face
+    # each other; boundary edges are the hull's
+    opp = {}
+    for t, (i, j, k) in enumerate(tris.tolist()):
+        for e, w in (((i, j), k), ((j, k), i), ((k, i), j)):
+            assert e not in opp, f"directed edge {e} twice"
+            opp[e] = (t, w)
+    edges = {tuple(sorted(e)) for e in opp}
+    # checkEuler: V - E + F = 1 (outer face not counted)
+    used = np.unique(tris)
+    assert len(used) == v, f"{v - len(used)} sites not in any triangle"
+    assert v - len(edges) + len(tris) == 1, "Euler characteristic"
+    # checkDelaunay: no opposite vertex strictly inside a neighbour's circle
+    ties = 0
+    for (i, j), (t, w) in opp.items():
+        if (j, i) not in opp:
+            continue
+        _, x = opp[(j, i)]
+        det, _ = _incircle(pts[i], pts[j], pts[w], pts[x])
+        assert det <= 0, f"edge {(i, j)} not locally Delaunay"
+        ties += det == 0
+    return {"vertices": v, "edges": len(edges), "triangles": len(tris), "hull": h,
+            "cocircular_edges": ties // 2}
+
+
+def sos_in_circle(p, a, b, d, hp, ha, hb, hd):
+    """The perturbed predicate: d inside the circle through p, a, b (CCW)."""
+    det, (m0, m1, m2) = _incircle(p, a, b, d)
+    if det:
+        return det > 0
+    top = max(hp, ha, hb, hd)
+    if top == hp:
+        return m0 > 0
+    if top == ha:
+        return m1 < 0
+    if top == hb:
+        return m2 > 0
+    return m0 - m1 + m2 < 0
+
+
+def sos_triangulation(points, n):
+    """All CCW triangles (sorted rows, smallest index first) whose perturbed
+    circumcircle holds no other site: the triangulation the symbolic
+    perturbation picks.  O(V^4): small sets only."""
+    pts = np.asarray(points, np.int64)
+    rank = pts[:, 1] * n + pts[:, 0]
+    v = len(pts)
+    out = []
+    for i, j, k in itertools.combinations(range(v), 3):
+        o = _orient(pts[i], pts[j], pts[k])
+        if o == 0:
+            continue
+        if o < 0:
+            j, k = k, j
+        others = np.array([q for q in range(v) if q not in (i, j, k)], np.int64)
+        if len(others):
+            det, m0, m1, m2 = _incircle_many(pts[i], pts[j], pts[k], pts[others])
+            if (det > 0).any():
+                continue
+            bad = False
+            for q in others[det == 0].tolist():
+                if sos_in_circle(pts[i], pts[j], pts[k], pts[q], rank[i], rank[j], rank[k],
+                                 rank[q]):
+                    bad = True
+                    break
+            if bad:
+                continue
+        out.append(canonical([(i, j, k)])[0])
+    return np.array(sorted(out), np.int64).reshape(-1, 3)
+
+
+def canonical(tris):
+    """Rotate each CCW triangle to start at its smallest index; sort rows."""
+    rows = []
+    for t in np.asarray(tris).reshape(-1, 3).tolist():
+        r = t.index(min(t))
+        rows.append(tuple(t[r:] + t[:r]))
+    return sorted(rows)

@@ -630,6 +630,42 @@ int gcvt_ctx_extract_points(gcvt_ctx *c, double scale, double left, double lower
   return GCVT_OK;
 }
 
+int gcvt_ctx_delaunay(gcvt_ctx *c, int32_t *triangles, int capacity, int *count, int mem) {
+  if (!c || !count || capacity < 0 || (capacity > 0 && !triangles)) return GCVT_ERR_ARGUMENT;
+  if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  const int n = c->cur_n;
+  const int level = level_of(c, n);
+  const unsigned cap = (unsigned)capacity;
+  int32_t *dst = mem == GCVT_MEM_HOST ? nullptr : triangles;
+  bool owned = false;
+  if (mem == GCVT_MEM_HOST && cap) {
+    // device staging: the label grid's buffer when it holds the triangles
+    if ((size_t)cap * 3 * sizeof(int32_t) <= (size_t)c->n_max * c->n_max * sizeof(uint32_t)) {
+      dst = reinterpret_cast<int32_t *>(c->grid);
+    } else {
+      if (cudaMalloc(reinterpret_cast<void **>(&dst), (size_t)cap * 3 * sizeof(int32_t)) !=
+          cudaSuccess)
+        return GCVT_ERR_ALLOC;
+      owned = true;
+    }
+  }
+  unsigned total = 0;
+  rc = delaunay_sites(c->bits[c->st_host->cur], c->fixed_bits[level], n, dst, cap, &total,
+                      c->stream);
+  if (!rc) {
+    *count = (int)total;
+    const size_t written = total < cap ? total : cap;
+    if (mem == GCVT_MEM_HOST && written)
+      rc = copy_out(triangles, dst, written * 3 * sizeof(int32_t), GCVT_MEM_HOST, c->stream);
+  }
+  if (owned) cudaFree(dst);
+  return rc;
+}
+
 int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, int mem) {
   if (!c || (!labels && !stats)) return GCVT_ERR_ARGUMENT;
   if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;

@@ -1,0 +1,693 @@
+// delaunay.cu -- the Delaunay triangulation of a context's free sites on the
+// GPU, in the point order of delaunayInput (delaunay.h:46-57), so that its
+// triangles index gcvt_ctx_extract_points' list and feed gcvt_lift.  This is
+// the Delaunay part of the reference's CDT stage (gDel2D,
+// gDel2D/GPU/GpuDelaunay.cu:46) for the CVT sites; constraint points and
+// segments are not inserted.
+//
+// Sites lie on the integer pixel lattice, so every predicate is exact in
+// 64-bit / 128-bit integers.  Co-circular sites (common on a lattice) are
+// resolved by symbolic perturbation of the lifting map (simulation of
+// simplicity): z(q) = |q|^2 + delta(q), with delta(q) > 0 infinitesimal and
+// infinitely larger for a larger rank h(q) = y n + x.  The perturbed lifted
+// points are in general position, so their lower hull is one Delaunay
+// triangulation of the sites, and every site that evaluates a predicate
+// gets the same sign, so all stars agree.
+//
+// Each site computes its own Delaunay star (its neighbours in angular order)
+// from the sites in a window around it: inverted about the site, the star is
+// the part of the candidates' convex hull facing away from the site, so the
+// candidates are inserted one by one into a sorted cyclic list (a candidate
+// inside the current hull never becomes a neighbour later; an inserted one
+// removes the neighbours it covers).  Certificate, exact: a triangle of the
+// star is final when no site outside the window lies in its circumcircle,
+// an open angular gap (>= pi) when no site lies strictly inside its cone
+// (then the site is on the sites' convex hull); both are searched through a
+// pyramid of tile occupancy, and a site found is inserted and the star
+// checked again.  Only a star of fewer than two neighbours widens the
+// window (a window covering the grid is exact).  Threads take the sites in
+// tile order (nearby sites share a warp); a triangle is written by its
+// vertex that comes first in delaunayInput's order (x, then y), counter-
+// clockwise, so the output does not depend on the scheduling.
+#include "gcvt_internal.cuh"
+#include "../../include/gcvt_gb300.h"
+
+#include <climits>
+
+namespace cvtgb {
+
+namespace {
+
+constexpr int kStar = 64;  // Delaunay neighbours a site can hold
+
+__device__ __forceinline__ int pk(int dx, int dy) { return (int)((unsigned)(dx & 0xffff) | ((unsigned)dy << 16)); }
+__device__ __forceinline__ int pdx(int v) { return (int)(int16_t)(v & 0xffff); }
+__device__ __forceinline__ int pdy(int v) { return v >> 16; }
+
+__device__ __forceinline__ long long cross(int ax, int ay, int bx, int by) {
+  return (long long)ax * by - (long long)ay * bx;
+}
+
+// angular order around the site: half 0 = [0, pi), half 1 = [pi, 2 pi)
+__device__ __forceinline__ int half_of(int x, int y) { return (y > 0 || (y == 0 && x > 0)) ? 0 : 1; }
+
+// a strictly before b in angle (same ray: not before)
+__device__ __forceinline__ bool ang_less(int ax, int ay, int bx, int by) {
+  const int ha = half_of(ax, ay), hb = half_of(bx, by);
+  if (ha != hb) return ha < hb;
+  return cross(ax, ay, bx, by) > 0;
+}
+
+// the CCW angle from a to b is >= pi (b not strictly left of a, and not the
+// same ray)
+__device__ __forceinline__ bool open_gap(int ax, int ay, int bx, int by) {
+  const long long c = cross(ax, ay, bx, by);
+  if (c > 0) return false;
+  if (c < 0) return true;
+  return (long long)ax * bx + (long long)ay * by < 0;  // opposite rays: exactly pi
+}
+
+// Perturbed incircle: is d strictly inside the circle through the site
+// (origin), a and b (counter-clockwise)?  Coordinates relative to the site;
+// hp, ha, hb, hd the perturbation keys h(q) = y n + x.
+__device__ bool in_circle(int ax, int ay, int bx, int by, int dx, int dy, long long hp,
+                          long long ha, long long hb, long long hd) {
+  // rows: p - d, a - d, b - d (p = origin)
+  const long long r0x = -dx, r0y = -dy, r1x = ax - dx, r1y = ay - dy, r2x = bx - dx,
+                  r2y = by - dy;
+  const long long m0 = r1x * r2y - r1y * r2x;  // cofactor of row 0
+  const long long m1 = r0x * r2y - r0y * r2x;
+  const long long m2 = r0x * r1y - r0y * r1x;
+  const long long z0 = r0x * r0x + r0y * r0y, z1 = r1x * r1x + r1y * r1y,
+                  z2 = r2x * r2x + r2y * r2y;
+  const __int128 d0 = (__int128)z0 * m0 - (__int128)z1 * m1 + (__int128)z2 * m2;
+  if (d0 != 0) return d0 > 0;
+  // co-circular: z(q) += delta(q), delta growing (infinitesimally) with
+  // h(q); the determinant is linear in the z column, so the sign is that of
+  // the top-ranked point's cofactor (none is zero: no three of four
+  // co-circular points are collinear)
+  if (hp > ha && hp > hb && hp > hd) return m0 > 0;
+  if (ha > hb && ha > hd) return m1 < 0;
+  if (hb > hd) return m2 > 0;
+  return m0 - m1 + m2 < 0;
+}
+
+struct Star {
+  int nb[kStar];  // packed (dx, dy), angular order
+  int m;
+  bool overflow;
+};
+
+__device__ __forceinline__ long long hkey(int n, int x, int y) { return (long long)y * n + x; }
+
+// Insert candidate q (relative (qx, qy)) into the star of site (sx, sy).
+// The star is sorted by angle from the +x axis; inverted about the site, its
+// neighbours are the hull vertices facing away from the site, and a
+// candidate inside that hull never becomes one later (the hull only grows).
+__device__ void star_insert(Star &st, int n, int sx, int sy, int qx, int qy) {
+  const long long hp = hkey(n, sx, sy), hq = hkey(n, sx + qx, sy + qy);
+  // a neighbour on the same ray: the nearer one wins (the farther one is
+  // strictly inside every circle through the site and the nearer one)
+  for (int k = 0; k < st.m; ++k) {
+    const int ux = pdx(st.nb[k]), uy = pdy(st.nb[k]);
+    if (cross(ux, uy, qx, qy) == 0 && (long long)ux * qx + (long long)uy * qy > 0) {
+      if ((long long)qx * qx + (long long)qy * qy >= (long long)ux * ux + (long long)uy * uy)
+        return;
+      for (int j = k; j + 1 < st.m; ++j) st.nb[j] = st.nb[j + 1];
+      --st.m;
+      break;
+    }
+  }
+  int m = st.m;
+  // position: neighbours [0, pos) come before q in angle
+  int pos = 0;
+  while (pos < m && ang_less(pdx(st.nb[pos]), pdy(st.nb[pos]), qx, qy)) ++pos;
+  if (m >= 2) {
+    const int u = st.nb[(pos + m - 1) % m], w = st.nb[pos % m];
+    const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
+    if (!open_gap(ux, uy, wx, wy) &&
+        !in_circle(ux, uy, wx, wy, qx, qy, hp, hkey(n, sx + ux, sy + uy),
+                   hkey(n, sx + wx, sy + wy), hq))
+      return;  // inside the hull: never a neighbour
+  }
+  if (m >= kStar) {
+    st.overflow = true;
+    return;
+  }
+  for (int k = m; k > pos; --k) st.nb[k] = st.nb[k - 1];
+  const int qv = pk(qx, qy);
+  st.nb[pos] = qv;
+  st.m = ++m;
+  // neighbours q now covers: clockwise of q, then counter-clockwise
+  for (;;) {
+    m = st.m;
+    if (m < 3) break;
+    int iq = 0;
+    while (st.nb[iq] != qv) ++iq;
+    const int iu = (iq + m - 1) % m, u = st.nb[iu], uu = st.nb[(iq + m - 2) % m];
+    const int ax = pdx(uu), ay = pdy(uu), vx = pdx(u), vy = pdy(u);
+    if (open_gap(ax, ay, qx, qy) ||
+        in_circle(ax, ay, qx, qy, vx, vy, hp, hkey(n, sx + ax, sy + ay), hq,
+                  hkey(n, sx + vx, sy + vy)))
+      break;
+    for (int k = iu; k + 1 < m; ++k) st.nb[k] = st.nb[k + 1];
+    --st.m;
+  }
+  for (;;) {
+    m = st.m;
+    if (m < 3) break;
+    int iq = 0;
+    while (st.nb[iq] != qv) ++iq;
+    const int iw = (iq + 1) % m, w = st.nb[iw], ww = st.nb[(iq + 2) % m];
+    const int bx = pdx(ww), by = pdy(ww), vx = pdx(w), vy = pdy(w);
+    if (open_gap(qx, qy, bx, by) ||
+        in_circle(qx, qy, bx, by, vx, vy, hp, hq, hkey(n, sx + bx, sy + by),
+                  hkey(n, sx + vx, sy + vy)))
+      break;
+    for (int k = iw; k + 1 < m; ++k) st.nb[k] = st.nb[k + 1];
+    --st.m;
+  }
+}
+
+// Is every grid point in the closed circumdisc of (site, u, w) inside the
+// window?  Relative to the site: centre (Nx, Ny) / D (D > 0), radius^2
+// (Nx^2 + Ny^2) / D^2 (the circle passes through the site).  The grid
+// outside the window [x0, x1] x [y0, y1] is up to four strips; the disc
+// must stay strictly clear of each (exact in 128-bit integers).
+__device__ __forceinline__ __int128 axis_gap(long long N, long long D, int lo, int hi) {
+  const __int128 a = (__int128)lo * D - N, b = (__int128)N - (__int128)hi * D;
+  return a > 0 ? a : (b > 0 ? b : (__int128)0);
+}
+__device__ bool clear_of(long long Nx, long long Ny, long long D, int lx, int hx, int ly, int hy) {
+  if (lx > hx || ly > hy) return true;  // empty strip
+  const __int128 gx = axis_gap(Nx, D, lx, hx), gy = axis_gap(Ny, D, ly, hy);
+  return gx * gx + gy * gy > (__int128)Nx * Nx + (__int128)Ny * Ny;
+}
+__device__ bool disc_in_window(int ux, int uy, int wx, int wy, int sx, int sy, int x0, int x1,
+                               int y0, int y1, int n) {
+  const long long u2 = (long long)ux * ux + (long long)uy * uy,
+                  w2 = (long long)wx * wx + (long long)wy * wy;
+  const long long D = 2 * cross(ux, uy, wx, wy);
+  const long long Nx = wy * u2 - uy * w2, Ny = ux * w2 - wx * u2;
+  const int gx0 = -sx, gx1 = n - 1 - sx, gy0 = -sy, gy1 = n - 1 - sy;  // the grid
+  const int wx0 = x0 - sx, wx1 = x1 - sx, wy0 = y0 - sy, wy1 = y1 - sy;  // the window
+  return clear_of(Nx, Ny, D, gx0, wx0 - 1, gy0, gy1) && clear_of(Nx, Ny, D, wx1 + 1, gx1, gy0, gy1) &&
+         clear_of(Nx, Ny, D, wx0, wx1, gy0, wy0 - 1) && clear_of(Nx, Ny, D, wx0, wx1, wy1 + 1, gy1);
+}
+
+// Site occupancy of 16 x 16 pixel tiles and its pyramid (level l: tiles of
+// 16 << l pixels, a byte each, nonzero when the tile holds a site).
+constexpr int kTile = 16;  // 1 << 4
+constexpr int kLevels = 16;
+struct Pyr {
+  const uint8_t *occ;
+  int off[kLevels], nt[kLevels];
+  int top;  // the one-node level
+};
+
+// Free sites: bits & ~fixed.
+__device__ __forceinline__ uint64_t free_word(const uint64_t *bits, const uint64_t *fixed,
+                                              size_t i) {
+  return fixed ? bits[i] & ~fixed[i] : bits[i];
+}
+
+// Insert the free sites of column x, rows [ya, yb] (the site itself left out).
+__device__ void insert_column(Star &st, const uint64_t *bits, const uint64_t *fixed, int n,
+                              int sx, int sy, int x, int ya, int yb) {
+  for (int b = ya / kBand; b <= yb / kBand; ++b) {
+    const int lo = max(ya - b * kBand, 0), hi = min(yb - b * kBand, 63);
+    const uint64_t up = hi >= 63 ? ~0ull : ((2ull << hi) - 1ull);
+    uint64_t w = free_word(bits, fixed, (size_t)b * n + x) & up & ~((1ull << lo) - 1ull);
+    while (w) {
+      const int i = __ffsll((long long)w) - 1;
+      w &= w - 1ull;
+      const int qx = x - sx, qy = b * kBand + i - sy;
+      if (qx != 0 || qy != 0) star_insert(st, n, sx, sy, qx, qy);
+    }
+  }
+}
+
+// The sites outside the window in the circumcircle of the star's triangle
+// (site, u, w): the occupancy pyramid is descended to the 16 x 16 tiles
+// outside the (tile-aligned) window that the closed circumdisc meets, and
+// their sites are tested with the perturbed predicate.  The first site
+// inside is inserted into the star (returns true: the triangle is gone);
+// false when the triangle is final.
+__device__ bool disc_scan(Star &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                          int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                          int y0, int y1) {
+  if (disc_in_window(ux, uy, wx, wy, sx, sy, x0, x1, y0, y1, n)) return false;
+  const long long u2 = (long long)ux * ux + (long long)uy * uy,
+                  w2 = (long long)wx * wx + (long long)wy * wy;
+  const long long D = 2 * cross(ux, uy, wx, wy);
+  const long long Nx = wy * u2 - uy * w2, Ny = ux * w2 - wx * u2;
+  const long long hp = hkey(n, sx, sy), hu = hkey(n, sx + ux, sy + uy),
+                  hw = hkey(n, sx + wx, sy + wy);
+  // start at the pyramid level where the disc's bounding box (FP64, one
+  // pixel of slack, clipped to the grid) spans at most 2 x 2 nodes
+  const double cx = (double)Nx / (double)D, cy = (double)Ny / (double)D;
+  const double r = sqrt(cx * cx + cy * cy) + 1.0;
+  const int bx0 = (int)fmax(0.0, floor(sx + cx - r)), bx1 = (int)fmin(n - 1.0, ceil(sx + cx + r));
+  const int by0 = (int)fmax(0.0, floor(sy + cy - r)), by1 = (int)fmin(n - 1.0, ceil(sy + cy + r));
+  int l0 = 0;
+  while (l0 < py.top && (((bx1 >> (4 + l0)) - (bx0 >> (4 + l0))) > 1 ||
+                         ((by1 >> (4 + l0)) - (by0 >> (4 + l0))) > 1))
+    ++l0;
+  unsigned stk[4 * kLevels];
+  int sp = 0;
+  for (int ty = by0 >> (4 + l0); ty <= by1 >> (4 + l0); ++ty)
+    for (int tx = bx0 >> (4 + l0); tx <= bx1 >> (4 + l0); ++tx)
+      stk[sp++] = ((unsigned)l0 << 28) | ((unsigned)tx << 14) | (unsigned)ty;
+  while (sp) {
+    const unsigned v = stk[--sp];
+    const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
+    if (!py.occ[py.off[l] + ty * py.nt[l] + tx]) continue;
+    const int S = kTile << l;
+    const int px0 = tx * S, px1 = px0 + S - 1, qy0 = ty * S, qy1 = qy0 + S - 1;
+    if (px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) continue;  // inside the window
+    if (clear_of(Nx, Ny, D, px0 - sx, px1 - sx, qy0 - sy, qy1 - sy)) continue;
+    if (l > 0) {
+      const int cn = py.nt[l - 1];
+      for (int c = 0; c < 4; ++c) {
+        const int cx = 2 * tx + (c & 1), cy = 2 * ty + (c >> 1);
+        if (cx < cn && cy < cn)
+          stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
+      }
+      continue;
+    }
+    // a 16 x 16 tile: its sites, by the exact predicate
+    const int b = qy0 / kBand, sh = qy0 % kBand;
+    for (int x = px0; x <= min(px1, n - 1); ++x) {
+      uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
+      while (w) {
+        const int i = __ffsll((long long)w) - 1;
+        w &= w - 1ull;
+        const int qx = x - sx, qy = qy0 + i - sy;
+        if ((qx == ux && qy == uy) || (qx == wx && qy == wy)) continue;
+        if (in_circle(ux, uy, wx, wy, qx, qy, hp, hu, hw, hkey(n, sx + qx, sy + qy))) {
+          star_insert(st, n, sx, sy, qx, qy);
+          return true;
+        }
+      }
+    }
+  }
+  return false;
+}
+
+// The sites outside the window strictly inside the open angular gap from u
+// to w (counter-clockwise, >= pi): the cone {q : u x q > 0 or q x w > 0}.
+// The first one found is inserted (returns true); false when the cone holds
+// no site, so the site is on the sites' convex hull and the gap is final.
+__device__ bool cone_scan(Star &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                          int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                          int y0, int y1) {
+  unsigned stk[4 * kLevels];
+  int sp = 0;
+  stk[sp++] = (unsigned)py.top << 28;
+  while (sp) {
+    const unsigned v = stk[--sp];
+    const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
+    if (!py.occ[py.off[l] + ty * py.nt[l] + tx]) continue;
+    const int S = kTile << l;
+    const int px0 = tx * S, px1 = min(px0 + S, n) - 1, qy0 = ty * S, qy1 = min(qy0 + S, n) - 1;
+    if (px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) continue;  // inside the window
+    // the cross products are linear: their largest value is at a corner
+    long long cu = LLONG_MIN, cw = LLONG_MIN;
+    for (int c = 0; c < 4; ++c) {
+      const int qx = ((c & 1) ? px1 : px0) - sx, qy = ((c >> 1) ? qy1 : qy0) - sy;
+      cu = max(cu, cross(ux, uy, qx, qy));
+      cw = max(cw, cross(qx, qy, wx, wy));
+    }
+    if (cu <= 0 && cw <= 0) continue;
+    if (l > 0) {
+      const int cn = py.nt[l - 1];
+      for (int c = 0; c < 4; ++c) {
+        const int cx = 2 * tx + (c & 1), cy = 2 * ty + (c >> 1);
+        if (cx < cn && cy < cn)
+          stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
+      }
+      continue;
+    }
+    const int b = qy0 / kBand, sh = qy0 % kBand;
+    for (int x = px0; x <= px1; ++x) {
+      uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
+      while (w) {
+        const int i = __ffsll((long long)w) - 1;
+        w &= w - 1ull;
+        const int qx = x - sx, qy = qy0 + i - sy;
+        if (cross(ux, uy, qx, qy) > 0 || cross(qx, qy, wx, wy) > 0) {
+          star_insert(st, n, sx, sy, qx, qy);
+          return true;
+        }
+      }
+    }
+  }
+  return false;
+}
+
+// The Delaunay star of site (sx, sy).  The window is the site's tile and
+// k = 1, 2, 4 ... tiles around it; each step inserts only the sites of the
+// new ring (nearer sites first keeps the intermediate stars small), then
+// tries the certificate.  Returns false when the star overflowed.
+__device__ bool site_star(Star &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
+                          int sy, const Pyr &py) {
+  st.m = 0;
+  st.overflow = false;
+  const int tx = sx / kTile, ty = sy / kTile;
+  int k = 0, x0 = sx, x1 = sx, y0 = sy, y1 = sy;
+  for (;;) {
+    k = k ? 2 * k : 1;
+    const int nx0 = max(0, (tx - k) * kTile), nx1 = min(n - 1, (tx + k + 1) * kTile - 1);
+    const int ny0 = max(0, (ty - k) * kTile), ny1 = min(n - 1, (ty + k + 1) * kTile - 1);
+    for (int x = nx0; x <= nx1; ++x) {
+      if (x < x0 || x > x1) {
+        insert_column(st, bits, fixed, n, sx, sy, x, ny0, ny1);
+      } else {
+        if (ny0 < y0) insert_column(st, bits, fixed, n, sx, sy, x, ny0, y0 - 1);
+        if (y1 < ny1) insert_column(st, bits, fixed, n, sx, sy, x, y1 + 1, ny1);
+      }
+    }
+    x0 = nx0;
+    x1 = nx1;
+    y0 = ny0;
+    y1 = ny1;
+    if (st.overflow) return false;
+    if (x0 == 0 && y0 == 0 && x1 == n - 1 && y1 == n - 1) return true;  // every site seen
+    // certificate, exact: the sites inside a triangle's circumcircle or an
+    // open gap's cone are inserted until there are none
+    bool ok, changed;
+    int rounds = 0;
+    do {
+      if (++rounds > (1 << 20)) {  // more insertions than any star needs: give up
+        st.overflow = true;
+        return false;
+      }
+      changed = false;
+      const int m = st.m;
+      ok = m > 0;
+      for (int j = 0; j < m && ok; ++j) {
+        const int u = st.nb[j], w = st.nb[(j + 1) % m];
+        const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
+        if (m < 2) {
+          ok = false;  // fewer than two neighbours: a wider window
+        } else if (open_gap(ux, uy, wx, wy)
+                       ? cone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)
+                       : disc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)) {
+          changed = true;
+          break;
+        }
+      }
+      if (st.overflow) return false;
+    } while (changed);
+    if (ok) return true;
+  }
+}
+
+// Tiles are visited in bricks of 4 x 4 (64 x 64 pixels), so that the sites
+// a warp handles lie close together and their windows overlap.
+constexpr int kBrick = 4;
+__device__ __forceinline__ int brick_of(int tx, int ty, int nt0) {
+  return ((ty / kBrick) * (nt0 / kBrick) + tx / kBrick) * (kBrick * kBrick) +
+         (ty % kBrick) * kBrick + tx % kBrick;
+}
+
+// Sites per tile (brick order) and level 0 of the occupancy pyramid: one
+// thread per (column, 64-row band).
+__global__ void k_dt_tiles(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
+                           int n, uint8_t *occ0, int nt0, unsigned *tcnt) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = n / kBand;
+  if (i >= (long long)nb * n) return;
+  const int b = (int)(i / n), x = (int)(i % n);
+  const uint64_t w = free_word(bits, fixed, (size_t)b * n + x);
+  for (int q = 0; q < kBand / kTile; ++q) {
+    const unsigned c = (unsigned)__popcll((w >> (q * kTile)) & 0xffffull);
+    if (c) {
+      const int ty = b * (kBand / kTile) + q, tx = x / kTile;
+      occ0[ty * nt0 + tx] = 1;
+      atomicAdd(&tcnt[brick_of(tx, ty, nt0)], c);
+    }
+  }
+}
+
+// Level l from level l - 1.
+__global__ void k_dt_up(const uint8_t *__restrict__ lo, int nlo, uint8_t *hi, int nhi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nhi * nhi) return;
+  const int x = i % nhi, y = i / nhi;
+  uint8_t v = 0;
+  for (int c = 0; c < 4; ++c) {
+    const int cx = 2 * x + (c & 1), cy = 2 * y + (c >> 1);
+    if (cx < nlo && cy < nlo) v |= lo[cy * nlo + cx];
+  }
+  hi[i] = v;
+}
+
+// Per column: free sites in the bands before each band, and in the column.
+// One warp per 32 columns; the band loop is unrolled so the loads overlap.
+__global__ void k_dt_columns(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
+                             int n, unsigned *colpre, unsigned *colcnt) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= n) return;
+  unsigned c = 0;
+#pragma unroll 8
+  for (int b = 0; b < n / kBand; ++b) {
+    colpre[(size_t)b * n + x] = c;
+    c += __popcll(free_word(bits, fixed, (size_t)b * n + x));
+  }
+  colcnt[x] = c;
+}
+
+// The sites in tile order: one thread per tile (brick order), its sites by
+// column, then row.
+__global__ void k_dt_order(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
+                           int n, int nt0, const unsigned *__restrict__ toff, int *order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt0 * nt0) return;
+  const int brick = i / (kBrick * kBrick), in = i % (kBrick * kBrick);
+  const int tx = (brick % (nt0 / kBrick)) * kBrick + in % kBrick;
+  const int ty = (brick / (nt0 / kBrick)) * kBrick + in / kBrick;
+  const int y0 = ty * kTile, b = y0 / kBand, sh = y0 % kBand;
+  unsigned pos = toff[i];
+  for (int x = tx * kTile; x < tx * kTile + kTile; ++x) {
+    uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
+    while (w) {
+      const int k = __ffsll((long long)w) - 1;
+      w &= w - 1ull;
+      order[pos++] = pk(x, y0 + k);
+    }
+  }
+}
+
+__device__ __forceinline__ int site_index(const uint64_t *bits, const uint64_t *fixed, int n,
+                                          const unsigned *coloff, const unsigned *colpre, int x,
+                                          int y) {
+  const int b = y / kBand, i = y % kBand;
+  const uint64_t w = free_word(bits, fixed, (size_t)b * n + x);
+  const uint64_t below = i ? (w & ((1ull << i) - 1ull)) : 0ull;
+  return (int)(coloff[x] + colpre[(size_t)b * n + x] + (unsigned)__popcll(below));
+}
+
+// The star of the t-th site in tile order, stored under its index in
+// delaunayInput's order with the number of triangles it writes.
+__global__ void k_dt_star(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
+                          int n, const int *__restrict__ order, int nsites, Pyr py,
+                          const unsigned *__restrict__ coloff, const unsigned *__restrict__ colpre,
+                          int *sitepos, int *stars, int *degree, unsigned *tcount, int *err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsites) return;
+  const int sx = pdx(order[t]) & 0xffff, sy = pdy(order[t]);
+  const int xm = site_index(bits, fixed, n, coloff, colpre, sx, sy);
+  sitepos[xm] = order[t];
+  Star st;
+  if (!site_star(st, bits, fixed, n, sx, sy, py)) {
+    atomicOr(err, 1);
+    degree[xm] = 0;
+    tcount[xm] = 0;
+    return;
+  }
+  const int m = st.m;
+  unsigned own = 0;
+  for (int k = 0; k < m; ++k) {
+    stars[(size_t)xm * kStar + k] = st.nb[k];
+    const int u = st.nb[k], w = st.nb[(k + 1) % m];
+    if (m < 2 || open_gap(pdx(u), pdy(u), pdx(w), pdy(w))) continue;
+    // written by the vertex first in (x, y) order
+    const int ux = sx + pdx(u), uy = sy + pdy(u), wx = sx + pdx(w), wy = sy + pdy(w);
+    const bool first = (sx < ux || (sx == ux && sy < uy)) && (sx < wx || (sx == wx && sy < wy));
+    own += first;
+  }
+  degree[xm] = m;
+  tcount[xm] = own;
+}
+
+__global__ void k_dt_emit(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
+                          int n, const int *__restrict__ sitepos, int nsites,
+                          const unsigned *__restrict__ coloff, const unsigned *__restrict__ colpre,
+                          const int *__restrict__ stars, const int *__restrict__ degree,
+                          const unsigned *__restrict__ toff, int *tris, unsigned cap) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsites) return;
+  const int sx = pdx(sitepos[t]) & 0xffff, sy = pdy(sitepos[t]);
+  const int m = degree[t];
+  unsigned pos = toff[t];
+  for (int k = 0; k < m; ++k) {
+    const int u = stars[(size_t)t * kStar + k], w = stars[(size_t)t * kStar + (k + 1) % m];
+    if (m < 2 || open_gap(pdx(u), pdy(u), pdx(w), pdy(w))) continue;
+    const int ux = sx + pdx(u), uy = sy + pdy(u), wx = sx + pdx(w), wy = sy + pdy(w);
+    const bool first = (sx < ux || (sx == ux && sy < uy)) && (sx < wx || (sx == wx && sy < wy));
+    if (!first) continue;
+    if (pos < cap) {
+      tris[3 * (size_t)pos] = t;
+      tris[3 * (size_t)pos + 1] = site_index(bits, fixed, n, coloff, colpre, ux, uy);
+      tris[3 * (size_t)pos + 2] = site_index(bits, fixed, n, coloff, colpre, wx, wy);
+    }
+    ++pos;
+  }
+}
+
+// Exclusive scan of large count arrays: blocks of 4096 counts scanned in
+// shared memory, the block totals by launch_scan, then the block offsets
+// added (offset[n] = total).
+constexpr int kScanBlock = 4096;
+__global__ void __launch_bounds__(1024) k_scan_local(const unsigned *__restrict__ count, int n,
+                                                     unsigned *offset, unsigned *total) {
+  __shared__ unsigned v[kScanBlock];
+  __shared__ unsigned wsum[32];
+  const int base = blockIdx.x * kScanBlock, t = threadIdx.x;
+  for (int k = t; k < kScanBlock; k += 1024) v[k] = base + k < n ? count[base + k] : 0u;
+  __syncthreads();
+  const unsigned a0 = v[4 * t], a1 = v[4 * t + 1], a2 = v[4 * t + 2], a3 = v[4 * t + 3];
+  const unsigned sum = a0 + a1 + a2 + a3;
+  unsigned inc = sum;  // inclusive scan over the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+    if ((t & 31) >= o) inc += y;
+  }
+  if ((t & 31) == 31) wsum[t >> 5] = inc;
+  __syncthreads();
+  if (t < 32) {
+    unsigned w = wsum[t], wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (t >= o) wi += y;
+    }
+    wsum[t] = wi - w;
+    if (t == 31) total[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  const unsigned ex = wsum[t >> 5] + inc - sum;
+  v[4 * t] = ex;
+  v[4 * t + 1] = ex + a0;
+  v[4 * t + 2] = ex + a0 + a1;
+  v[4 * t + 3] = ex + a0 + a1 + a2;
+  __syncthreads();
+  for (int k = t; k < kScanBlock; k += 1024)
+    if (base + k < n) offset[base + k] = v[k];
+}
+
+__global__ void k_scan_add(unsigned *offset, int n, const unsigned *__restrict__ boff, int nblock) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) offset[i] += boff[i / kScanBlock];
+  if (i == 0) offset[n] = boff[nblock];
+}
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+#define DCK(call)                                 \
+  do {                                            \
+    if ((call) != cudaSuccess) return GCVT_ERR_CUDA; \
+  } while (0)
+
+// Exclusive scan of count[0..n) into offset[0..n] (n >= 1).
+int scan_big(const unsigned *count, int n, unsigned *offset, Scratch &sc, cudaStream_t s) {
+  const int nblock = (n + kScanBlock - 1) / kScanBlock;
+  unsigned *tot = sc.take<unsigned>(nblock), *boff = sc.take<unsigned>(nblock + 1),
+           *cur = sc.take<unsigned>(nblock);
+  if (!tot || !boff || !cur) return GCVT_ERR_ALLOC;
+  k_scan_local<<<nblock, 1024, 0, s>>>(count, n, offset, tot);
+  DCK(cudaGetLastError());
+  DCK(launch_scan(reinterpret_cast<const int *>(tot), nblock, reinterpret_cast<int *>(boff),
+                  reinterpret_cast<int *>(cur), s));
+  k_scan_add<<<nblk(n, 256), 256, 0, s>>>(offset, n, boff, nblock);
+  DCK(cudaGetLastError());
+  return GCVT_OK;
+}
+
+}  // namespace
+
+// The Delaunay triangles of the free sites of `bits` (n x n, n a multiple of
+// 64), as indices into delaunayInput's point order; host-synchronous on `s`.
+int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris, unsigned cap,
+                   unsigned *ntris, cudaStream_t s) {
+  *ntris = 0;
+  if (n <= 0 || n % kBand) return GCVT_ERR_ARGUMENT;
+  Scratch sc;
+  const size_t nb = (size_t)(n / kBand) * n;
+  const int nt0 = n / kTile, ntiles = nt0 * nt0;
+  unsigned *colpre = sc.take<unsigned>(nb), *colcnt = sc.take<unsigned>(n),
+           *coloff = sc.take<unsigned>(n + 1), *cur = sc.take<unsigned>(n),
+           *tilecnt = sc.take<unsigned>(ntiles), *tileoff = sc.take<unsigned>(ntiles + 1);
+  int *err = sc.take<int>(1);
+  Pyr py{};
+  size_t occ_bytes = 0;
+  for (int l = 0, t = nt0;; ++l, t = (t + 1) / 2) {
+    if (l >= kLevels) return GCVT_ERR_ARGUMENT;
+    py.off[l] = (int)occ_bytes;
+    py.nt[l] = t;
+    occ_bytes += (size_t)t * t;
+    if (t == 1) {
+      py.top = l;
+      break;
+    }
+  }
+  uint8_t *occ = sc.take<uint8_t>(occ_bytes);
+  py.occ = occ;
+  if (!colpre || !colcnt || !coloff || !cur || !tilecnt || !tileoff || !err || !occ)
+    return GCVT_ERR_ALLOC;
+  DCK(cudaMemsetAsync(err, 0, sizeof(int), s));
+  DCK(cudaMemsetAsync(occ, 0, occ_bytes, s));
+  DCK(cudaMemsetAsync(tilecnt, 0, (size_t)ntiles * sizeof(unsigned), s));
+  k_dt_columns<<<nblk(n, 64), 64, 0, s>>>(bits, fixed, n, colpre, colcnt);
+  DCK(cudaGetLastError());
+  k_dt_tiles<<<nblk((long long)nb, 256), 256, 0, s>>>(bits, fixed, n, occ, nt0, tilecnt);
+  DCK(cudaGetLastError());
+  for (int l = 1; l <= py.top; ++l) {
+    k_dt_up<<<nblk((long long)py.nt[l] * py.nt[l], 256), 256, 0, s>>>(
+        occ + py.off[l - 1], py.nt[l - 1], occ + py.off[l], py.nt[l]);
+    DCK(cudaGetLastError());
+  }
+  DCK(launch_scan(reinterpret_cast<const int *>(colcnt), n, reinterpret_cast<int *>(coloff),
+                  reinterpret_cast<int *>(cur), s));
+  int rc = scan_big(tilecnt, ntiles, tileoff, sc, s);
+  if (rc) return rc;
+  unsigned nsites_u = 0;
+  DCK(cudaMemcpyAsync(&nsites_u, coloff + n, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  DCK(cudaStreamSynchronize(s));
+  const int nsites = (int)nsites_u;
+  if (nsites < 3) return GCVT_OK;
+  int *order = sc.take<int>(nsites), *sitepos = sc.take<int>(nsites),
+      *stars = sc.take<int>((size_t)nsites * kStar), *degree = sc.take<int>(nsites);
+  unsigned *tcnt = sc.take<unsigned>(nsites), *toff = sc.take<unsigned>(nsites + 1);
+  if (!order || !sitepos || !stars || !degree || !tcnt || !toff) return GCVT_ERR_ALLOC;
+  k_dt_order<<<nblk(ntiles, 128), 128, 0, s>>>(bits, fixed, n, nt0, tileoff, order);
+  DCK(cudaGetLastError());
+  k_dt_star<<<nblk(nsites, 128), 128, 0, s>>>(bits, fixed, n, order, nsites, py, coloff, colpre,
+                                              sitepos, stars, degree, tcnt, err);
+  DCK(cudaGetLastError());
+  if ((rc = scan_big(tcnt, nsites, toff, sc, s))) return rc;
+  if (tris && cap) {
+    k_dt_emit<<<nblk(nsites, 128), 128, 0, s>>>(bits, fixed, n, sitepos, nsites, coloff, colpre,
+                                                stars, degree, toff, tris, cap);
+    DCK(cudaGetLastError());
+  }
+  unsigned h[2] = {0, 0};
+  DCK(cudaMemcpyAsync(&h[0], toff + nsites, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  DCK(cudaMemcpyAsync(&h[1], err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  DCK(cudaStreamSynchronize(s));
+  if (h[1]) return GCVT_ERR_INPUT;
+  *ntris = h[0];
+  return GCVT_OK;
+}
+
+}  // namespace cvtgb

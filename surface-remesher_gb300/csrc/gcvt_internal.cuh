@@ -134,6 +134,8 @@ cudaError_t rows_configure();
 cudaError_t launch_extract(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *colcnt,
                            double scale, double left, double lower, double *xy,
                            unsigned capacity, unsigned *total, cudaStream_t s);
+int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris, unsigned cap,
+                   unsigned *ntris, cudaStream_t s);
 cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigned *lofs,
                               unsigned nblocks, unsigned *gofs, unsigned *done, unsigned *ticket,
                               cudaStream_t s);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "gcvt_rasterize": ([P, P, I, P, I, P, ctypes.c_double, I, I], I),
     "gcvt_ctx_extract_points": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I,
                                  ctypes.POINTER(I), I], I),
+    "gcvt_ctx_delaunay": ([P, P, I, ctypes.POINTER(I), I], I),
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
     "gcvt_ctx_jfa_label": ([P, P, P, I], I),
     "gcvt_ctx_autotune": ([P, ctypes.POINTER(Tuning)], I),
@@ -236,6 +237,20 @@ class Context:
         _check(self.lib.gcvt_ctx_extract_points(self.h, float(scale), float(left), float(lower),
                                                 out.ctypes.data, int(capacity), ctypes.byref(cnt),
                                                 MEM_HOST), "gcvt_ctx_extract_points")
+        return out[:min(cnt.value, capacity)]
+
+    def delaunay(self, capacity=None):
+        """Delaunay triangles (T, 3) int32 of the current free sites, as
+        indices into extract_points' list, counter-clockwise."""
+        cnt = I(0)
+        if capacity is None:  # a triangulation of V points has at most 2V - 5 triangles
+            _check(self.lib.gcvt_ctx_extract_points(self.h, 1.0, 0.0, 0.0, None, 0,
+                                                    ctypes.byref(cnt), MEM_HOST),
+                   "gcvt_ctx_extract_points")
+            capacity = max(2 * cnt.value - 5, 0)
+        out = np.empty((max(capacity, 1), 3), np.int32)
+        _check(self.lib.gcvt_ctx_delaunay(self.h, out.ctypes.data, int(capacity),
+                                          ctypes.byref(cnt), MEM_HOST), "gcvt_ctx_delaunay")
         return out[:min(cnt.value, capacity)]
 
     def autotune(self):
