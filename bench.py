@@ -366,6 +366,8 @@ def run_ours(args):
         t_e2e = timed(step_host, args.steps)
         # time to E <= (1 + 1e-4) E_conv, plain and with gated learned jumps
         tte = time_to_energy_line(G, ctx, n, sites, rho, mask)
+        # the Delaunay triangulation of the converged sites (outside the timing)
+        _, delaunay = delaunay_stage(ctx, G.load_library(), len(ctx.extract_points()), args)
         # a labelling pass (final output) and a jump-flooding labelling,
         # timed alone; the jump-flooding error on the initial sites
         ctx.load(d_sites, d_rho, d_mask)
@@ -395,6 +397,7 @@ def run_ours(args):
         "jfa": jfa_line(n, kms[2], jfa_stats, peak, tuning["jfa_tail_halo"]),
         "tuning": tuning,
         "time_to_energy": tte,
+        "delaunay": delaunay,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(workload),
                      "peak_source": peak_kind,
@@ -658,23 +661,56 @@ def run_mesh(args):
     return 0
 
 
+def delaunay_stage(ctx, lib, npts, args):
+    """The Delaunay triangulation of the final sites on the GPU
+    (gcvt_ctx_delaunay, device output; the call is host-synchronous, so it is
+    timed on the host clock), and scipy's Qhull on the same points on the
+    host for comparison (a library, not the reference: the reference's
+    gDel2D does not build here)."""
+    import ctypes
+    import torch
+    import gcvt_gb300 as G
+    cap = max(2 * npts - 5, 1)
+    d_tri = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+    cnt = ctypes.c_int(0)
+    times = []
+    for r in range(max(3, args.warmup) + max(3, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G._check(lib.gcvt_ctx_delaunay(ctx.h, d_tri.data_ptr(), cap, ctypes.byref(cnt),
+                                       G.MEM_DEVICE), "gcvt_ctx_delaunay")
+        if r >= max(3, args.warmup):
+            times.append((time.perf_counter() - t0) * 1e3)
+    res = {"triangles": int(cnt.value), "ms": statistics.median(times)}
+    try:
+        from scipy.spatial import Delaunay
+        pts = ctx.extract_points()
+        t0 = time.perf_counter()
+        q = Delaunay(pts)
+        res["qhull_ms"] = (time.perf_counter() - t0) * 1e3
+        res["qhull_triangles"] = int(len(q.simplices))
+    except ImportError:
+        pass
+    return d_tri[:cnt.value], res
+
+
 def lift_stage(ctx, n, args):
-    """The stage after the CDT: the final sites, extracted as CDT input points
-    (delaunay.h:46-57), lifted onto the surface and the triangles filtered
-    (recover.h:98-157) by gcvt_lift, device buffers, CUDA events.  The CDT
-    itself is scipy's Delaunay on the host (outside the timing).  Beside it,
+    """The stages after the Lloyd loop: the final sites, extracted as CDT
+    input points (delaunay.h:46-57), triangulated on the GPU
+    (gcvt_ctx_delaunay), lifted onto the surface and the triangles filtered
+    (recover.h:98-157) by gcvt_lift, device buffers, CUDA events.  Beside it,
     the oracle's single-thread restatement of recover() -- the reference's
     O(queries x faces) scan -- timed on 400 queries and scaled to all."""
     import torch
     import gcvt_gb300 as G
-    from scipy.spatial import Delaunay
     from workloads import disk_surface, raster_inputs
     uv, xyz, tris = disk_surface(256, seed=2)
     _, scale, left, lower = raster_inputs(uv, n)
     pts = ctx.extract_points(scale, left, lower)
-    cdt = Delaunay(pts).simplices.astype(np.int32)
     lib = G.load_library()
-    d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (uv, xyz, tris, pts, cdt)]
+    d_cdt, dstage = delaunay_stage(ctx, lib, len(pts), args)
+    cdt = d_cdt.cpu().numpy()
+    d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (uv, xyz, tris, pts)] + [d_cdt]
     out = torch.empty((len(pts), 3), dtype=torch.float64, device="cuda")
     face = torch.empty(len(pts), dtype=torch.int32, device="cuda")
     keep = torch.empty(len(cdt), dtype=torch.uint8, device="cuda")
@@ -696,7 +732,7 @@ def lift_stage(ctx, n, args):
             times.append(ev[0].elapsed_time(ev[1]))
     res = {"points": int(len(pts)), "faces": int(len(tris)), "cdt_triangles": int(len(cdt)),
            "kept": int(keep.sum().item()), "located": int((face >= 0).sum().item()),
-           "lift_ms": statistics.median(times)}
+           "lift_ms": statistics.median(times), "delaunay": dstage}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as orc

@@ -14,21 +14,21 @@
 // triangulation of the sites, and every site that evaluates a predicate
 // gets the same sign, so all stars agree.
 //
-// Each site computes its own Delaunay star (its neighbours in angular order)
-// from the sites in a window around it: inverted about the site, the star is
-// the part of the candidates' convex hull facing away from the site, so the
-// candidates are inserted one by one into a sorted cyclic list (a candidate
-// inside the current hull never becomes a neighbour later; an inserted one
-// removes the neighbours it covers).  Certificate, exact: a triangle of the
-// star is final when no site outside the window lies in its circumcircle,
-// an open angular gap (>= pi) when no site lies strictly inside its cone
-// (then the site is on the sites' convex hull); both are searched through a
-// pyramid of tile occupancy, and a site found is inserted and the star
-// checked again.  Only a star of fewer than two neighbours widens the
-// window (a window covering the grid is exact).  Threads take the sites in
-// tile order (nearby sites share a warp); a triangle is written by its
-// vertex that comes first in delaunayInput's order (x, then y), counter-
-// clockwise, so the output does not depend on the scheduling.
+// Each site's Delaunay star (its neighbours in angular order) is computed
+// by one warp from the sites in a window around it: inverted about the
+// site, the star is the part of the candidates' convex hull facing away from
+// the site, so the candidates are inserted one by one into a sorted cyclic
+// list held in the warp's registers (a candidate inside the current hull
+// never becomes a neighbour later; an inserted one removes the neighbours it
+// covers).  Certificate, exact: a triangle of the star is final when no site
+// outside the window lies in its circumcircle, an open angular gap (>= pi)
+// when no site lies strictly inside its cone (then the site is on the
+// sites' convex hull); both are searched through a pyramid of tile
+// occupancy, and a site found is inserted and the star checked again.  Only
+// a star of fewer than two neighbours widens the window (a window covering
+// the grid is exact).  Warps take the sites in tile order; a triangle is
+// written by its vertex that comes first in delaunayInput's order (x, then
+// y), counter-clockwise, so the output does not depend on the scheduling.
 #include "gcvt_internal.cuh"
 #include "../../include/gcvt_gb300.h"
 
@@ -51,13 +51,6 @@ __device__ __forceinline__ long long cross(int ax, int ay, int bx, int by) {
 // angular order around the site: half 0 = [0, pi), half 1 = [pi, 2 pi)
 __device__ __forceinline__ int half_of(int x, int y) { return (y > 0 || (y == 0 && x > 0)) ? 0 : 1; }
 
-// a strictly before b in angle (same ray: not before)
-__device__ __forceinline__ bool ang_less(int ax, int ay, int bx, int by) {
-  const int ha = half_of(ax, ay), hb = half_of(bx, by);
-  if (ha != hb) return ha < hb;
-  return cross(ax, ay, bx, by) > 0;
-}
-
 // the CCW angle from a to b is >= pi (b not strictly left of a, and not the
 // same ray)
 __device__ __forceinline__ bool open_gap(int ax, int ay, int bx, int by) {
@@ -69,18 +62,21 @@ __device__ __forceinline__ bool open_gap(int ax, int ay, int bx, int by) {
 
 // Perturbed incircle: is d strictly inside the circle through the site
 // (origin), a and b (counter-clockwise)?  Coordinates relative to the site;
-// hp, ha, hb, hd the perturbation keys h(q) = y n + x.
-__device__ bool in_circle(int ax, int ay, int bx, int by, int dx, int dy, long long hp,
-                          long long ha, long long hb, long long hd) {
+// hp, ha, hb, hd the ranks h(q) = y n + x.  With n <= 8192 every
+// coordinate difference is below 2^14, each cofactor and lifted term below
+// 2^29 and the determinant below 2^61: exact in 64-bit integers.
+__device__ __forceinline__ bool in_circle(int ax, int ay, int bx, int by, int dx, int dy,
+                                          long long hp, long long ha, long long hb,
+                                          long long hd) {
   // rows: p - d, a - d, b - d (p = origin)
-  const long long r0x = -dx, r0y = -dy, r1x = ax - dx, r1y = ay - dy, r2x = bx - dx,
-                  r2y = by - dy;
-  const long long m0 = r1x * r2y - r1y * r2x;  // cofactor of row 0
-  const long long m1 = r0x * r2y - r0y * r2x;
-  const long long m2 = r0x * r1y - r0y * r1x;
-  const long long z0 = r0x * r0x + r0y * r0y, z1 = r1x * r1x + r1y * r1y,
-                  z2 = r2x * r2x + r2y * r2y;
-  const __int128 d0 = (__int128)z0 * m0 - (__int128)z1 * m1 + (__int128)z2 * m2;
+  const int r0x = -dx, r0y = -dy, r1x = ax - dx, r1y = ay - dy, r2x = bx - dx, r2y = by - dy;
+  const long long m0 = (long long)r1x * r2y - (long long)r1y * r2x;  // cofactor of row 0
+  const long long m1 = (long long)r0x * r2y - (long long)r0y * r2x;
+  const long long m2 = (long long)r0x * r1y - (long long)r0y * r1x;
+  const long long z0 = (long long)r0x * r0x + (long long)r0y * r0y,
+                  z1 = (long long)r1x * r1x + (long long)r1y * r1y,
+                  z2 = (long long)r2x * r2x + (long long)r2y * r2y;
+  const long long d0 = z0 * m0 - z1 * m1 + z2 * m2;
   if (d0 != 0) return d0 > 0;
   // co-circular: z(q) += delta(q), delta growing (infinitesimally) with
   // h(q); the determinant is linear in the z column, so the sign is that of
@@ -92,81 +88,14 @@ __device__ bool in_circle(int ax, int ay, int bx, int by, int dx, int dy, long l
   return m0 - m1 + m2 < 0;
 }
 
-struct Star {
-  int nb[kStar];  // packed (dx, dy), angular order
-  int m;
-  bool overflow;
-};
-
 __device__ __forceinline__ long long hkey(int n, int x, int y) { return (long long)y * n + x; }
 
-// Insert candidate q (relative (qx, qy)) into the star of site (sx, sy).
-// The star is sorted by angle from the +x axis; inverted about the site, its
-// neighbours are the hull vertices facing away from the site, and a
-// candidate inside that hull never becomes one later (the hull only grows).
-__device__ void star_insert(Star &st, int n, int sx, int sy, int qx, int qy) {
-  const long long hp = hkey(n, sx, sy), hq = hkey(n, sx + qx, sy + qy);
-  // a neighbour on the same ray: the nearer one wins (the farther one is
-  // strictly inside every circle through the site and the nearer one)
-  for (int k = 0; k < st.m; ++k) {
-    const int ux = pdx(st.nb[k]), uy = pdy(st.nb[k]);
-    if (cross(ux, uy, qx, qy) == 0 && (long long)ux * qx + (long long)uy * qy > 0) {
-      if ((long long)qx * qx + (long long)qy * qy >= (long long)ux * ux + (long long)uy * uy)
-        return;
-      for (int j = k; j + 1 < st.m; ++j) st.nb[j] = st.nb[j + 1];
-      --st.m;
-      break;
-    }
-  }
-  int m = st.m;
-  // position: neighbours [0, pos) come before q in angle
-  int pos = 0;
-  while (pos < m && ang_less(pdx(st.nb[pos]), pdy(st.nb[pos]), qx, qy)) ++pos;
-  if (m >= 2) {
-    const int u = st.nb[(pos + m - 1) % m], w = st.nb[pos % m];
-    const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
-    if (!open_gap(ux, uy, wx, wy) &&
-        !in_circle(ux, uy, wx, wy, qx, qy, hp, hkey(n, sx + ux, sy + uy),
-                   hkey(n, sx + wx, sy + wy), hq))
-      return;  // inside the hull: never a neighbour
-  }
-  if (m >= kStar) {
-    st.overflow = true;
-    return;
-  }
-  for (int k = m; k > pos; --k) st.nb[k] = st.nb[k - 1];
-  const int qv = pk(qx, qy);
-  st.nb[pos] = qv;
-  st.m = ++m;
-  // neighbours q now covers: clockwise of q, then counter-clockwise
-  for (;;) {
-    m = st.m;
-    if (m < 3) break;
-    int iq = 0;
-    while (st.nb[iq] != qv) ++iq;
-    const int iu = (iq + m - 1) % m, u = st.nb[iu], uu = st.nb[(iq + m - 2) % m];
-    const int ax = pdx(uu), ay = pdy(uu), vx = pdx(u), vy = pdy(u);
-    if (open_gap(ax, ay, qx, qy) ||
-        in_circle(ax, ay, qx, qy, vx, vy, hp, hkey(n, sx + ax, sy + ay), hq,
-                  hkey(n, sx + vx, sy + vy)))
-      break;
-    for (int k = iu; k + 1 < m; ++k) st.nb[k] = st.nb[k + 1];
-    --st.m;
-  }
-  for (;;) {
-    m = st.m;
-    if (m < 3) break;
-    int iq = 0;
-    while (st.nb[iq] != qv) ++iq;
-    const int iw = (iq + 1) % m, w = st.nb[iw], ww = st.nb[(iq + 2) % m];
-    const int bx = pdx(ww), by = pdy(ww), vx = pdx(w), vy = pdy(w);
-    if (open_gap(qx, qy, bx, by) ||
-        in_circle(qx, qy, bx, by, vx, vy, hp, hq, hkey(n, sx + bx, sy + by),
-                  hkey(n, sx + vx, sy + vy)))
-      break;
-    for (int k = iw; k + 1 < m; ++k) st.nb[k] = st.nb[k + 1];
-    --st.m;
-  }
+// Tiles are visited in bricks of 4 x 4 (64 x 64 pixels), so that the sites
+// a warp handles lie close together and their windows overlap.
+constexpr int kBrick = 4;
+__device__ __forceinline__ int brick_of(int tx, int ty, int nt0) {
+  return ((ty / kBrick) * (nt0 / kBrick) + tx / kBrick) * (kBrick * kBrick) +
+         (ty % kBrick) * kBrick + tx % kBrick;
 }
 
 // Is every grid point in the closed circumdisc of (site, u, w) inside the
@@ -211,32 +140,199 @@ __device__ __forceinline__ uint64_t free_word(const uint64_t *bits, const uint64
   return fixed ? bits[i] & ~fixed[i] : bits[i];
 }
 
-// Insert the free sites of column x, rows [ya, yb] (the site itself left out).
-__device__ void insert_column(Star &st, const uint64_t *bits, const uint64_t *fixed, int n,
-                              int sx, int sy, int x, int ya, int yb) {
-  for (int b = ya / kBand; b <= yb / kBand; ++b) {
-    const int lo = max(ya - b * kBand, 0), hi = min(yb - b * kBand, 63);
-    const uint64_t up = hi >= 63 ? ~0ull : ((2ull << hi) - 1ull);
-    uint64_t w = free_word(bits, fixed, (size_t)b * n + x) & up & ~((1ull << lo) - 1ull);
-    while (w) {
-      const int i = __ffsll((long long)w) - 1;
-      w &= w - 1ull;
-      const int qx = x - sx, qy = b * kBand + i - sy;
-      if (qx != 0 || qy != 0) star_insert(st, n, sx, sy, qx, qy);
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// The star of one site, held by a warp: neighbour k (packed (dx, dy),
+// angular order) in lane k % 32 of `a` (k < 32) or of `b`; m and overflow
+// are the same in every lane.  Every function below is called by all 32
+// lanes with the same arguments and takes the same branches in each.
+struct WStar {
+  int a, b;
+  int m;
+  bool overflow;
+};
+
+__device__ __forceinline__ int wget(const WStar &s, int k) {
+  return __shfl_sync(kFull, k < 32 ? s.a : s.b, k & 31);
+}
+
+__device__ __forceinline__ void wset(WStar &s, int k, int v) {
+  if (lane_id() == (k & 31)) {
+    if (k < 32) s.a = v;
+    else s.b = v;
+  }
+}
+
+// v becomes neighbour pos; neighbours pos.. move up one
+__device__ __forceinline__ void wins(WStar &s, int pos, int v) {
+  const int l = lane_id();
+  const int aup = __shfl_up_sync(kFull, s.a, 1), bup = __shfl_up_sync(kFull, s.b, 1);
+  const int a31 = __shfl_sync(kFull, s.a, 31);
+  const int na = l < pos ? s.a : (l == pos ? v : aup);
+  const int nb = l + 32 < pos ? s.b : (l + 32 == pos ? v : (l == 0 ? a31 : bup));
+  s.a = na;
+  s.b = nb;
+  ++s.m;
+}
+
+// neighbour k leaves; neighbours k+1.. move down one
+__device__ __forceinline__ void wdel(WStar &s, int k) {
+  const int l = lane_id();
+  const int adn = __shfl_down_sync(kFull, s.a, 1), bdn = __shfl_down_sync(kFull, s.b, 1);
+  const int b0 = __shfl_sync(kFull, s.b, 0);
+  const int na = l < k ? s.a : (l == 31 ? b0 : adn);
+  const int nb = l + 32 < k ? s.b : bdn;
+  s.a = na;
+  s.b = nb;
+  --s.m;
+}
+
+// Insert candidate q (relative (qx, qy)) into the star of site (sx, sy).
+// The star is sorted by angle from the +x axis; inverted about the site, its
+// neighbours are the hull vertices facing away from the site, and a
+// candidate inside that hull never becomes one later (the hull only grows).
+__device__ void winsert(WStar &st, int n, int sx, int sy, int qx, int qy) {
+  const long long hp = hkey(n, sx, sy), hq = hkey(n, sx + qx, sy + qy);
+  const int qv = pk(qx, qy), l = lane_id();
+  int m = st.m;
+  // q's position (the neighbours before it in angle form a prefix) and a
+  // neighbour on the same ray, each lane for its two entries
+  const int hqh = half_of(qx, qy);
+  bool ba = false, sa = false, bb = false, sb = false;
+  if (l < m) {
+    const int ux = pdx(st.a), uy = pdy(st.a), hu = half_of(ux, uy);
+    const long long c = cross(ux, uy, qx, qy);
+    ba = hu < hqh || (hu == hqh && c > 0);
+    sa = c == 0 && hu == hqh;
+  }
+  if (l + 32 < m) {
+    const int ux = pdx(st.b), uy = pdy(st.b), hu = half_of(ux, uy);
+    const long long c = cross(ux, uy, qx, qy);
+    bb = hu < hqh || (hu == hqh && c > 0);
+    sb = c == 0 && hu == hqh;
+  }
+  const unsigned mba = __ballot_sync(kFull, ba), mbb = __ballot_sync(kFull, bb);
+  const unsigned msa = __ballot_sync(kFull, sa), msb = __ballot_sync(kFull, sb);
+  const int pos = __popc(mba) + __popc(mbb);
+  const int same = msa ? __ffs(msa) - 1 : (msb ? 31 + __ffs(msb) : -1);
+  int iq;
+  if (same >= 0) {
+    // the nearer site on a ray wins (the farther one is strictly inside
+    // every circle through the site and the nearer one); a nearer q lies
+    // outside the hull, so it takes the neighbour's place
+    const int u = wget(st, same), ux = pdx(u), uy = pdy(u);
+    if ((long long)qx * qx + (long long)qy * qy >= (long long)ux * ux + (long long)uy * uy) return;
+    wset(st, same, qv);
+    iq = same;
+  } else {
+    if (m >= 2) {
+      const int u = wget(st, (pos + m - 1) % m), w = wget(st, pos % m);
+      const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
+      if (!open_gap(ux, uy, wx, wy) &&
+          !in_circle(ux, uy, wx, wy, qx, qy, hp, hkey(n, sx + ux, sy + uy),
+                     hkey(n, sx + wx, sy + wy), hq))
+        return;  // inside the hull: never a neighbour
     }
+    if (m >= kStar) {
+      st.overflow = true;
+      return;
+    }
+    wins(st, pos, qv);
+    m = st.m;
+    iq = pos;
+  }
+  // neighbours q now covers: clockwise of q, then counter-clockwise
+  while (m >= 3) {
+    const int iu = iq ? iq - 1 : m - 1, iuu = iu ? iu - 1 : m - 1;
+    const int u = wget(st, iu), uu = wget(st, iuu);
+    const int ax = pdx(uu), ay = pdy(uu), vx = pdx(u), vy = pdy(u);
+    if (open_gap(ax, ay, qx, qy) ||
+        in_circle(ax, ay, qx, qy, vx, vy, hp, hkey(n, sx + ax, sy + ay), hq,
+                  hkey(n, sx + vx, sy + vy)))
+      break;
+    wdel(st, iu);
+    m = st.m;
+    if (iu < iq) --iq;
+  }
+  while (m >= 3) {
+    const int iw = iq + 1 < m ? iq + 1 : 0, iww = iw + 1 < m ? iw + 1 : 0;
+    const int w = wget(st, iw), ww = wget(st, iww);
+    const int bx = pdx(ww), by = pdy(ww), vx = pdx(w), vy = pdy(w);
+    if (open_gap(qx, qy, bx, by) ||
+        in_circle(qx, qy, bx, by, vx, vy, hp, hq, hkey(n, sx + bx, sy + by),
+                  hkey(n, sx + vx, sy + vy)))
+      break;
+    wdel(st, iw);
+    m = st.m;
+    if (iw < iq) --iq;
+  }
+}
+
+// Rows [lo, hi] of band b as a bit mask.
+__device__ __forceinline__ uint64_t band_rows(int b, int lo, int hi) {
+  lo = max(lo - b * kBand, 0);
+  hi = min(hi - b * kBand, kBand - 1);
+  if (lo > hi) return 0ull;
+  const uint64_t up = hi >= 63 ? ~0ull : ((2ull << hi) - 1ull);
+  return up & ~((1ull << lo) - 1ull);
+}
+
+// Insert the free sites of the window [nx0, nx1] x [ny0, ny1] that are not
+// in the window [x0, x1] x [y0, y1] inserted before; the lanes take 32
+// columns at a time, then insert the sites they found one by one.
+__device__ void wwindow(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
+                        int sy, int nx0, int nx1, int ny0, int ny1, int x0, int x1, int y0,
+                        int y1) {
+  const int l = lane_id();
+  for (int cx = nx0; cx <= nx1; cx += 32) {
+    const int x = cx + l;
+    for (int b = ny0 / kBand; b <= ny1 / kBand; ++b) {
+      uint64_t w = 0;
+      if (x <= nx1) {
+        w = free_word(bits, fixed, (size_t)b * n + x) & band_rows(b, ny0, ny1);
+        if (x >= x0 && x <= x1) w &= ~band_rows(b, y0, y1);
+      }
+      unsigned pend = __ballot_sync(kFull, w != 0);
+      while (pend) {
+        const int L = __ffs(pend) - 1;
+        pend &= pend - 1u;
+        uint64_t wl = __shfl_sync(kFull, (unsigned long long)w, L);
+        while (wl) {
+          const int i = __ffsll((long long)wl) - 1;
+          wl &= wl - 1ull;
+          const int qx = cx + L - sx, qy = b * kBand + i - sy;
+          if (qx != 0 || qy != 0) winsert(st, n, sx, sy, qx, qy);
+        }
+      }
+    }
+  }
+}
+
+// Push the children of node (l, tx, ty) of side S pixels, farthest from the
+// site first, so that the search reaches the tiles near the site first.
+__device__ __forceinline__ void push_children(unsigned *stk, int &sp, const Pyr &py, int l, int tx,
+                                              int ty, int S, int px0, int qy0, int sx, int sy) {
+  const int cn = py.nt[l - 1], h = S / 2;
+  const int fx = sx - px0 >= h, fy = sy - qy0 >= h;  // the site's quadrant
+  for (int c = 3; c >= 0; --c) {
+    const int cx = 2 * tx + ((c & 1) ^ fx), cy = 2 * ty + ((c >> 1) ^ fy);
+    if (cx < cn && cy < cn)
+      stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
   }
 }
 
 // The sites outside the window in the circumcircle of the star's triangle
 // (site, u, w): the occupancy pyramid is descended to the 16 x 16 tiles
-// outside the (tile-aligned) window that the closed circumdisc meets, and
-// their sites are tested with the perturbed predicate.  The first site
-// inside is inserted into the star (returns true: the triangle is gone);
-// false when the triangle is final.
-__device__ bool disc_scan(Star &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
-                          int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
-                          int y0, int y1) {
-  if (disc_in_window(ux, uy, wx, wy, sx, sy, x0, x1, y0, y1, n)) return false;
+// not wholly inside the window that the closed circumdisc meets, nearest
+// first, and their sites are tested with the perturbed predicate (a lane
+// per column).  The sites inside from the first tile that has any are
+// inserted into the star (returns true: the triangle is gone); false when
+// the triangle is final.
+__device__ bool wdisc_scan(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                           int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                           int y0, int y1) {
   const long long u2 = (long long)ux * ux + (long long)uy * uy,
                   w2 = (long long)wx * wx + (long long)wy * wy;
   const long long D = 2 * cross(ux, uy, wx, wy);
@@ -258,6 +354,7 @@ __device__ bool disc_scan(Star &st, const Pyr &py, const uint64_t *bits, const u
   for (int ty = by0 >> (4 + l0); ty <= by1 >> (4 + l0); ++ty)
     for (int tx = bx0 >> (4 + l0); tx <= bx1 >> (4 + l0); ++tx)
       stk[sp++] = ((unsigned)l0 << 28) | ((unsigned)tx << 14) | (unsigned)ty;
+  const int lane = lane_id();
   while (sp) {
     const unsigned v = stk[--sp];
     const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
@@ -267,43 +364,52 @@ __device__ bool disc_scan(Star &st, const Pyr &py, const uint64_t *bits, const u
     if (px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) continue;  // inside the window
     if (clear_of(Nx, Ny, D, px0 - sx, px1 - sx, qy0 - sy, qy1 - sy)) continue;
     if (l > 0) {
-      const int cn = py.nt[l - 1];
-      for (int c = 0; c < 4; ++c) {
-        const int cx = 2 * tx + (c & 1), cy = 2 * ty + (c >> 1);
-        if (cx < cn && cy < cn)
-          stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
-      }
+      push_children(stk, sp, py, l, tx, ty, S, px0, qy0, sx, sy);
       continue;
     }
-    // a 16 x 16 tile: its sites, by the exact predicate
-    const int b = qy0 / kBand, sh = qy0 % kBand;
-    for (int x = px0; x <= min(px1, n - 1); ++x) {
-      uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
+    // a 16 x 16 tile: lane j tests the sites of column px0 + j
+    const int b = qy0 / kBand, sh = qy0 % kBand, x = px0 + lane;
+    unsigned hit = 0;
+    if (lane < kTile && x < n) {
+      unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
       while (w) {
-        const int i = __ffsll((long long)w) - 1;
-        w &= w - 1ull;
+        const int i = __ffs(w) - 1;
+        w &= w - 1u;
         const int qx = x - sx, qy = qy0 + i - sy;
         if ((qx == ux && qy == uy) || (qx == wx && qy == wy)) continue;
-        if (in_circle(ux, uy, wx, wy, qx, qy, hp, hu, hw, hkey(n, sx + qx, sy + qy))) {
-          star_insert(st, n, sx, sy, qx, qy);
-          return true;
-        }
+        if (in_circle(ux, uy, wx, wy, qx, qy, hp, hu, hw, hkey(n, sx + qx, sy + qy)))
+          hit |= 1u << i;
       }
     }
+    unsigned pend = __ballot_sync(kFull, hit != 0);
+    if (!pend) continue;
+    while (pend) {
+      const int L = __ffs(pend) - 1;
+      pend &= pend - 1u;
+      unsigned hl = __shfl_sync(kFull, hit, L);
+      while (hl) {
+        const int i = __ffs(hl) - 1;
+        hl &= hl - 1u;
+        winsert(st, n, sx, sy, px0 + L - sx, qy0 + i - sy);
+      }
+    }
+    return true;  // the star changed: its triangles are checked again
   }
   return false;
 }
 
 // The sites outside the window strictly inside the open angular gap from u
 // to w (counter-clockwise, >= pi): the cone {q : u x q > 0 or q x w > 0}.
-// The first one found is inserted (returns true); false when the cone holds
-// no site, so the site is on the sites' convex hull and the gap is final.
-__device__ bool cone_scan(Star &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
-                          int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
-                          int y0, int y1) {
+// The first one found (nearest tiles first) is inserted (returns true);
+// false when the cone holds no site, so the site is on the sites' convex
+// hull and the gap is final.
+__device__ bool wcone_scan(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                           int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                           int y0, int y1) {
   unsigned stk[4 * kLevels];
   int sp = 0;
   stk[sp++] = (unsigned)py.top << 28;
+  const int lane = lane_id();
   while (sp) {
     const unsigned v = stk[--sp];
     const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
@@ -320,53 +426,62 @@ __device__ bool cone_scan(Star &st, const Pyr &py, const uint64_t *bits, const u
     }
     if (cu <= 0 && cw <= 0) continue;
     if (l > 0) {
-      const int cn = py.nt[l - 1];
-      for (int c = 0; c < 4; ++c) {
-        const int cx = 2 * tx + (c & 1), cy = 2 * ty + (c >> 1);
-        if (cx < cn && cy < cn)
-          stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
-      }
+      push_children(stk, sp, py, l, tx, ty, S, px0, qy0, sx, sy);
       continue;
     }
-    const int b = qy0 / kBand, sh = qy0 % kBand;
-    for (int x = px0; x <= px1; ++x) {
-      uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
+    const int b = qy0 / kBand, sh = qy0 % kBand, x = px0 + lane;
+    unsigned hit = 0;
+    if (lane < kTile && x <= px1) {
+      unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
       while (w) {
-        const int i = __ffsll((long long)w) - 1;
-        w &= w - 1ull;
+        const int i = __ffs(w) - 1;
+        w &= w - 1u;
         const int qx = x - sx, qy = qy0 + i - sy;
-        if (cross(ux, uy, qx, qy) > 0 || cross(qx, qy, wx, wy) > 0) {
-          star_insert(st, n, sx, sy, qx, qy);
-          return true;
-        }
+        if (cross(ux, uy, qx, qy) > 0 || cross(qx, qy, wx, wy) > 0) hit |= 1u << i;
       }
     }
+    const unsigned pend = __ballot_sync(kFull, hit != 0);
+    if (!pend) continue;
+    const int L = __ffs(pend) - 1;
+    const unsigned hl = __shfl_sync(kFull, hit, L);
+    winsert(st, n, sx, sy, px0 + L - sx, qy0 + __ffs(hl) - 1 - sy);
+    return true;
   }
   return false;
 }
 
-// The Delaunay star of site (sx, sy).  The window is the site's tile and
-// k = 1, 2, 4 ... tiles around it; each step inserts only the sites of the
-// new ring (nearer sites first keeps the intermediate stars small), then
-// tries the certificate.  Returns false when the star overflowed.
-__device__ bool site_star(Star &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
-                          int sy, const Pyr &py) {
+// Neighbour (k + 1) % m for the lane's entry k (lane l: k = l or l + 32).
+__device__ __forceinline__ int wnext(const WStar &s, int k) {
+  const int e = k + 1 < s.m ? k + 1 : 0;
+  const int va = __shfl_sync(kFull, s.a, e & 31), vb = __shfl_sync(kFull, s.b, e & 31);
+  return e < 32 ? va : vb;
+}
+
+// The Delaunay star of site (sx, sy), computed by a warp.  The first window
+// is sized from the local site density (the 3 x 3 tiles around the site:
+// half-width 2 site spacings, which holds a regular site's neighbours and
+// triangles' circles); the certificate then settles the triangles exactly,
+// and only a star of fewer than two neighbours doubles the window
+// (inserting just the new ring).  Returns false when the star overflowed.
+__device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
+                           int sy, const Pyr &py, const unsigned *tilecnt) {
+  st.a = st.b = 0;
   st.m = 0;
   st.overflow = false;
-  const int tx = sx / kTile, ty = sy / kTile;
-  int k = 0, x0 = sx, x1 = sx, y0 = sy, y1 = sy;
-  for (;;) {
-    k = k ? 2 * k : 1;
-    const int nx0 = max(0, (tx - k) * kTile), nx1 = min(n - 1, (tx + k + 1) * kTile - 1);
-    const int ny0 = max(0, (ty - k) * kTile), ny1 = min(n - 1, (ty + k + 1) * kTile - 1);
-    for (int x = nx0; x <= nx1; ++x) {
-      if (x < x0 || x > x1) {
-        insert_column(st, bits, fixed, n, sx, sy, x, ny0, ny1);
-      } else {
-        if (ny0 < y0) insert_column(st, bits, fixed, n, sx, sy, x, ny0, y0 - 1);
-        if (y1 < ny1) insert_column(st, bits, fixed, n, sx, sy, x, y1 + 1, ny1);
-      }
+  const int tx = sx / kTile, ty = sy / kTile, nt0 = py.nt[0], lane = lane_id();
+  unsigned cnt = 0, tiles = 0;
+  for (int j = max(ty - 1, 0); j <= min(ty + 1, nt0 - 1); ++j)
+    for (int i = max(tx - 1, 0); i <= min(tx + 1, nt0 - 1); ++i) {
+      cnt += tilecnt[brick_of(i, j, nt0)];
+      ++tiles;
     }
+  int W = (int)ceilf(2.0f * sqrtf((float)(tiles * kTile * kTile) / (float)max(cnt, 1u)));
+  W = min(max(W, 4), 2 * n);
+  int x0 = sx, x1 = sx, y0 = sy, y1 = sy;  // the window so far: the site
+  for (;;) {
+    const int nx0 = max(0, sx - W), nx1 = min(n - 1, sx + W);
+    const int ny0 = max(0, sy - W), ny1 = min(n - 1, sy + W);
+    wwindow(st, bits, fixed, n, sx, sy, nx0, nx1, ny0, ny1, x0, x1, y0, y1);
     x0 = nx0;
     x1 = nx1;
     y0 = ny0;
@@ -384,31 +499,50 @@ __device__ bool site_star(Star &st, const uint64_t *bits, const uint64_t *fixed,
       }
       changed = false;
       const int m = st.m;
-      ok = m > 0;
-      for (int j = 0; j < m && ok; ++j) {
-        const int u = st.nb[j], w = st.nb[(j + 1) % m];
+      ok = m >= 2;  // fewer than two neighbours: a wider window
+      if (!ok) break;
+      // each lane checks its two triangles against the window; the ones
+      // that the window does not settle are searched one by one
+      bool need_a = false, need_b = false;
+      {
+        const int wa = wnext(st, lane), wb = wnext(st, lane + 32);
+        if (lane < m) {
+          const int ux = pdx(st.a), uy = pdy(st.a), wx = pdx(wa), wy = pdy(wa);
+          need_a = open_gap(ux, uy, wx, wy) ||
+                   !disc_in_window(ux, uy, wx, wy, sx, sy, x0, x1, y0, y1, n);
+        }
+        if (lane + 32 < m) {
+          const int ux = pdx(st.b), uy = pdy(st.b), wx = pdx(wb), wy = pdy(wb);
+          need_b = open_gap(ux, uy, wx, wy) ||
+                   !disc_in_window(ux, uy, wx, wy, sx, sy, x0, x1, y0, y1, n);
+        }
+      }
+      unsigned pa = __ballot_sync(kFull, need_a), pb = __ballot_sync(kFull, need_b);
+      while (pa || pb) {
+        int k;
+        if (pa) {
+          k = __ffs(pa) - 1;
+          pa &= pa - 1u;
+        } else {
+          k = 31 + __ffs(pb);
+          pb &= pb - 1u;
+        }
+        const int u = wget(st, k), w = wget(st, k + 1 < m ? k + 1 : 0);
         const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
-        if (m < 2) {
-          ok = false;  // fewer than two neighbours: a wider window
-        } else if (open_gap(ux, uy, wx, wy)
-                       ? cone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)
-                       : disc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)) {
+        const bool found =
+            open_gap(ux, uy, wx, wy)
+                ? wcone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)
+                : wdisc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1);
+        if (st.overflow) return false;
+        if (found) {
           changed = true;
           break;
         }
       }
-      if (st.overflow) return false;
     } while (changed);
     if (ok) return true;
+    W = min(2 * W, 2 * n);
   }
-}
-
-// Tiles are visited in bricks of 4 x 4 (64 x 64 pixels), so that the sites
-// a warp handles lie close together and their windows overlap.
-constexpr int kBrick = 4;
-__device__ __forceinline__ int brick_of(int tx, int ty, int nt0) {
-  return ((ty / kBrick) * (nt0 / kBrick) + tx / kBrick) * (kBrick * kBrick) +
-         (ty % kBrick) * kBrick + tx % kBrick;
 }
 
 // Sites per tile (brick order) and level 0 of the occupancy pyramid: one
@@ -488,37 +622,49 @@ __device__ __forceinline__ int site_index(const uint64_t *bits, const uint64_t *
   return (int)(coloff[x] + colpre[(size_t)b * n + x] + (unsigned)__popcll(below));
 }
 
-// The star of the t-th site in tile order, stored under its index in
-// delaunayInput's order with the number of triangles it writes.
-__global__ void k_dt_star(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
-                          int n, const int *__restrict__ order, int nsites, Pyr py,
-                          const unsigned *__restrict__ coloff, const unsigned *__restrict__ colpre,
-                          int *sitepos, int *stars, int *degree, unsigned *tcount, int *err) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nsites) return;
+// The star of the t-th site in tile order (one warp per site), stored
+// under its index in delaunayInput's order with the number of triangles it
+// writes.
+__global__ void __launch_bounds__(128)
+    k_dt_star(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed, int n,
+              const int *__restrict__ order, int nsites, Pyr py,
+              const unsigned *__restrict__ coloff, const unsigned *__restrict__ colpre,
+              const unsigned *__restrict__ tilecnt, int *sitepos, int *stars, int *degree,
+              unsigned *tcount, int *err) {
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (t >= nsites) return;  // the whole warp
+  const int lane = lane_id();
   const int sx = pdx(order[t]) & 0xffff, sy = pdy(order[t]);
   const int xm = site_index(bits, fixed, n, coloff, colpre, sx, sy);
-  sitepos[xm] = order[t];
-  Star st;
-  if (!site_star(st, bits, fixed, n, sx, sy, py)) {
-    atomicOr(err, 1);
-    degree[xm] = 0;
-    tcount[xm] = 0;
+  WStar st;
+  if (!wsite_star(st, bits, fixed, n, sx, sy, py, tilecnt)) {
+    if (lane == 0) {
+      atomicOr(err, 1);
+      sitepos[xm] = order[t];
+      degree[xm] = 0;
+      tcount[xm] = 0;
+    }
     return;
   }
   const int m = st.m;
-  unsigned own = 0;
-  for (int k = 0; k < m; ++k) {
-    stars[(size_t)xm * kStar + k] = st.nb[k];
-    const int u = st.nb[k], w = st.nb[(k + 1) % m];
-    if (m < 2 || open_gap(pdx(u), pdy(u), pdx(w), pdy(w))) continue;
-    // written by the vertex first in (x, y) order
+  int *row = stars + (size_t)xm * kStar;
+  if (lane < m) row[lane] = st.a;
+  if (lane + 32 < m) row[lane + 32] = st.b;
+  // triangles (k, k + 1) this site writes: the one of its vertices first in
+  // (x, y) order
+  auto owns = [&](int u, int w) {
+    if (m < 2 || open_gap(pdx(u), pdy(u), pdx(w), pdy(w))) return false;
     const int ux = sx + pdx(u), uy = sy + pdy(u), wx = sx + pdx(w), wy = sy + pdy(w);
-    const bool first = (sx < ux || (sx == ux && sy < uy)) && (sx < wx || (sx == wx && sy < wy));
-    own += first;
+    return (sx < ux || (sx == ux && sy < uy)) && (sx < wx || (sx == wx && sy < wy));
+  };
+  const int wa = wnext(st, lane), wb = wnext(st, lane + 32);
+  const bool oa = lane < m && owns(st.a, wa), ob = lane + 32 < m && owns(st.b, wb);
+  const int own = __popc(__ballot_sync(kFull, oa)) + __popc(__ballot_sync(kFull, ob));
+  if (lane == 0) {
+    sitepos[xm] = order[t];
+    degree[xm] = m;
+    tcount[xm] = own;
   }
-  degree[xm] = m;
-  tcount[xm] = own;
 }
 
 __global__ void k_dt_emit(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
@@ -672,8 +818,9 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
   if (!order || !sitepos || !stars || !degree || !tcnt || !toff) return GCVT_ERR_ALLOC;
   k_dt_order<<<nblk(ntiles, 128), 128, 0, s>>>(bits, fixed, n, nt0, tileoff, order);
   DCK(cudaGetLastError());
-  k_dt_star<<<nblk(nsites, 128), 128, 0, s>>>(bits, fixed, n, order, nsites, py, coloff, colpre,
-                                              sitepos, stars, degree, tcnt, err);
+  k_dt_star<<<nblk(32ll * nsites, 128), 128, 0, s>>>(bits, fixed, n, order, nsites, py, coloff,
+                                                     colpre, tilecnt, sitepos, stars, degree, tcnt,
+                                                     err);
   DCK(cudaGetLastError());
   if ((rc = scan_big(tcnt, nsites, toff, sc, s))) return rc;
   if (tris && cap) {

@@ -70,6 +70,27 @@ def test_small_sets_match_the_perturbed_triangulation(gcvt_lib, cuda_device, nam
     dorc.check(got_pts, tris)
 
 
+def test_random_small_sets_match_the_perturbed_triangulation(gcvt_lib, cuda_device):
+    """Forty seeded small sets: uniform, clustered in the grid's corners and
+    on a coarse lattice (many co-circular quadruples)."""
+    rng = np.random.default_rng(12)
+    for trial in range(40):
+        n = int(rng.choice([256, 512]))
+        m = int(rng.integers(3, 45))
+        kind = trial % 3
+        if kind == 0:
+            pts = rng.integers(0, n, (m, 2))
+        elif kind == 1:
+            pts = np.concatenate([rng.integers(0, 6, (m // 2, 2)),
+                                  rng.integers(n - 6, n, (m - m // 2, 2))])
+        else:
+            pts = rng.integers(0, 8, (m, 2)) * (n // 8)
+        pts = sorted(set((int(x), int(y)) for x, y in pts))
+        got_pts, tris = _triangulate(gcvt_lib, _grid(n, pts))
+        want = dorc.sos_triangulation(got_pts, n)
+        assert dorc.canonical(tris) == [tuple(r) for r in want.tolist()], (trial, n, kind)
+
+
 @pytest.mark.parametrize("pts", [[], [(5, 5)], [(5, 5), (200, 7)],
                                  [(x, 2 * x + 3) for x in range(0, 120, 7)],
                                  [(77, y) for y in range(0, 256, 5)]])
