@@ -787,6 +787,34 @@ def run_profile_lift(repeats):
     return 0
 
 
+def run_profile_delaunay(repeats, workload):
+    """The Delaunay of a plain workload's sites after its Lloyd iterations,
+    `repeats` times into a device buffer (for ncu)."""
+    import ctypes
+    import torch
+    import gcvt_gb300 as G
+    from workloads import config_inputs
+    sites, rho, mask, iters = config_inputs(workload, seed=SEED)
+    ctx = G.Context(sites.shape[0])
+    ctx.load(sites, rho, mask)
+    ctx.iterate(iters)
+    cap = 2 * len(ctx.extract_points())
+    d = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+    cnt = ctypes.c_int(0)
+    lib = G.load_library()
+    ms = []
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G._check(lib.gcvt_ctx_delaunay(ctx.h, d.data_ptr(), cap, ctypes.byref(cnt), G.MEM_DEVICE),
+                 "gcvt_ctx_delaunay")
+        ms.append((time.perf_counter() - t0) * 1e3)
+    print(json.dumps({"profile_delaunay": workload, "iterations": iters,
+                      "triangles": cnt.value, "ms": ms}))
+    ctx.close()
+    return 0
+
+
 def run_profile_jfa(repeats):
     """The bench workload's jump-flooding labelling, `repeats` times (for ncu)."""
     import torch
@@ -821,6 +849,9 @@ def main():
                     help="only run REPEATS jump-flooding labellings of the workload (for ncu)")
     ap.add_argument("--profile-lift", type=int, default=0, metavar="REPEATS",
                     help="only run REPEATS lifts of 65,536 points on the mesh (for ncu)")
+    ap.add_argument("--profile-delaunay", type=int, default=0, metavar="REPEATS",
+                    help="only run REPEATS Delaunay triangulations of the workload's sites "
+                         "after its Lloyd iterations (for ncu)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args.profile_case,
@@ -829,6 +860,9 @@ def main():
         return run_profile_jfa(args.profile_jfa)
     if args.profile_lift:
         return run_profile_lift(args.profile_lift)
+    if args.profile_delaunay:
+        return run_profile_delaunay(args.profile_delaunay,
+                                    args.config if args.config in PLAIN else CONFIG)
     if args.warmup < 3:
         args.warmup = 3
     if args.config == "batched_64" and args.impl == "ours":

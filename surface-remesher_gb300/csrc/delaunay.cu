@@ -459,10 +459,17 @@ __device__ __forceinline__ int wnext(const WStar &s, int k) {
 
 // The Delaunay star of site (sx, sy), computed by a warp.  The first window
 // is sized from the local site density (the 3 x 3 tiles around the site:
-// half-width 2 site spacings, which holds a regular site's neighbours and
-// triangles' circles); the certificate then settles the triangles exactly,
-// and only a star of fewer than two neighbours doubles the window
-// (inserting just the new ring).  Returns false when the star overflowed.
+// half-width kWindow site spacings, which holds a regular site's neighbours
+// and triangles' circles).  When kWiden or more of its triangles reach past
+// it (as around irregular sites), the window doubles once before any search
+// (inserting a ring costs less than searching); then the certificate
+// settles the triangles exactly, and only a star of fewer than two
+// neighbours doubles the window again (each time inserting just the new
+// ring).  kWindow and kWiden are the fastest of a sweep on converged CVT
+// sites and on uniform random ones at 4096^2 and 8192^2.  Returns false
+// when the star overflowed.
+constexpr float kWindow = 1.4f;
+constexpr int kWiden = 1;
 __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
                            int sy, const Pyr &py, const unsigned *tilecnt) {
   st.a = st.b = 0;
@@ -475,9 +482,10 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
       cnt += tilecnt[brick_of(i, j, nt0)];
       ++tiles;
     }
-  int W = (int)ceilf(2.0f * sqrtf((float)(tiles * kTile * kTile) / (float)max(cnt, 1u)));
+  int W = (int)ceilf(kWindow * sqrtf((float)(tiles * kTile * kTile) / (float)max(cnt, 1u)));
   W = min(max(W, 4), 2 * n);
   int x0 = sx, x1 = sx, y0 = sy, y1 = sy;  // the window so far: the site
+  bool first = true;
   for (;;) {
     const int nx0 = max(0, sx - W), nx1 = min(n - 1, sx + W);
     const int ny0 = max(0, sy - W), ny1 = min(n - 1, sy + W);
@@ -518,6 +526,10 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
         }
       }
       unsigned pa = __ballot_sync(kFull, need_a), pb = __ballot_sync(kFull, need_b);
+      if (first && rounds == 1 && __popc(pa) + __popc(pb) >= kWiden) {
+        ok = false;  // an irregular neighbourhood: a wider window before searching
+        break;
+      }
       while (pa || pb) {
         int k;
         if (pa) {
@@ -541,6 +553,7 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
       }
     } while (changed);
     if (ok) return true;
+    first = false;
     W = min(2 * W, 2 * n);
   }
 }
