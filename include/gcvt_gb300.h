@@ -33,7 +33,7 @@ enum gcvt_status {
     GCVT_ERR_ARGUMENT = 1, /* null pointer or invalid enum value              */
     GCVT_ERR_SIZE = 2,     /* grid size outside the supported set             */
     GCVT_ERR_CUDA = 3,     /* a CUDA runtime call failed                      */
-    GCVT_ERR_INPUT = 4,    /* a site pixel does not hold its own coordinates  */
+    GCVT_ERR_INPUT = 4,    /* invalid input data (see each call)              */
     GCVT_ERR_STATE = 5,    /* call order: no problem loaded                   */
     GCVT_ERR_ALLOC = 6     /* device or host allocation failed                */
 };

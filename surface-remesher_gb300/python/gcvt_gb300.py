@@ -25,7 +25,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.normpath(os.path.join(_HERE, "..", "lib", "libgcvt_gb300.so"))
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported grid size", 3: "CUDA runtime error",
-          4: "site grid pixel does not hold its own coordinates", 5: "no problem loaded",
+          4: "invalid input data (a site pixel not holding its own coordinates, a Delaunay "
+             "star over 64 neighbours)", 5: "no problem loaded",
           6: "allocation failed"}
 
 

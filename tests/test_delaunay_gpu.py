@@ -144,3 +144,45 @@ def test_disk_of_sites_with_wide_gaps(gcvt_lib, cuda_device):
     pts = [(int(x), int(y)) for y, x in pick] + [(3, 1000), (1020, 4), (1010, 1015), (2, 2)]
     pts_got, tris = _triangulate(gcvt_lib, _grid(n, pts))
     dorc.check(pts_got, tris)
+
+
+def test_star_overflow_is_an_input_error(gcvt_lib, cuda_device):
+    """A site with more than 64 Delaunay neighbours (the centre of 108
+    co-circular lattice sites, radius 1105) fails with GCVT_ERR_INPUT and
+    leaves the context usable."""
+    n = 4096
+    r2 = 1105 ** 2
+    ring = set()
+    for x in range(-1105, 1106):
+        y = int(round((r2 - x * x) ** 0.5))
+        if x * x + y * y == r2:
+            ring |= {(x, y), (x, -y)}
+    assert len(ring) == 108
+    pts = [(2048 + x, 2048 + y) for x, y in ring] + [(2048, 2048)]
+    ctx = gcvt_lib.Context(n)
+    ctx.load(_grid(n, pts), np.ones((n, n), np.float32), np.zeros((n, n), np.uint8))
+    with pytest.raises(gcvt_lib.GcvtError) as e:
+        ctx.delaunay()
+    assert e.value.code == 4  # GCVT_ERR_INPUT
+    ctx.load(_grid(n, [(10, 10), (300, 40), (100, 500)]), np.ones((n, n), np.float32),
+             np.zeros((n, n), np.uint8))
+    assert ctx.delaunay().shape == (1, 3)
+    ctx.close()
+
+
+def test_device_output_equals_host_output(gcvt_lib, cuda_device):
+    import ctypes
+    import torch
+    sites, rho, mask = small_case(512, 2500, seed=45)
+    ctx = gcvt_lib.Context(512)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(6)
+    host = ctx.delaunay()
+    d = torch.full((len(host) + 7, 3), -1, dtype=torch.int32, device="cuda")
+    cnt = ctypes.c_int(0)
+    rc = gcvt_lib.load_library().gcvt_ctx_delaunay(ctx.h, d.data_ptr(), len(d), ctypes.byref(cnt),
+                                                    gcvt_lib.MEM_DEVICE)
+    assert rc == 0 and cnt.value == len(host)
+    assert np.array_equal(d[:len(host)].cpu().numpy(), host)
+    assert (d[len(host):] == -1).all()
+    ctx.close()
