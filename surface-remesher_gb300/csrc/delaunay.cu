@@ -323,6 +323,63 @@ __device__ __forceinline__ void push_children(unsigned *stk, int &sp, const Pyr 
   }
 }
 
+// The bounding box of the closed disc with centre (Nx, Ny) / D relative to
+// the site (radius = |centre|): FP64 with one pixel of slack, clipped to
+// the grid, so it holds every grid point of the disc.
+__device__ __forceinline__ void disc_box(long long Nx, long long Ny, long long D, int sx, int sy,
+                                         int n, int &bx0, int &bx1, int &by0, int &by1) {
+  const double cx = (double)Nx / (double)D, cy = (double)Ny / (double)D;
+  const double r = sqrt(cx * cx + cy * cy) + 1.0;
+  bx0 = (int)fmax(0.0, floor(sx + cx - r));
+  bx1 = (int)fmin(n - 1.0, ceil(sx + cx + r));
+  by0 = (int)fmax(0.0, floor(sy + cy - r));
+  by1 = (int)fmin(n - 1.0, ceil(sy + cy + r));
+}
+
+// The sites of the box [bx0, bx1] x [by0, by1] outside the window that lie
+// in the circumcircle of the star's triangle (site, u, w), a lane per
+// column, are inserted; true when there were any (the triangle is gone).
+__device__ bool wbox_scan(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
+                          int sy, int ux, int uy, int wx, int wy, int x0, int x1, int y0, int y1,
+                          int bx0, int bx1, int by0, int by1) {
+  const long long hp = hkey(n, sx, sy), hu = hkey(n, sx + ux, sy + uy),
+                  hw = hkey(n, sx + wx, sy + wy);
+  const int lane = lane_id();
+  bool found = false;
+  for (int cx = bx0; cx <= bx1; cx += 32) {
+    const int x = cx + lane;
+    for (int b = by0 / kBand; b <= by1 / kBand; ++b) {
+      uint64_t w = 0;
+      if (x <= bx1) {
+        w = free_word(bits, fixed, (size_t)b * n + x) & band_rows(b, by0, by1);
+        if (x >= x0 && x <= x1) w &= ~band_rows(b, y0, y1);
+      }
+      uint64_t hit = 0;
+      while (w) {
+        const int i = __ffsll((long long)w) - 1;
+        w &= w - 1ull;
+        const int qx = x - sx, qy = b * kBand + i - sy;
+        if ((qx == ux && qy == uy) || (qx == wx && qy == wy)) continue;
+        if (in_circle(ux, uy, wx, wy, qx, qy, hp, hu, hw, hkey(n, sx + qx, sy + qy)))
+          hit |= 1ull << i;
+      }
+      unsigned pend = __ballot_sync(kFull, hit != 0);
+      while (pend) {
+        const int L = __ffs(pend) - 1;
+        pend &= pend - 1u;
+        uint64_t hl = __shfl_sync(kFull, (unsigned long long)hit, L);
+        while (hl) {
+          const int i = __ffsll((long long)hl) - 1;
+          hl &= hl - 1ull;
+          winsert(st, n, sx, sy, cx + L - sx, b * kBand + i - sy);
+          found = true;
+        }
+      }
+    }
+  }
+  return found;
+}
+
 // The sites outside the window in the circumcircle of the star's triangle
 // (site, u, w): the occupancy pyramid is descended to the 16 x 16 tiles
 // not wholly inside the window that the closed circumdisc meets, nearest
@@ -339,12 +396,10 @@ __device__ bool wdisc_scan(WStar &st, const Pyr &py, const uint64_t *bits, const
   const long long Nx = wy * u2 - uy * w2, Ny = ux * w2 - wx * u2;
   const long long hp = hkey(n, sx, sy), hu = hkey(n, sx + ux, sy + uy),
                   hw = hkey(n, sx + wx, sy + wy);
-  // start at the pyramid level where the disc's bounding box (FP64, one
-  // pixel of slack, clipped to the grid) spans at most 2 x 2 nodes
-  const double cx = (double)Nx / (double)D, cy = (double)Ny / (double)D;
-  const double r = sqrt(cx * cx + cy * cy) + 1.0;
-  const int bx0 = (int)fmax(0.0, floor(sx + cx - r)), bx1 = (int)fmin(n - 1.0, ceil(sx + cx + r));
-  const int by0 = (int)fmax(0.0, floor(sy + cy - r)), by1 = (int)fmin(n - 1.0, ceil(sy + cy + r));
+  // start at the pyramid level where the disc's bounding box spans at most
+  // 2 x 2 nodes
+  int bx0, bx1, by0, by1;
+  disc_box(Nx, Ny, D, sx, sy, n, bx0, bx1, by0, by1);
   int l0 = 0;
   while (l0 < py.top && (((bx1 >> (4 + l0)) - (bx0 >> (4 + l0))) > 1 ||
                          ((by1 >> (4 + l0)) - (by0 >> (4 + l0))) > 1))
@@ -470,6 +525,7 @@ __device__ __forceinline__ int wnext(const WStar &s, int k) {
 // when the star overflowed.
 constexpr float kWindow = 1.4f;
 constexpr int kWiden = 1;
+constexpr int kBoxCols = 96, kBoxBands = 3;  // largest disc box scanned directly
 __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
                            int sy, const Pyr &py, const unsigned *tilecnt) {
   st.a = st.b = 0;
@@ -497,7 +553,12 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
     if (st.overflow) return false;
     if (x0 == 0 && y0 == 0 && x1 == n - 1 && y1 == n - 1) return true;  // every site seen
     // certificate, exact: the sites inside a triangle's circumcircle or an
-    // open gap's cone are inserted until there are none
+    // open gap's cone are inserted until there are none.  A triangle (or gap)
+    // a search found final stays final while it is in the star (its circle
+    // and the window do not change), so its key (u, w) is kept, one per lane,
+    // and not searched again after another triangle changed the star.
+    long long vkey = 0;
+    int nver = 0;
     bool ok, changed;
     int rounds = 0;
     do {
@@ -541,14 +602,33 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
         }
         const int u = wget(st, k), w = wget(st, k + 1 < m ? k + 1 : 0);
         const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
-        const bool found =
-            open_gap(ux, uy, wx, wy)
-                ? wcone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1)
-                : wdisc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1);
+        const long long key = ((long long)(unsigned)u << 32) | (unsigned)w;
+        if (__ballot_sync(kFull, lane < nver && vkey == key)) continue;  // known final
+        bool found;
+        if (open_gap(ux, uy, wx, wy)) {
+          found = wcone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1);
+        } else {
+          // a small disc: its bounding box outside the window, column by
+          // column; a large one through the occupancy pyramid
+          const long long u2 = (long long)ux * ux + (long long)uy * uy,
+                          w2 = (long long)wx * wx + (long long)wy * wy;
+          const long long D = 2 * cross(ux, uy, wx, wy);
+          int bx0, bx1, by0, by1;
+          disc_box(wy * u2 - uy * w2, ux * w2 - wx * u2, D, sx, sy, n, bx0, bx1, by0, by1);
+          found = bx1 - bx0 < kBoxCols && by1 / kBand - by0 / kBand < kBoxBands
+                      ? wbox_scan(st, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1,
+                                  bx0, bx1, by0, by1)
+                      : wdisc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0,
+                                   y1);
+        }
         if (st.overflow) return false;
         if (found) {
           changed = true;
           break;
+        }
+        if (nver < 32) {  // final: remembered
+          if (lane == nver) vkey = key;
+          ++nver;
         }
       }
     } while (changed);
@@ -590,6 +670,31 @@ __global__ void k_dt_up(const uint8_t *__restrict__ lo, int nlo, uint8_t *hi, in
   hi[i] = v;
 }
 
+// Edge tiles first: an occupied tile with an empty tile (or the grid's edge)
+// among its eight neighbours holds the sites whose stars reach far (flat
+// triangles along the sites' boundary, convex-hull gaps).  Their sites are
+// listed before the interior ones so the long stars start first instead of
+// finishing last.  cnt2[c * ntiles + i]: the sites of brick-order tile i in
+// class c (0 edge, 1 interior).
+__global__ void k_dt_class(const uint8_t *__restrict__ occ0, int nt0,
+                           const unsigned *__restrict__ tilecnt, unsigned *cnt2, uint8_t *cls) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt0 * nt0) return;
+  const int brick = i / (kBrick * kBrick), in = i % (kBrick * kBrick);
+  const int tx = (brick % (nt0 / kBrick)) * kBrick + in % kBrick;
+  const int ty = (brick / (nt0 / kBrick)) * kBrick + in / kBrick;
+  bool edge = false;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int x = tx + dx, y = ty + dy;
+      edge |= x < 0 || y < 0 || x >= nt0 || y >= nt0 || !occ0[y * nt0 + x];
+    }
+  const unsigned c = tilecnt[i];
+  cnt2[i] = edge ? c : 0u;
+  cnt2[nt0 * nt0 + i] = edge ? 0u : c;
+  cls[i] = edge ? 0 : 1;
+}
+
 // Per column: free sites in the bands before each band, and in the column.
 // One warp per 32 columns; the band loop is unrolled so the loads overlap.
 __global__ void k_dt_columns(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
@@ -605,17 +710,18 @@ __global__ void k_dt_columns(const uint64_t *__restrict__ bits, const uint64_t *
   colcnt[x] = c;
 }
 
-// The sites in tile order: one thread per tile (brick order), its sites by
-// column, then row.
+// The sites in tile order, edge tiles first: one thread per tile (brick
+// order), its sites by column, then row.
 __global__ void k_dt_order(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed,
-                           int n, int nt0, const unsigned *__restrict__ toff, int *order) {
+                           int n, int nt0, const unsigned *__restrict__ toff,
+                           const uint8_t *__restrict__ cls, int *order) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nt0 * nt0) return;
   const int brick = i / (kBrick * kBrick), in = i % (kBrick * kBrick);
   const int tx = (brick % (nt0 / kBrick)) * kBrick + in % kBrick;
   const int ty = (brick / (nt0 / kBrick)) * kBrick + in / kBrick;
   const int y0 = ty * kTile, b = y0 / kBand, sh = y0 % kBand;
-  unsigned pos = toff[i];
+  unsigned pos = toff[(size_t)cls[i] * nt0 * nt0 + i];
   for (int x = tx * kTile; x < tx * kTile + kTile; ++x) {
     uint64_t w = (free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull;
     while (w) {
@@ -786,7 +892,9 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
   const int nt0 = n / kTile, ntiles = nt0 * nt0;
   unsigned *colpre = sc.take<unsigned>(nb), *colcnt = sc.take<unsigned>(n),
            *coloff = sc.take<unsigned>(n + 1), *cur = sc.take<unsigned>(n),
-           *tilecnt = sc.take<unsigned>(ntiles), *tileoff = sc.take<unsigned>(ntiles + 1);
+           *tilecnt = sc.take<unsigned>(ntiles), *cnt2 = sc.take<unsigned>(2 * (size_t)ntiles),
+           *tileoff = sc.take<unsigned>(2 * (size_t)ntiles + 1);
+  uint8_t *cls = sc.take<uint8_t>(ntiles);
   int *err = sc.take<int>(1);
   Pyr py{};
   size_t occ_bytes = 0;
@@ -802,7 +910,8 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
   }
   uint8_t *occ = sc.take<uint8_t>(occ_bytes);
   py.occ = occ;
-  if (!colpre || !colcnt || !coloff || !cur || !tilecnt || !tileoff || !err || !occ)
+  if (!colpre || !colcnt || !coloff || !cur || !tilecnt || !cnt2 || !tileoff || !cls || !err ||
+      !occ)
     return GCVT_ERR_ALLOC;
   DCK(cudaMemsetAsync(err, 0, sizeof(int), s));
   DCK(cudaMemsetAsync(occ, 0, occ_bytes, s));
@@ -818,7 +927,9 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
   }
   DCK(launch_scan(reinterpret_cast<const int *>(colcnt), n, reinterpret_cast<int *>(coloff),
                   reinterpret_cast<int *>(cur), s));
-  int rc = scan_big(tilecnt, ntiles, tileoff, sc, s);
+  k_dt_class<<<nblk(ntiles, 256), 256, 0, s>>>(occ, nt0, tilecnt, cnt2, cls);
+  DCK(cudaGetLastError());
+  int rc = scan_big(cnt2, 2 * ntiles, tileoff, sc, s);
   if (rc) return rc;
   unsigned nsites_u = 0;
   DCK(cudaMemcpyAsync(&nsites_u, coloff + n, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -829,7 +940,7 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
       *stars = sc.take<int>((size_t)nsites * kStar), *degree = sc.take<int>(nsites);
   unsigned *tcnt = sc.take<unsigned>(nsites), *toff = sc.take<unsigned>(nsites + 1);
   if (!order || !sitepos || !stars || !degree || !tcnt || !toff) return GCVT_ERR_ALLOC;
-  k_dt_order<<<nblk(ntiles, 128), 128, 0, s>>>(bits, fixed, n, nt0, tileoff, order);
+  k_dt_order<<<nblk(ntiles, 128), 128, 0, s>>>(bits, fixed, n, nt0, tileoff, cls, order);
   DCK(cudaGetLastError());
   k_dt_star<<<nblk(32ll * nsites, 128), 128, 0, s>>>(bits, fixed, n, order, nsites, py, coloff,
                                                      colpre, tilecnt, sitepos, stars, degree, tcnt,

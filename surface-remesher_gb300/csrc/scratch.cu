@@ -1,8 +1,9 @@
 // scratch.cu -- grow-only device scratch for the one-shot entry points
-// (gcvt_rasterize, gcvt_lift, gcvt_vertex_weights).  Their buffers depend on
-// the input (triangles, grid cells, list lengths), so they were allocated and
-// freed per call; on a GB300 host a cudaMalloc / cudaFree pair costs tens of
-// microseconds, more than some of these calls' kernels.  A Scratch hands out
+// (gcvt_rasterize, gcvt_lift, gcvt_vertex_weights, gcvt_ctx_delaunay).  Their
+// buffers depend on the input (triangles, grid cells, list lengths, sites),
+// so they were allocated and freed per call; on a GB300 host a cudaMalloc /
+// cudaFree pair costs tens of microseconds, more than some of these calls'
+// kernels.  A Scratch hands out
 // 256-byte aligned pieces of blocks it keeps for the device: a call that
 // outgrows the current block gets another one, and the next call finds one
 // block covering the total.  Calls on a device are serialised by its lock.
