@@ -40,7 +40,10 @@ namespace {
 
 constexpr int kStar = 64;  // Delaunay neighbours a site can hold
 
-__device__ __forceinline__ int pk(int dx, int dy) { return (int)((unsigned)(dx & 0xffff) | ((unsigned)dy << 16)); }
+// (dx, dy) packed in one int: dx in the low 16 bits, dy in the high 16
+__device__ __forceinline__ int pk(int dx, int dy) {
+  return (int)((unsigned)(dx & 0xffff) | ((unsigned)dy << 16));
+}
 __device__ __forceinline__ int pdx(int v) { return (int)(int16_t)(v & 0xffff); }
 __device__ __forceinline__ int pdy(int v) { return v >> 16; }
 
@@ -49,7 +52,9 @@ __device__ __forceinline__ long long cross(int ax, int ay, int bx, int by) {
 }
 
 // angular order around the site: half 0 = [0, pi), half 1 = [pi, 2 pi)
-__device__ __forceinline__ int half_of(int x, int y) { return (y > 0 || (y == 0 && x > 0)) ? 0 : 1; }
+__device__ __forceinline__ int half_of(int x, int y) {
+  return (y > 0 || (y == 0 && x > 0)) ? 0 : 1;
+}
 
 // the CCW angle from a to b is >= pi (b not strictly left of a, and not the
 // same ray)
@@ -107,7 +112,8 @@ __device__ __forceinline__ __int128 axis_gap(long long N, long long D, int lo, i
   const __int128 a = (__int128)lo * D - N, b = (__int128)N - (__int128)hi * D;
   return a > 0 ? a : (b > 0 ? b : (__int128)0);
 }
-__device__ bool clear_of(long long Nx, long long Ny, long long D, int lx, int hx, int ly, int hy) {
+__device__ bool clear_of(long long Nx, long long Ny, long long D, int lx, int hx, int ly,
+                         int hy) {
   if (lx > hx || ly > hy) return true;  // empty strip
   const __int128 gx = axis_gap(Nx, D, lx, hx), gy = axis_gap(Ny, D, ly, hy);
   return gx * gx + gy * gy > (__int128)Nx * Nx + (__int128)Ny * Ny;
@@ -120,8 +126,10 @@ __device__ bool disc_in_window(int ux, int uy, int wx, int wy, int sx, int sy, i
   const long long Nx = wy * u2 - uy * w2, Ny = ux * w2 - wx * u2;
   const int gx0 = -sx, gx1 = n - 1 - sx, gy0 = -sy, gy1 = n - 1 - sy;  // the grid
   const int wx0 = x0 - sx, wx1 = x1 - sx, wy0 = y0 - sy, wy1 = y1 - sy;  // the window
-  return clear_of(Nx, Ny, D, gx0, wx0 - 1, gy0, gy1) && clear_of(Nx, Ny, D, wx1 + 1, gx1, gy0, gy1) &&
-         clear_of(Nx, Ny, D, wx0, wx1, gy0, wy0 - 1) && clear_of(Nx, Ny, D, wx0, wx1, wy1 + 1, gy1);
+  return clear_of(Nx, Ny, D, gx0, wx0 - 1, gy0, gy1) &&
+         clear_of(Nx, Ny, D, wx1 + 1, gx1, gy0, gy1) &&
+         clear_of(Nx, Ny, D, wx0, wx1, gy0, wy0 - 1) &&
+         clear_of(Nx, Ny, D, wx0, wx1, wy1 + 1, gy1);
 }
 
 // Site occupancy of 16 x 16 pixel tiles and its pyramid (level l: tiles of
