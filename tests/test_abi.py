@@ -55,6 +55,9 @@ def test_argument_errors_without_gpu(gcvt_lib):
     # null pointers and bad sizes are rejected before any CUDA call
     assert lib.gcvt_compute(None, None, None, 256, 1, 10) == 1
     assert lib.gcvt_label_grid(None, None, 256, 0) == 1
+    cnt = ctypes.c_int(0)
+    assert lib.gcvt_ctx_delaunay(None, None, 0, ctypes.byref(cnt), 0) == 1
+    assert lib.gcvt_ctx_extract_points(None, 1.0, 0.0, 0.0, None, 0, ctypes.byref(cnt), 0) == 1
     h = ctypes.c_void_p()
     assert lib.gcvt_ctx_create(100, ctypes.byref(h)) == 2
     assert lib.gcvt_ctx_create(16384 + 256, ctypes.byref(h)) == 2
