@@ -8,6 +8,8 @@ Only tests/ use this module.  Two parts:
   arithmetic, plus the coverage the reference's checker leaves implicit: the
   triangles tile the sites' convex hull (their areas sum to the hull's) and
   every site is a vertex, so the count is 2V - h - 2 (h: sites on the hull).
+* check_fast(points, tris): the same checks vectorised with numpy, for the
+  full-size workloads (10^5 - 10^6 sites).
 * sos_triangulation(points, n): the one Delaunay triangulation that the
   symbolic perturbation z(q) = |q|^2 + delta(q) picks (delta infinitesimal,
   infinitely larger for a larger rank y n + x), by brute force over all
@@ -175,3 +177,89 @@ def canonical(tris):
         r = t.index(min(t))
         rows.append(tuple(t[r:] + t[:r]))
     return sorted(rows)
+
+
+def check_fast(points, tris):
+    """The checks of check() vectorised with numpy (for 10^5 - 10^6 sites):
+    orientation, each directed edge once, every site a vertex, Euler,
+    2V - h - 2 triangles, area sum = hull area, and every interior edge
+    locally Delaunay (exact int64 incircle).  Returns the same counts."""
+    pts = np.asarray(points, np.int64)
+    t = np.asarray(tris, np.int64).reshape(-1, 3)
+    v = len(pts)
+    h, corners = hull_size_fast(pts)
+    if len(corners) < 3:
+        assert len(t) == 0, "triangles of collinear sites"
+        return {"vertices": 0, "edges": 0, "triangles": 0, "hull": 0}
+    assert len(t) == 2 * v - h - 2, f"{len(t)} triangles, expected {2 * v - h - 2}"
+    assert t.min() >= 0 and t.max() < v, "index out of range"
+    a, b, c = pts[t[:, 0]], pts[t[:, 1]], pts[t[:, 2]]
+    o = (b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0])
+    assert (o > 0).all(), f"{int((o <= 0).sum())} triangles not counter-clockwise"
+    cs = corners.astype(np.int64)
+    hull2 = int(((cs[1:-1, 0] - cs[0, 0]) * (cs[2:, 1] - cs[0, 1]) -
+                 (cs[1:-1, 1] - cs[0, 1]) * (cs[2:, 0] - cs[0, 0])).sum())
+    assert int(o.sum()) == hull2, "triangles do not tile the hull"
+    assert len(np.unique(t)) == v, "sites not in any triangle"
+    # directed edges (i, j) with the opposite vertex w
+    src = np.concatenate([t[:, 0], t[:, 1], t[:, 2]])
+    dst = np.concatenate([t[:, 1], t[:, 2], t[:, 0]])
+    opp = np.concatenate([t[:, 2], t[:, 0], t[:, 1]])
+    key = src * v + dst
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    assert (ks[1:] != ks[:-1]).all(), "a directed edge twice"
+    edges = np.unique(np.minimum(src, dst) * v + np.maximum(src, dst))
+    assert v - len(edges) + len(t) == 1, "Euler characteristic"
+    # the reverse of each directed edge, when it exists: interior edges
+    rkey = dst * v + src
+    pos = np.searchsorted(ks, rkey)
+    pos_c = np.minimum(pos, len(ks) - 1)
+    found = ks[pos_c] == rkey
+    i, j, w = src[found], dst[found], opp[found]
+    x = opp[order[pos_c[found]]]
+    # x must not be strictly inside the circle through i, j, w (CCW)
+    p0, p1, p2, d = pts[i], pts[j], pts[w], pts[x]
+    r0, r1, r2 = p0 - d, p1 - d, p2 - d
+    m0 = r1[:, 0] * r2[:, 1] - r1[:, 1] * r2[:, 0]
+    m1 = r0[:, 0] * r2[:, 1] - r0[:, 1] * r2[:, 0]
+    m2 = r0[:, 0] * r1[:, 1] - r0[:, 1] * r1[:, 0]
+    det = (r0 * r0).sum(1) * m0 - (r1 * r1).sum(1) * m1 + (r2 * r2).sum(1) * m2
+    assert (det <= 0).all(), f"{int((det > 0).sum())} edges not locally Delaunay"
+    return {"vertices": v, "edges": int(len(edges)), "triangles": int(len(t)), "hull": h,
+            "cocircular_edges": int((det == 0).sum()) // 2}
+
+
+def hull_size_fast(points):
+    """hull_size for large sets: strict monotone chain (Python loop over the
+    sorted unique points), then the sites on each hull edge counted exactly
+    by a vectorised collinearity test per edge."""
+    pts = np.unique(np.asarray(points, np.int64), axis=0)  # sorted by x, then y
+    if len(pts) < 3:
+        return len(pts), np.zeros((0, 2), np.int64)
+
+    def chain(seq):
+        hh = []
+        for q in seq:
+            while len(hh) >= 2 and _orient(hh[-2], hh[-1], q) <= 0:
+                hh.pop()
+            hh.append(q)
+        return hh
+    # only points extreme in their column can be hull corners
+    xs = pts[:, 0]
+    first = np.r_[True, xs[1:] != xs[:-1]]
+    last = np.r_[xs[1:] != xs[:-1], True]
+    ext = [tuple(p) for p in pts[first | last].tolist()]
+    lower, upper = chain(ext), chain(ext[::-1])
+    corners = lower[:-1] + upper[:-1]
+    if len(corners) < 3:
+        return 0, np.zeros((0, 2), np.int64)
+    cs = np.array(corners, np.int64)
+    on = np.zeros(len(pts), bool)
+    for e in range(len(cs)):
+        a, b = cs[e], cs[(e + 1) % len(cs)]
+        cr = (b[0] - a[0]) * (pts[:, 1] - a[1]) - (b[1] - a[1]) * (pts[:, 0] - a[0])
+        inside = ((np.minimum(a[0], b[0]) <= pts[:, 0]) & (pts[:, 0] <= np.maximum(a[0], b[0])) &
+                  (np.minimum(a[1], b[1]) <= pts[:, 1]) & (pts[:, 1] <= np.maximum(a[1], b[1])))
+        on |= (cr == 0) & inside
+    return int(on.sum()), cs

@@ -186,3 +186,21 @@ def test_device_output_equals_host_output(gcvt_lib, cuda_device):
     assert np.array_equal(d[:len(host)].cpu().numpy(), host)
     assert (d[len(host):] == -1).all()
     ctx.close()
+
+
+@pytest.mark.parametrize("workload", ["plain_4096", "plain_8192"])
+def test_full_size_workloads_pass_the_checks(gcvt_lib, cuda_device, workload):
+    """The benchmark workloads at full size (262,144 and 1,048,576 sites after
+    their Lloyd iterations): every property of the restated DelaunayChecker,
+    vectorised."""
+    from workloads import config_inputs
+    sites, rho, mask, iters = config_inputs(workload)
+    n = sites.shape[0]
+    ctx = gcvt_lib.Context(n)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(iters)
+    pts = ctx.extract_points().astype(np.int64)
+    tris = ctx.delaunay()
+    ctx.close()
+    info = dorc.check_fast(pts, tris)
+    assert info["vertices"] == len(pts) and info["triangles"] == len(tris)

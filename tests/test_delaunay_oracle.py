@@ -59,3 +59,18 @@ def test_checker_rejects_planted_mistakes():
                 dorc.check(pts, flipped)
             return
     pytest.fail("no flippable edge")
+
+
+@pytest.mark.parametrize("seed", [7, 8, 9])
+def test_vectorised_checker_agrees_and_rejects(seed):
+    rng = np.random.default_rng(seed)
+    pts = np.unique(rng.integers(0, 30, (50, 2)), axis=0)  # dense: many ties
+    pts = pts[np.lexsort((pts[:, 1], pts[:, 0]))]
+    good = dorc.sos_triangulation(pts, 64)
+    assert dorc.check_fast(pts, good) == dorc.check(pts, good)
+    with pytest.raises(AssertionError):
+        dorc.check_fast(pts, good[1:])
+    bad = good.copy()
+    bad[0] = bad[0][[0, 2, 1]]
+    with pytest.raises(AssertionError):
+        dorc.check_fast(pts, bad)
