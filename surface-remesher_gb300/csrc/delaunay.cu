@@ -570,7 +570,7 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
     bool ok, changed;
     int rounds = 0;
     do {
-      if (++rounds > (1 << 20)) {  // more insertions than any star needs: give up
+      if (++rounds > (1 << 16)) {  // more insertions than any star needs: give up
         st.overflow = true;
         return false;
       }
