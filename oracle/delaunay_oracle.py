@@ -5,7 +5,7 @@ Only tests/ use this module.  Two parts:
 * check(points, tris): restates gDel2D's DelaunayChecker
   (gDel2D/DelaunayChecker.cpp:27-87 checkEuler, :99-144 checkAdjacency,
   :146-169 checkOrientation, :171-213 checkDelaunay) in exact integer
-  arithmetic, plus the coverage the reference's checker leaves implicit: the
+  arithmetic, plus the coverage DelaunayChecker leaves implicit: the
   triangles tile the sites' convex hull (their areas sum to the hull's) and
   every site is a vertex, so the count is 2V - h - 2 (h: sites on the hull).
 * check_fast(points, tris): the same checks vectorised with numpy, for the

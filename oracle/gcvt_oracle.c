@@ -1,6 +1,6 @@
 /*
  * gcvt_oracle.c -- CPU oracle for the CVT hot path.  TEST INFRASTRUCTURE ONLY:
- * the checker for the CUDA path and the CPU baseline timed beside it.  Never
+ * what the tests compare the CUDA path with, and the CPU baseline timed beside it.  Never
  * linked into the product library.
  *
  * Every function cites the reference file:line it restates.  "Reference" means

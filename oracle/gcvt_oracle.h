@@ -2,8 +2,8 @@
  * gcvt_oracle.h -- CPU oracle for the CVT hot path (TEST INFRASTRUCTURE ONLY).
  *
  * This library restates, on the host, the algorithm of the reference's gCVT
- * (source/gcvt.cu) and rasteriser (source/discretization.cu).  It is the
- * checker for the CUDA path and the CPU baseline timed beside it; the product
+ * (source/gcvt.cu) and rasteriser (source/discretization.cu).  The tests
+ * compare the CUDA path with it, and it is the CPU baseline timed beside it; the product
  * library never links or calls it.  Only tests/, __graft_entry__.smoke() and
  * bench.py's cpu_baseline / --impl reference legs may load it.
  *

@@ -1,6 +1,6 @@
 """The Delaunay oracle on the CPU: the perturbed brute-force triangulation
 equals scipy's Qhull where the triangulation is unique, passes the restated
-DelaunayChecker where it is not, and the checker rejects planted mistakes."""
+DelaunayChecker where it is not, and the restated checks reject planted mistakes."""
 import numpy as np
 import pytest
 
@@ -32,7 +32,7 @@ def test_lattice_block_is_one_valid_triangulation():
     assert info["triangles"] == 2 * 36 - 20 - 2 and info["cocircular_edges"] == 25
 
 
-def test_checker_rejects_planted_mistakes():
+def test_delaunay_checks_reject_planted_mistakes():
     pts = _random(5)
     good = dorc.sos_triangulation(pts, 4096)
     dorc.check(pts, good)
@@ -62,7 +62,7 @@ def test_checker_rejects_planted_mistakes():
 
 
 @pytest.mark.parametrize("seed", [7, 8, 9])
-def test_vectorised_checker_agrees_and_rejects(seed):
+def test_vectorised_checks_agree_and_reject(seed):
     rng = np.random.default_rng(seed)
     pts = np.unique(rng.integers(0, 30, (50, 2)), axis=0)  # dense: many ties
     pts = pts[np.lexsort((pts[:, 1], pts[:, 0]))]
