@@ -318,19 +318,6 @@ __device__ void wwindow(WStar &st, const uint64_t *bits, const uint64_t *fixed, 
   }
 }
 
-// Push the children of node (l, tx, ty) of side S pixels, farthest from the
-// site first, so that the search reaches the tiles near the site first.
-__device__ __forceinline__ void push_children(unsigned *stk, int &sp, const Pyr &py, int l, int tx,
-                                              int ty, int S, int px0, int qy0, int sx, int sy) {
-  const int cn = py.nt[l - 1], h = S / 2;
-  const int fx = sx - px0 >= h, fy = sy - qy0 >= h;  // the site's quadrant
-  for (int c = 3; c >= 0; --c) {
-    const int cx = 2 * tx + ((c & 1) ^ fx), cy = 2 * ty + ((c >> 1) ^ fy);
-    if (cx < cn && cy < cn)
-      stk[sp++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
-  }
-}
-
 // The bounding box of the closed disc with centre (Nx, Ny) / D relative to
 // the site (radius = |centre|): FP64 with one pixel of slack, clipped to
 // the grid, so it holds every grid point of the disc.
@@ -388,129 +375,200 @@ __device__ bool wbox_scan(WStar &st, const uint64_t *bits, const uint64_t *fixed
   return found;
 }
 
-// The sites outside the window in the circumcircle of the star's triangle
-// (site, u, w): the occupancy pyramid is descended to the 16 x 16 tiles
-// not wholly inside the window that the closed circumdisc meets, nearest
-// first, and their sites are tested with the perturbed predicate (a lane
-// per column).  The sites inside from the first tile that has any are
-// inserted into the star (returns true: the triangle is gone); false when
-// the triangle is final.
-__device__ bool wdisc_scan(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
-                           int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
-                           int y0, int y1) {
+// What a search of the occupancy pyramid looks for: the sites in the
+// closed circumdisc of the star's triangle (site, u, w) -- centre (Nx, Ny) /
+// D relative to the site -- or, for an open angular gap from u to w
+// (counter-clockwise, >= pi), the sites strictly inside its cone
+// {q : u x q > 0 or q x w > 0}.
+struct Probe {
+  bool cone;
+  int ux, uy, wx, wy;
+  long long Nx, Ny, D, hp, hu, hw;
+};
+
+// Can the tile [px0, px1] x [qy0, qy1] hold a site the probe looks for?
+__device__ __forceinline__ bool probe_node(const Probe &pr, int sx, int sy, int px0, int px1,
+                                           int qy0, int qy1) {
+  if (!pr.cone) return !clear_of(pr.Nx, pr.Ny, pr.D, px0 - sx, px1 - sx, qy0 - sy, qy1 - sy);
+  // the cross products are linear: their largest value is at a corner
+  long long cu = LLONG_MIN, cw = LLONG_MIN;
+  for (int c = 0; c < 4; ++c) {
+    const int qx = ((c & 1) ? px1 : px0) - sx, qy = ((c >> 1) ? qy1 : qy0) - sy;
+    cu = max(cu, cross(pr.ux, pr.uy, qx, qy));
+    cw = max(cw, cross(qx, qy, pr.wx, pr.wy));
+  }
+  return cu > 0 || cw > 0;
+}
+
+// Is site q (relative to the site) one the probe looks for?
+__device__ __forceinline__ bool probe_site(const Probe &pr, int n, int sx, int sy, int qx,
+                                           int qy) {
+  if (pr.cone) return cross(pr.ux, pr.uy, qx, qy) > 0 || cross(qx, qy, pr.wx, pr.wy) > 0;
+  if ((qx == pr.ux && qy == pr.uy) || (qx == pr.wx && qy == pr.wy)) return false;
+  return in_circle(pr.ux, pr.uy, pr.wx, pr.wy, qx, qy, pr.hp, pr.hu, pr.hw,
+                   hkey(n, sx + qx, sy + qy));
+}
+
+constexpr int kWarpsPerBlock = 4;  // k_dt_star's blocks: 128 threads
+constexpr int kFrontier = 1536;    // pyramid nodes one warp's search holds
+enum { kFinal = 0, kInserted = 1, kGaveUp = 2 };
+
+// Warp-parallel search of the occupancy pyramid for the probe's sites
+// outside the window.  The nodes still to test form a stack in the warp's
+// shared memory (stk, sp of them already there); each step the lanes take up
+// to 32 nodes from its top, and an occupied node not wholly inside the
+// window that the probe can reach either puts its children on the stack or,
+// as a 16 x 16 tile, has its sites tested by its lane.  As soon as a step
+// finds sites, the tile nearest the site among those with any decides: for a
+// disc every site of it inside the circle is inserted, for a cone the first
+// one found (kInserted).  kFinal when no site is found; kGaveUp when the stack
+// would overflow (the caller then widens the window instead).  Each step
+// pops at least one node and pushes only lower levels, so the search ends;
+// a descent adds at most 3 x 32 nodes per level, so 14 levels stay below
+// kFrontier.
+__device__ int wsearch(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                       int n, int sx, int sy, const Probe &pr, int x0, int x1, int y0, int y1,
+                       unsigned *stk, int sp) {
+  const int lane = lane_id();
+  while (sp > 0) {
+    const int k = min(sp, 32);
+    unsigned v = 0;
+    if (lane < k) v = stk[sp - k + lane];
+    __syncwarp();
+    sp -= k;
+    unsigned ch[4];
+    int nch = 0, hq = 0;
+    unsigned key = 0xffffffffu;  // (distance to the site, lane) of a tile with sites found
+    if (lane < k) {
+      const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
+      const int S = kTile << l;
+      const int px0 = tx * S, px1 = min(px0 + S, n) - 1, qy0 = ty * S, qy1 = min(qy0 + S, n) - 1;
+      if (py.occ[py.off[l] + ty * py.nt[l] + tx] &&
+          !(px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) &&
+          probe_node(pr, sx, sy, px0, px1, qy0, qy1)) {
+        if (l > 0) {
+          const int cn = py.nt[l - 1];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int cx = 2 * tx + (c & 1), cy = 2 * ty + (c >> 1);
+            if (cx < cn && cy < cn)
+              ch[nch++] = ((unsigned)(l - 1) << 28) | ((unsigned)cx << 14) | (unsigned)cy;
+          }
+        } else {  // a tile: its sites, column by column, until one is found
+          const int b = qy0 / kBand, sh = qy0 % kBand;
+          bool found = false;
+          for (int x = px0; x <= px1 && !found; ++x) {
+            unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
+            while (w) {
+              const int i = __ffs(w) - 1;
+              w &= w - 1u;
+              if (probe_site(pr, n, sx, sy, x - sx, qy0 + i - sy)) {
+                found = true;
+                hq = pk(x - sx, qy0 + i - sy);
+                break;
+              }
+            }
+          }
+          if (found) {
+            const long long dx = px0 + kTile / 2 - sx, dy = qy0 + kTile / 2 - sy;
+            key = (unsigned)min((dx * dx + dy * dy) >> 4, (long long)(1 << 26)) << 5 | lane;
+          }
+        }
+      }
+    }
+    const unsigned best = __reduce_min_sync(kFull, key);
+    if (best != 0xffffffffu) {
+      const int L = (int)(best & 31u);
+      const unsigned vL = __shfl_sync(kFull, v, L);
+      const int qL = __shfl_sync(kFull, hq, L);
+      if (pr.cone) {
+        winsert(st, n, sx, sy, pdx(qL), pdy(qL));
+        return kInserted;
+      }
+      // the disc: every site of that tile inside the circle, a lane per column
+      const int tx = (int)((vL >> 14) & 0x3fff), ty = (int)(vL & 0x3fff);
+      const int px0 = tx * kTile, qy0 = ty * kTile, b = qy0 / kBand, sh = qy0 % kBand;
+      const int x = px0 + lane;
+      unsigned hit = 0;
+      if (lane < kTile && x < n) {
+        unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
+        while (w) {
+          const int i = __ffs(w) - 1;
+          w &= w - 1u;
+          if (probe_site(pr, n, sx, sy, x - sx, qy0 + i - sy)) hit |= 1u << i;
+        }
+      }
+      unsigned pend = __ballot_sync(kFull, hit != 0);
+      while (pend) {
+        const int Lc = __ffs(pend) - 1;
+        pend &= pend - 1u;
+        unsigned hl = __shfl_sync(kFull, hit, Lc);
+        while (hl) {
+          const int i = __ffs(hl) - 1;
+          hl &= hl - 1u;
+          winsert(st, n, sx, sy, px0 + Lc - sx, qy0 + i - sy);
+        }
+      }
+      return kInserted;
+    }
+    // the children onto the stack
+    int off = nch;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, off, o);
+      if (lane >= o) off += y;
+    }
+    const int total = __shfl_sync(kFull, off, 31);
+    off -= nch;
+    if (sp + total > kFrontier) return kGaveUp;
+    for (int c = 0; c < nch; ++c) stk[sp + off + c] = ch[c];
+    __syncwarp();
+    sp += total;
+  }
+  return kFinal;
+}
+
+// Search for the sites in the circumcircle of (site, u, w) outside the
+// window, starting at the pyramid level where the disc's bounding box spans
+// at most 2 x 2 nodes.
+__device__ int wdisc_search(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                            int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                            int y0, int y1, unsigned *stk) {
+  Probe pr;
+  pr.cone = false;
+  pr.ux = ux, pr.uy = uy, pr.wx = wx, pr.wy = wy;
   const long long u2 = (long long)ux * ux + (long long)uy * uy,
                   w2 = (long long)wx * wx + (long long)wy * wy;
-  const long long D = 2 * cross(ux, uy, wx, wy);
-  const long long Nx = wy * u2 - uy * w2, Ny = ux * w2 - wx * u2;
-  const long long hp = hkey(n, sx, sy), hu = hkey(n, sx + ux, sy + uy),
-                  hw = hkey(n, sx + wx, sy + wy);
-  // start at the pyramid level where the disc's bounding box spans at most
-  // 2 x 2 nodes
+  pr.D = 2 * cross(ux, uy, wx, wy);
+  pr.Nx = wy * u2 - uy * w2;
+  pr.Ny = ux * w2 - wx * u2;
+  pr.hp = hkey(n, sx, sy), pr.hu = hkey(n, sx + ux, sy + uy), pr.hw = hkey(n, sx + wx, sy + wy);
   int bx0, bx1, by0, by1;
-  disc_box(Nx, Ny, D, sx, sy, n, bx0, bx1, by0, by1);
+  disc_box(pr.Nx, pr.Ny, pr.D, sx, sy, n, bx0, bx1, by0, by1);
   int l0 = 0;
   while (l0 < py.top && (((bx1 >> (4 + l0)) - (bx0 >> (4 + l0))) > 1 ||
                          ((by1 >> (4 + l0)) - (by0 >> (4 + l0))) > 1))
     ++l0;
-  unsigned stk[4 * kLevels];
-  int sp = 0;
-  for (int ty = by0 >> (4 + l0); ty <= by1 >> (4 + l0); ++ty)
-    for (int tx = bx0 >> (4 + l0); tx <= bx1 >> (4 + l0); ++tx)
-      stk[sp++] = ((unsigned)l0 << 28) | ((unsigned)tx << 14) | (unsigned)ty;
+  const int tx0 = bx0 >> (4 + l0), ty0 = by0 >> (4 + l0);
+  const int ntx = (bx1 >> (4 + l0)) - tx0 + 1, nty = (by1 >> (4 + l0)) - ty0 + 1;  // <= 2 each
   const int lane = lane_id();
-  while (sp) {
-    const unsigned v = stk[--sp];
-    const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
-    if (!py.occ[py.off[l] + ty * py.nt[l] + tx]) continue;
-    const int S = kTile << l;
-    const int px0 = tx * S, px1 = px0 + S - 1, qy0 = ty * S, qy1 = qy0 + S - 1;
-    if (px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) continue;  // inside the window
-    if (clear_of(Nx, Ny, D, px0 - sx, px1 - sx, qy0 - sy, qy1 - sy)) continue;
-    if (l > 0) {
-      push_children(stk, sp, py, l, tx, ty, S, px0, qy0, sx, sy);
-      continue;
-    }
-    // a 16 x 16 tile: lane j tests the sites of column px0 + j
-    const int b = qy0 / kBand, sh = qy0 % kBand, x = px0 + lane;
-    unsigned hit = 0;
-    if (lane < kTile && x < n) {
-      unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
-      while (w) {
-        const int i = __ffs(w) - 1;
-        w &= w - 1u;
-        const int qx = x - sx, qy = qy0 + i - sy;
-        if ((qx == ux && qy == uy) || (qx == wx && qy == wy)) continue;
-        if (in_circle(ux, uy, wx, wy, qx, qy, hp, hu, hw, hkey(n, sx + qx, sy + qy)))
-          hit |= 1u << i;
-      }
-    }
-    unsigned pend = __ballot_sync(kFull, hit != 0);
-    if (!pend) continue;
-    while (pend) {
-      const int L = __ffs(pend) - 1;
-      pend &= pend - 1u;
-      unsigned hl = __shfl_sync(kFull, hit, L);
-      while (hl) {
-        const int i = __ffs(hl) - 1;
-        hl &= hl - 1u;
-        winsert(st, n, sx, sy, px0 + L - sx, qy0 + i - sy);
-      }
-    }
-    return true;  // the star changed: its triangles are checked again
-  }
-  return false;
+  if (lane < ntx * nty)
+    stk[lane] = ((unsigned)l0 << 28) | ((unsigned)(tx0 + lane % ntx) << 14) |
+                (unsigned)(ty0 + lane / ntx);
+  __syncwarp();
+  return wsearch(st, py, bits, fixed, n, sx, sy, pr, x0, x1, y0, y1, stk, ntx * nty);
 }
 
-// The sites outside the window strictly inside the open angular gap from u
-// to w (counter-clockwise, >= pi): the cone {q : u x q > 0 or q x w > 0}.
-// The first one found (nearest tiles first) is inserted (returns true);
-// false when the cone holds no site, so the site is on the sites' convex
-// hull and the gap is final.
-__device__ bool wcone_scan(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
-                           int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
-                           int y0, int y1) {
-  unsigned stk[4 * kLevels];
-  int sp = 0;
-  stk[sp++] = (unsigned)py.top << 28;
-  const int lane = lane_id();
-  while (sp) {
-    const unsigned v = stk[--sp];
-    const int l = (int)(v >> 28), tx = (int)((v >> 14) & 0x3fff), ty = (int)(v & 0x3fff);
-    if (!py.occ[py.off[l] + ty * py.nt[l] + tx]) continue;
-    const int S = kTile << l;
-    const int px0 = tx * S, px1 = min(px0 + S, n) - 1, qy0 = ty * S, qy1 = min(qy0 + S, n) - 1;
-    if (px0 >= x0 && px1 <= x1 && qy0 >= y0 && qy1 <= y1) continue;  // inside the window
-    // the cross products are linear: their largest value is at a corner
-    long long cu = LLONG_MIN, cw = LLONG_MIN;
-    for (int c = 0; c < 4; ++c) {
-      const int qx = ((c & 1) ? px1 : px0) - sx, qy = ((c >> 1) ? qy1 : qy0) - sy;
-      cu = max(cu, cross(ux, uy, qx, qy));
-      cw = max(cw, cross(qx, qy, wx, wy));
-    }
-    if (cu <= 0 && cw <= 0) continue;
-    if (l > 0) {
-      push_children(stk, sp, py, l, tx, ty, S, px0, qy0, sx, sy);
-      continue;
-    }
-    const int b = qy0 / kBand, sh = qy0 % kBand, x = px0 + lane;
-    unsigned hit = 0;
-    if (lane < kTile && x <= px1) {
-      unsigned w = (unsigned)((free_word(bits, fixed, (size_t)b * n + x) >> sh) & 0xffffull);
-      while (w) {
-        const int i = __ffs(w) - 1;
-        w &= w - 1u;
-        const int qx = x - sx, qy = qy0 + i - sy;
-        if (cross(ux, uy, qx, qy) > 0 || cross(qx, qy, wx, wy) > 0) hit |= 1u << i;
-      }
-    }
-    const unsigned pend = __ballot_sync(kFull, hit != 0);
-    if (!pend) continue;
-    const int L = __ffs(pend) - 1;
-    const unsigned hl = __shfl_sync(kFull, hit, L);
-    winsert(st, n, sx, sy, px0 + L - sx, qy0 + __ffs(hl) - 1 - sy);
-    return true;
-  }
-  return false;
+// Search for the sites strictly inside the open gap's cone, from the root.
+__device__ int wcone_search(WStar &st, const Pyr &py, const uint64_t *bits, const uint64_t *fixed,
+                            int n, int sx, int sy, int ux, int uy, int wx, int wy, int x0, int x1,
+                            int y0, int y1, unsigned *stk) {
+  Probe pr;
+  pr.cone = true;
+  pr.ux = ux, pr.uy = uy, pr.wx = wx, pr.wy = wy;
+  pr.Nx = pr.Ny = pr.D = pr.hp = pr.hu = pr.hw = 0;
+  if (lane_id() == 0) stk[0] = (unsigned)py.top << 28;
+  __syncwarp();
+  return wsearch(st, py, bits, fixed, n, sx, sy, pr, x0, x1, y0, y1, stk, 1);
 }
 
 // Neighbour (k + 1) % m for the lane's entry k (lane l: k = l or l + 32).
@@ -535,7 +593,7 @@ constexpr float kWindow = 1.4f;
 constexpr int kWiden = 1;
 constexpr int kBoxCols = 96, kBoxBands = 3;  // largest disc box scanned directly
 __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixed, int n, int sx,
-                           int sy, const Pyr &py, const unsigned *tilecnt) {
+                           int sy, const Pyr &py, const unsigned *tilecnt, unsigned *stk) {
   st.a = st.b = 0;
   st.m = 0;
   st.overflow = false;
@@ -612,9 +670,9 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
         const int ux = pdx(u), uy = pdy(u), wx = pdx(w), wy = pdy(w);
         const long long key = ((long long)(unsigned)u << 32) | (unsigned)w;
         if (__ballot_sync(kFull, lane < nver && vkey == key)) continue;  // known final
-        bool found;
+        int res;
         if (open_gap(ux, uy, wx, wy)) {
-          found = wcone_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1);
+          res = wcone_search(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1, stk);
         } else {
           // a small disc: its bounding box outside the window, column by
           // column; a large one through the occupancy pyramid
@@ -623,12 +681,19 @@ __device__ bool wsite_star(WStar &st, const uint64_t *bits, const uint64_t *fixe
           const long long D = 2 * cross(ux, uy, wx, wy);
           int bx0, bx1, by0, by1;
           disc_box(wy * u2 - uy * w2, ux * w2 - wx * u2, D, sx, sy, n, bx0, bx1, by0, by1);
-          found = bx1 - bx0 < kBoxCols && by1 / kBand - by0 / kBand < kBoxBands
-                      ? wbox_scan(st, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1,
-                                  bx0, bx1, by0, by1)
-                      : wdisc_scan(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0,
-                                   y1);
+          res = bx1 - bx0 < kBoxCols && by1 / kBand - by0 / kBand < kBoxBands
+                    ? (wbox_scan(st, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1, bx0,
+                                 bx1, by0, by1)
+                           ? kInserted
+                           : kFinal)
+                    : wdisc_search(st, py, bits, fixed, n, sx, sy, ux, uy, wx, wy, x0, x1, y0, y1,
+                                   stk);
         }
+        if (res == kGaveUp) {  // the search did not fit: a wider window instead
+          ok = false;
+          break;
+        }
+        const bool found = res == kInserted;
         if (st.overflow) return false;
         if (found) {
           changed = true;
@@ -752,7 +817,7 @@ __device__ __forceinline__ int site_index(const uint64_t *bits, const uint64_t *
 // The star of the t-th site in tile order (one warp per site), stored
 // under its index in delaunayInput's order with the number of triangles it
 // writes.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
     k_dt_star(const uint64_t *__restrict__ bits, const uint64_t *__restrict__ fixed, int n,
               const int *__restrict__ order, int nsites, Pyr py,
               const unsigned *__restrict__ coloff, const unsigned *__restrict__ colpre,
@@ -763,8 +828,9 @@ __global__ void __launch_bounds__(128)
   const int lane = lane_id();
   const int sx = pdx(order[t]) & 0xffff, sy = pdy(order[t]);
   const int xm = site_index(bits, fixed, n, coloff, colpre, sx, sy);
+  __shared__ unsigned s_front[kWarpsPerBlock][kFrontier];
   WStar st;
-  if (!wsite_star(st, bits, fixed, n, sx, sy, py, tilecnt)) {
+  if (!wsite_star(st, bits, fixed, n, sx, sy, py, tilecnt, s_front[threadIdx.x >> 5])) {
     if (lane == 0) {
       atomicOr(err, 1);
       sitepos[xm] = order[t];
@@ -950,9 +1016,9 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
   if (!order || !sitepos || !stars || !degree || !tcnt || !toff) return GCVT_ERR_ALLOC;
   k_dt_order<<<nblk(ntiles, 128), 128, 0, s>>>(bits, fixed, n, nt0, tileoff, cls, order);
   DCK(cudaGetLastError());
-  k_dt_star<<<nblk(32ll * nsites, 128), 128, 0, s>>>(bits, fixed, n, order, nsites, py, coloff,
-                                                     colpre, tilecnt, sitepos, stars, degree, tcnt,
-                                                     err);
+  k_dt_star<<<nblk(32ll * nsites, 32 * kWarpsPerBlock), 32 * kWarpsPerBlock, 0, s>>>(
+      bits, fixed, n, order, nsites, py, coloff, colpre, tilecnt, sitepos, stars, degree, tcnt,
+      err);
   DCK(cudaGetLastError());
   if ((rc = scan_big(tcnt, nsites, toff, sc, s))) return rc;
   if (tris && cap) {
