@@ -12,6 +12,12 @@ Outputs:
                                    source/recover.h and source/weighting.h (only
                                    where the checkout exists; host code, so it
                                    does not run on another architecture)
+  oracle/_ref/libseed_ref.so    -- ref_seed.cpp around the reference's own
+                                   source/gcvt.h seeding (same conditions)
+
+The reference checkout is found at $GCVT_REFERENCE_DIR, or given with
+--reference DIR, or else taken to be the directory `reference` beside this
+repository's root.
 
 The reference's gcvt.cu includes <helper_timer.h> from the CUDA Samples
 (gcvt.cu:27) without using it; an empty stand-in header is generated under
@@ -25,7 +31,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("GCVT_REFERENCE_DIR", "/root/reference")
+REFERENCE = os.environ.get("GCVT_REFERENCE_DIR") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference"))
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -84,11 +91,25 @@ def build_reference_recover():
     return out
 
 
+def build_reference_seed():
+    """The reference's gcvt.h seeding behind ref_seed.cpp; None where the
+    checkout is absent."""
+    src = os.path.join(REFERENCE, "source")
+    if not os.path.exists(os.path.join(src, "gcvt.h")):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    out = os.path.join(REF_OUT, "libseed_ref.so")
+    _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-ffp-contract=off", "-I", src,
+          "-o", out, os.path.join(HERE, "ref_seed.cpp")])
+    return out
+
+
 def build_all():
     paths = [build_oracle()]
-    rr = build_reference_recover()
-    if rr:
-        paths.append(rr)
+    for extra in (build_reference_recover, build_reference_seed):
+        rr = extra()
+        if rr:
+            paths.append(rr)
     try:
         paths.append(build_harness())
     except RuntimeError as e:  # no CUDA headers: the harness is optional
@@ -98,6 +119,8 @@ def build_all():
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        REFERENCE = sys.argv[sys.argv.index("--reference") + 1]
     if "--clean" in sys.argv:
         shutil.rmtree(BUILD, ignore_errors=True)
     for p in build_all():

@@ -222,6 +222,43 @@ def ref_vertex_weights(uv, xyz, triangles):
 
 # ---- the reference's own kernels -------------------------------------------
 
+def seed_ref_available():
+    return os.path.exists(os.path.join(REF, "libseed_ref.so"))
+
+
+_seed = None
+
+
+def _sr():
+    global _seed
+    if _seed is None:
+        S = ctypes.CDLL(os.path.join(REF, "libseed_ref.so"))
+        S.refseed_state.argtypes = [P, P]
+        S.refseed_state.restype = None
+        S.refseed_sites.argtypes = [P, P, P, I, I]
+        S.refseed_sites.restype = None
+        _seed = S
+    return _seed
+
+
+def ref_seed_sites(density, mask, num, state=None):
+    """The reference's own putConstrains + randomPoints (gcvt.h:56-122,
+    compiled from the checkout into oracle/_ref/libseed_ref.so).  state: the
+    generator's (z, w, jsr, jcong) to start from (None: zeros, the unseeded
+    globals); returns (site grid, state after)."""
+    S = _sr()
+    n = density.shape[0]
+    st = np.zeros(4, np.uint64) if state is None else np.array(state, np.uint64)
+    S.refseed_state(None, st.ctypes.data)
+    v = np.empty((n, n, 2), np.int16)
+    d = np.ascontiguousarray(density, np.float32).copy()
+    S.refseed_sites(v.ctypes.data, d.ctypes.data,
+                    np.ascontiguousarray(mask, np.uint8).ctypes.data, int(num), n)
+    after = np.zeros(4, np.uint64)
+    S.refseed_state(after.ctypes.data, None)
+    return v, after
+
+
 def ref_available():
     return (os.path.exists(os.path.join(REF, "gcvt_ref.cubin")) and
             os.path.exists(os.path.join(BUILD, "librefh.so")))
@@ -282,14 +319,15 @@ def ref_gcvt(voronoi, density, mask, depth=1, max_iter=1000, fixed_iters=0):
     v = np.ascontiguousarray(voronoi).copy()
     n = v.shape[0]
     energies = np.zeros(4096, np.float32)
-    stats = np.zeros(2, np.int32)
+    stats = np.zeros(3, np.int32)
     times = np.zeros(2, np.float32)
     _chk(refh().refh_gcvt(v.ctypes.data, np.ascontiguousarray(density, np.float32).ctypes.data,
                           np.ascontiguousarray(mask, np.uint8).ctypes.data, n, depth, max_iter,
                           fixed_iters, energies.ctypes.data, len(energies), stats.ctypes.data,
                           times.ctypes.data), "refh_gcvt")
     ne = int(stats[1])
-    return v, {"iterations": int(stats[0]), "energies": energies[:min(ne, 4096)].tolist(),
+    return v, {"iterations": int(stats[0]), "omega": float(stats[2:3].view(np.float32)[0]),
+               "energies": energies[:min(ne, 4096)].tolist(),
                "total_ms": float(times[0]), "loop_ms": float(times[1])}
 
 

@@ -291,7 +291,8 @@ int refh_lloyd_step(const int16_t *sites, const float *density, const uint8_t *m
 /* gCVT (gcvt.cu:1087-1156).  fixed_iters > 0 runs exactly that many
  * iterations per level without the stop rule (the omega schedule still runs);
  * energies (may be NULL) receives each sampled energy in order (cap
- * max_energies); stats: [0] = iterations, [1] = number of energies.
+ * max_energies); stats: [0] = iterations, [1] = number of energies,
+ * [2] = the final omega (pbaOmega) as float bits.
  * times_ms (may be NULL): [0] = whole call, [1] = the Lloyd loop only. */
 int refh_gcvt(int16_t *voronoi, const float *density, const uint8_t *mask, int size, int depth,
               int max_iter, int fixed_iters, float *energies, int max_energies, int *stats,
@@ -380,7 +381,11 @@ int refh_gcvt(int16_t *voronoi, const float *density, const uint8_t *mask, int s
         CHK(cuEventElapsedTime(&times_ms[1], e1, e2));
     }
     cuEventDestroy(e0); cuEventDestroy(e1); cuEventDestroy(e2); cuEventDestroy(e3);
-    if (stats) { stats[0] = iters; stats[1] = ne; }
+    if (stats) {
+        stats[0] = iters;
+        stats[1] = ne;
+        memcpy(&stats[2], &s.omega, sizeof(float)); /* pbaOmega at the end */
+    }
     return 0;
 }
 

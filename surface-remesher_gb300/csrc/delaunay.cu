@@ -961,7 +961,7 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
                    unsigned *ntris, cudaStream_t s) {
   *ntris = 0;
   if (n <= 0 || n % kBand) return GCVT_ERR_ARGUMENT;
-  Scratch sc;
+  Scratch sc(s);
   const size_t nb = (size_t)(n / kBand) * n;
   const int nt0 = n / kTile, ntiles = nt0 * nt0;
   unsigned *colpre = sc.take<unsigned>(nb), *colcnt = sc.take<unsigned>(n),

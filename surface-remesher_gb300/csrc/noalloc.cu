@@ -18,6 +18,10 @@
 // names a host-side stand-in).  The first call on a device takes the array's
 // device address with cudaGetSymbolAddress, with that device current, and
 // caches it for the device; make that first call before any stream capture.
+// A call waits for its stream before it returns (its one readback is the
+// error flag).  A malformed site grid is found by the GPU while the labelling
+// runs, so on GCVT_ERR_INPUT the label grid has been written with unspecified
+// contents.
 #include "gcvt_internal.cuh"
 #include "../../include/gcvt_gb300.h"
 

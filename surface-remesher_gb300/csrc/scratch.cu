@@ -6,7 +6,8 @@
 // kernels.  A Scratch hands out
 // 256-byte aligned pieces of blocks it keeps for the device: a call that
 // outgrows the current block gets another one, and the next call finds one
-// block covering the total.  Calls on a device are serialised by its lock.
+// block covering the total.  Calls on a device are serialised by its lock,
+// which is released only after the call's stream has drained.
 #include "gcvt_internal.cuh"
 
 #include <algorithm>
@@ -26,7 +27,8 @@ Pool g_pool[64];
 
 }  // namespace
 
-Scratch::Scratch() : pool_(nullptr), block_(0), used_(0), total_(0), ok_(false) {
+Scratch::Scratch(cudaStream_t stream)
+    : pool_(nullptr), stream_(stream), block_(0), used_(0), total_(0), ok_(false) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
   Pool *p = &g_pool[dev];
@@ -38,6 +40,9 @@ Scratch::Scratch() : pool_(nullptr), block_(0), used_(0), total_(0), ok_(false) 
 Scratch::~Scratch() {
   if (!pool_) return;
   Pool *p = static_cast<Pool *>(pool_);
+  // nothing queued by this call may still use the memory once it is released
+  // (on the success paths the call has synchronised already: no wait)
+  cudaStreamSynchronize(stream_);
   // several blocks this time: replace them by one block of their total, so a
   // call of the same size needs no allocation next time
   if (p->blocks.size() > 1 && cudaDeviceSynchronize() == cudaSuccess) {
