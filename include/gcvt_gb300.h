@@ -197,6 +197,17 @@ int gcvt_mlp_forward(const float *params, const float *feat, int count, float *o
 int gcvt_mlp_train(const float *samples, long long count, float *params, int steps, int batch,
                    float lr, unsigned long long seed, float *loss);
 
+/* One backward pass of the trainer without the Adam step: the gradient
+ * (gcvt_mlp_param_count() floats, host) of the mean loss 0.5 |out - target|^2
+ * over the `batch` samples gcvt_mlp_train draws at step `step` with `seed`,
+ * with respect to the FP32 parameters `params`; the forward rounds weights
+ * and activations to bfloat16 and the backward passes through those
+ * roundings unchanged.  loss (may be NULL) receives the batch's mean loss.
+ * Gradients are summed across blocks with FP32 atomics, so the last bits can
+ * differ run to run. */
+int gcvt_mlp_gradient(const float *samples, long long count, const float *params, int batch,
+                      unsigned long long seed, int step, float *grad, float *loss);
+
 /* Schedule state (iterations, omega, energies). */
 int gcvt_ctx_info(gcvt_ctx *ctx, gcvt_run_info *info);
 
@@ -322,7 +333,11 @@ int gcvt_vertex_weights(const double *uv, const double *xyz, int num_vertex,
  * array sized for n <= 2048 (about 0.8 MB, held by every device that loads the
  * library until exit); larger n returns GCVT_ERR_SIZE.  The first call on a
  * device looks up that array's device address -- make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race. */
+ * capture.  Every call waits for `stream` to finish its work before it
+ * returns.  Calls share the array, so calls that overlap on the GPU race.
+ * A site pixel that does not hold its own (x, y) is detected on the GPU while
+ * the labelling runs: the call then returns GCVT_ERR_INPUT and the contents
+ * of `labels` are unspecified (gcvt_label_grid returns before writing). */
 int gcvt_label_grid_static(const int16_t *sites, int16_t *labels, int n, void *stream);
 
 #ifdef __cplusplus

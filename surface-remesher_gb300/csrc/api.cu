@@ -993,6 +993,7 @@ int gcvt_ctx_features(gcvt_ctx *c, float *feat, int *ids, int *xy, int capacity,
   int total = 0;
   rc = GCVT_OK;
   if (launch_list(b, 0, c->stream) != cudaSuccess ||
+      launch_cells(b, 2, nullptr, c->stream, c->cell_grid) != cudaSuccess ||
       launch_features(b, dids, dxy, 4 * 152, c->stream) != cudaSuccess ||
       cudaMemcpyAsync(&total, &c->st->snap_count, sizeof(int), cudaMemcpyDeviceToHost,
                       c->stream) != cudaSuccess ||
@@ -1100,6 +1101,42 @@ int gcvt_mlp_train(const float *samples, long long count, float *params, int ste
               (loss && cudaMemcpyAsync(loss, dloss, steps * sizeof(float), cudaMemcpyDeviceToHost,
                                        s) != cudaSuccess) ||
               cudaStreamSynchronize(s) != cudaSuccess))
+    rc = GCVT_ERR_CUDA;
+  if (s) cudaStreamDestroy(s);
+  cudaFree(ds);
+  cudaFree(dp);
+  return rc;
+}
+
+int gcvt_mlp_gradient(const float *samples, long long count, const float *params, int batch,
+                      unsigned long long seed, int step, float *grad, float *loss) {
+  if (!samples || !params || !grad || count < 1 || batch < 1 || step < 0)
+    return GCVT_ERR_ARGUMENT;
+  if (mlp_configure() != cudaSuccess) return GCVT_ERR_CUDA;
+  const int np = mlp_param_count();
+  float *ds = nullptr, *dp = nullptr;
+  cudaStream_t s = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&ds), (size_t)count * 12 * sizeof(float)) !=
+          cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&dp), (size_t)(2 * np + 1) * sizeof(float)) !=
+          cudaSuccess) {
+    cudaFree(ds);
+    return GCVT_ERR_ALLOC;
+  }
+  float *master = dp, *dgrad = dp + np, *dloss = dp + 2 * np;
+  int rc = GCVT_OK;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMemcpyAsync(ds, samples, (size_t)count * 12 * sizeof(float), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess ||
+      cudaMemcpyAsync(master, params, np * sizeof(float), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(dgrad, 0, (size_t)(np + 1) * sizeof(float), s) != cudaSuccess ||
+      launch_mlp_grad(ds, count, master, dgrad, dloss, batch, seed, step, s) != cudaSuccess ||
+      cudaMemcpyAsync(grad, dgrad, np * sizeof(float), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess ||
+      (loss && cudaMemcpyAsync(loss, dloss, sizeof(float), cudaMemcpyDeviceToHost, s) !=
+                   cudaSuccess) ||
+      cudaStreamSynchronize(s) != cudaSuccess)
     rc = GCVT_ERR_CUDA;
   if (s) cudaStreamDestroy(s);
   cudaFree(ds);

@@ -501,19 +501,27 @@ __device__ __forceinline__ void clear_ahead(const LevelBufs &a, int cur, size_t 
   for (size_t i = t0; i < nlb; i += gthreads) czro[i] = 0u;
 }
 
-// Features of listed site idx at (sx, sy) for the learned step: its last four
-// moves (newest first) and the density gradient over the density at the
-// site, all in units of the mean cell radius (DevState::feat_scale).
+// Features of listed site idx at (sx, sy) with cell sums cs, for the learned
+// step, all in units of the mean cell radius (DevState::feat_scale): its
+// pending Lloyd displacement (the centroid of its cell minus the site, not
+// yet rounded to a pixel; 0 for a cell without density), its last three
+// applied moves (newest first) and the density gradient over the density at
+// the site.
 __device__ __forceinline__ void site_features(const LevelBufs &a, const IterView &v, int idx,
-                                              int sx, int sy) {
+                                              int sx, int sy, const CellSums &cs) {
   const int n = a.n;
   const float r = a.st->feat_scale, ir = 1.0f / r;
   const uint64_t h = a.hist[v.hc][(size_t)sy * n + sx];
   float *f = a.feat + (size_t)idx * 10;
+  const bool mass = cs.wh > 0.f;
+  const float cx = mass ? cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl) - (float)sx : 0.f;
+  const float cy = mass ? cell_centroid(sy, cs.yh, cs.yl, cs.wh, cs.wl) - (float)sy : 0.f;
+  f[0] = cx * ir;
+  f[1] = cy * ir;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    f[2 * k] = (float)(int8_t)(h >> (16 * k)) * ir;
-    f[2 * k + 1] = (float)(int8_t)(h >> (16 * k + 8)) * ir;
+  for (int k = 0; k < 3; ++k) {
+    f[2 + 2 * k] = (float)(int8_t)(h >> (16 * k)) * ir;
+    f[3 + 2 * k] = (float)(int8_t)(h >> (16 * k + 8)) * ir;
   }
   const float *d = a.density;
   const float r0 = d[(size_t)sy * n + sx];
@@ -646,7 +654,7 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
     } else {
       dfa(eh, el, cs.eh, cs.el);
       r2 = (unsigned)cs.r2;
-      if (MODE == 2) site_features(a, v, idx, sx, sy);
+      if (MODE == 2) site_features(a, v, idx, sx, sy, cs);
       else if (MODE == 3) a.hint[pid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
       else mv = move_site(a, v, e, sx, sy, cs);
     }

@@ -161,14 +161,20 @@ cudaError_t launch_mlp_train_step(const float *samples, long long count, float *
                                   float *grad, float *m, float *v, float *params_bf, float *loss,
                                   int batch, unsigned long long seed, int step, float lr,
                                   cudaStream_t s);
+cudaError_t launch_mlp_grad(const float *samples, long long count, const float *master,
+                            float *grad, float *loss, int batch, unsigned long long seed, int step,
+                            cudaStream_t s);
 cudaError_t launch_round_params(const float *master, float *params_bf, cudaStream_t s);
 // Grow-only device scratch for one call of a one-shot entry point; holds the
 // device's scratch lock for its lifetime (calls on a device serialise).
 // take() returns 256-byte aligned device memory valid until the Scratch is
-// destroyed, or nullptr when no memory can be had.
+// destroyed, or nullptr when no memory can be had.  The destructor waits for
+// `stream` (the stream the call queues its work on) before it releases the
+// lock, so a call that returns early with kernels still queued cannot hand
+// memory they use to the next call.
 class Scratch {
  public:
-  Scratch();
+  explicit Scratch(cudaStream_t stream = nullptr);
   ~Scratch();
   Scratch(const Scratch &) = delete;
   Scratch &operator=(const Scratch &) = delete;
@@ -177,6 +183,7 @@ class Scratch {
 
  private:
   void *pool_;
+  cudaStream_t stream_;
   size_t block_, used_, total_;
   bool ok_;
 };

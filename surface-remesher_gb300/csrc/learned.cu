@@ -2,7 +2,8 @@
 // site's Lloyd trajectory ends, trained on trajectories the plain method
 // produces, and applied as a jump that the energy decides on.
 //
-// Features of a site (k_cell MODE 2 or k_features): its last four integer
+// Features of a site (k_cell MODE 2): its pending Lloyd displacement (the
+// centroid of its cell minus the site, sub-pixel), its last three integer
 // moves (newest first) and the density gradient over the density at the
 // site, in units of the mean cell radius r: 10 inputs.  The MLP 10 -> 64 ->
 // 64 -> 2 (ReLU) predicts the displacement to the site's converged position,
@@ -151,29 +152,15 @@ __global__ void __launch_bounds__(256) k_gate_resolve(LevelBufs a) {
   }
 }
 
-// Features of the listed sites without their cells (training samples).
+// Ids and pixel positions of the listed sites (training samples; their
+// features come from a features pass, k_cell MODE 2, over the same list).
 __global__ void __launch_bounds__(256) k_features(LevelBufs a, int *out_ids, int *out_xy) {
   const DevState *st = a.st;
   const int n = a.n, hc = st->snap_hist, ns = st->snap_count;
-  const float r = st->feat_scale, ir = 1.0f / r;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
     const uint32_t e = a.list[i];
     const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
     const size_t pid = (size_t)sy * n + sx;
-    const uint64_t h = a.hist[hc][pid];
-    float *f = a.feat + (size_t)i * kIn;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      f[2 * k] = (float)(int8_t)(h >> (16 * k)) * ir;
-      f[2 * k + 1] = (float)(int8_t)(h >> (16 * k + 8)) * ir;
-    }
-    const float *d = a.density;
-    const float r0 = d[pid];
-    const int xa = max(sx - 1, 0), xb = min(sx + 1, n - 1), ya = max(sy - 1, 0), yb = min(sy + 1, n - 1);
-    const float gx = (d[(size_t)sy * n + xb] - d[(size_t)sy * n + xa]) / (float)(xb - xa);
-    const float gy = (d[(size_t)yb * n + sx] - d[(size_t)ya * n + sx]) / (float)(yb - ya);
-    f[8] = r0 > 0.f ? gx / r0 * r : 0.f;
-    f[9] = r0 > 0.f ? gy / r0 * r : 0.f;
     if (out_ids) out_ids[i] = a.ids[0] ? a.ids[hc][pid] : -1;
     if (out_xy) {
       out_xy[2 * i] = sx;
@@ -606,6 +593,15 @@ cudaError_t launch_mlp_train_step(const float *samples, long long count, float *
   k_mlp_grad<<<blocks, kTrainTile, mlp_grad_smem(), s>>>(samples, count, master, grad, loss,
                                                          batch, seed, step);
   k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(master, grad, m, v, params_bf, lr, step + 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_grad(const float *samples, long long count, const float *master,
+                            float *grad, float *loss, int batch, unsigned long long seed, int step,
+                            cudaStream_t s) {
+  const int blocks = (batch + kTrainTile - 1) / kTrainTile;
+  k_mlp_grad<<<blocks, kTrainTile, mlp_grad_smem(), s>>>(samples, count, master, grad, loss,
+                                                         batch, seed, step);
   return cudaGetLastError();
 }
 

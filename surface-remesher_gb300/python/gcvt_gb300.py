@@ -87,6 +87,7 @@ SIGNATURES = {
     "gcvt_ctx_iterate_learned": ([P, I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
     "gcvt_mlp_forward": ([P, P, I, P, I], I),
     "gcvt_mlp_train": ([P, ctypes.c_longlong, P, I, I, ctypes.c_float, ctypes.c_ulonglong, P], I),
+    "gcvt_mlp_gradient": ([P, ctypes.c_longlong, P, I, ctypes.c_ulonglong, I, P, P], I),
     "gcvt_ctx_set_tuning": ([P, ctypes.POINTER(Tuning)], I),
     "gcvt_batch_create": ([I, P, ctypes.POINTER(P)], I),
     "gcvt_batch_destroy": ([P], I),
@@ -393,6 +394,19 @@ def mlp_train(samples, params, steps=2000, batch=4096, lr=1e-3, seed=0):
     _check(lib.gcvt_mlp_train(s.ctypes.data, len(s), p.ctypes.data, int(steps), int(batch),
                               float(lr), int(seed), loss.ctypes.data), "gcvt_mlp_train")
     return p, loss
+
+
+def mlp_gradient(samples, params, batch, seed=0, step=0):
+    """Gradient (FP32, gcvt_mlp_param_count()) and mean loss of the batch the
+    trainer draws at `step` with `seed`, at the FP32 parameters `params`."""
+    lib = load_library()
+    s = np.ascontiguousarray(samples, np.float32)
+    p = np.ascontiguousarray(params, np.float32)
+    g = np.empty(mlp_param_count(), np.float32)
+    loss = np.empty(1, np.float32)
+    _check(lib.gcvt_mlp_gradient(s.ctypes.data, len(s), p.ctypes.data, int(batch), int(seed),
+                                 int(step), g.ctypes.data, loss.ctypes.data), "gcvt_mlp_gradient")
+    return g, float(loss[0])
 
 
 def seed_sites(density, mask, num, state=None):

@@ -48,26 +48,30 @@ def mean_radius(rho, sites):
     return max(np.sqrt(px / max(sites, 1) / np.pi), 0.5)
 
 
-def collect(runs, horizon, keep=0.5, seed=0):
+def collect(runs, horizon, keep=0.5, seed=0, site_counts=(SITES,)):
     """Samples (features, target) of plain runs: the target of a site seen at
     iteration t is its displacement to iteration t + horizon (horizon 0: to
-    iteration T_FINAL), in mean cell radii."""
+    iteration T_FINAL), in mean cell radii.  Run r has site_counts[r % k]
+    sites (more sites: smaller cells, in pixels); every run keeps about
+    keep * 4096 sites per recorded iteration."""
     rng = np.random.default_rng(seed)
     ctx = G.Context(N)
     ctx.learning(True, track_ids=True)
     out = []
     last = T_FINAL if horizon <= 0 else RECORD[-1] + horizon
     for r in range(runs):
+        m = int(site_counts[r % len(site_counts)])
         rho = gaussian_density(N, K, A_MAX, S_LO, S_HI, 1000 + r)
-        sites = disk_sites(N, SITES, 1000 + r, rho)
+        sites = disk_sites(N, m, 1000 + r, rho)
         ctx.load(sites, rho, np.zeros((N, N), np.uint8))
-        rbar = mean_radius(rho, SITES)
+        rbar = mean_radius(rho, m)
+        frac = keep * min(1.0, SITES / m)
         snaps, pos = {}, {}
         for t in range(1, last + 1):
             ctx.iterate(1)
             if t in RECORD or (horizon > 0 and t - horizon in RECORD) or t == last:
                 f, ids, xy = ctx.features(with_ids=True)
-                p = np.full((SITES, 2), np.nan, np.float32)
+                p = np.full((m, 2), np.nan, np.float32)
                 p[ids] = xy
                 pos[t] = p
                 if t in RECORD:
@@ -75,7 +79,7 @@ def collect(runs, horizon, keep=0.5, seed=0):
         for t, (f, ids, xy) in snaps.items():
             end = pos[last] if horizon <= 0 else pos[t + horizon]
             tgt = (end[ids] - xy) / rbar
-            ok = np.isfinite(tgt).all(1) & (rng.random(len(ids)) < keep)
+            ok = np.isfinite(tgt).all(1) & (rng.random(len(ids)) < frac)
             out.append(np.concatenate([f[ok], tgt[ok]], 1).astype(np.float32))
     ctx.close()
     return np.concatenate(out)
@@ -83,7 +87,8 @@ def collect(runs, horizon, keep=0.5, seed=0):
 
 def train(args):
     t0 = time.time()
-    samples = collect(args.runs, args.horizon)
+    counts = tuple(int(v) for v in str(args.sites).split(","))
+    samples = collect(args.runs, args.horizon, site_counts=counts)
     t1 = time.time()
     p0 = G.mlp_init(args.seed)
     params, loss = G.mlp_train(samples, p0, steps=args.steps, batch=args.batch, lr=args.lr,
@@ -93,7 +98,7 @@ def train(args):
     np.save(os.path.join(args.out, "step_mlp.npy"), params.astype(np.float32))
     meta = {"runs": args.runs, "samples": int(len(samples)), "steps": args.steps,
             "batch": args.batch, "lr": args.lr, "seed": args.seed,
-            "grid": N, "sites": SITES, "gaussians": K, "record": RECORD,
+            "grid": N, "sites": list(counts), "gaussians": K, "record": RECORD,
             "horizon": args.horizon if args.horizon > 0 else T_FINAL,
             "loss_first": float(loss[:20].mean()), "loss_last": float(loss[-50:].mean()),
             "target_var": float(samples[:, 10:].var(0).sum() / 2),
@@ -163,6 +168,8 @@ def main():
     ap.add_argument("--params", default=os.path.join(DATA, "step_mlp.npy"))
     ap.add_argument("--conv-iters", type=int, default=1000)
     ap.add_argument("--jump-every", type=int, default=4)
+    ap.add_argument("--sites", default=str(SITES),
+                    help="site counts of the training runs, comma-separated, used in turn")
     ap.add_argument("--horizon", type=int, default=4,
                     help="target: displacement over this many iterations (0: to iteration 200)")
     args = ap.parse_args()

@@ -1,9 +1,12 @@
-"""Learned steps: the MLP kernels against numpy, training against a known
-function, the energy gate (a jump that does not lower the energy is undone
-without a trace), and the training features (histories, ids)."""
+"""Learned steps: the MLP kernels against numpy and the host oracle
+(oracle/mlp_oracle.py: forward bit for bit, gradients, Adam), training
+against a known function, the energy gate (a jump that does not lower the
+energy is undone without a trace), and the training features (histories,
+ids)."""
 import numpy as np
 import pytest
 
+import mlp_oracle as M
 from workloads import MARKER, small_case
 
 pytestmark = pytest.mark.gpu
@@ -111,7 +114,8 @@ def test_features_track_moves_and_ids(gcvt_lib, cuda_device):
     ctx.load(sites, rho, mask)
     f0, ids0, xy0 = ctx.features(with_ids=True)
     assert len(f0) == m0 and np.array_equal(np.sort(ids0), np.arange(m0))
-    assert np.all(f0[:, :8] == 0)  # no moves yet
+    assert np.all(f0[:, 2:8] == 0)  # no moves yet
+    assert np.count_nonzero(f0[:, :2]) > 0.9 * m0  # pending displacements: centroid - site
     prev = {int(i): tuple(p) for i, p in zip(ids0, xy0)}
     ctx.iterate(1)
     f1, ids1, xy1 = ctx.features(with_ids=True)
@@ -119,15 +123,102 @@ def test_features_track_moves_and_ids(gcvt_lib, cuda_device):
     ys, xs = np.nonzero(s[..., 0] != MARKER)
     assert set(zip(xs.tolist(), ys.tolist())) == set(map(tuple, xy1.tolist()))
     assert len(np.unique(ids1)) == len(ids1) and ids1.min() >= 0 and ids1.max() < m0
-    # the newest move of each site is its displacement in this iteration
+    # the newest applied move of each site is its displacement in this
+    # iteration: the over-relaxed pending displacement of the features before
     r = None
     for f, i, p in zip(f1, ids1, xy1):
         dx, dy = p[0] - prev[int(i)][0], p[1] - prev[int(i)][1]
         if dx or dy:
-            r = dx / f[0] if f[0] else dy / f[1]
+            r = dx / f[2] if f[2] else dy / f[3]
             break
     assert r is not None and r > 0
-    moves = np.rint(f1[:, :2] * r).astype(int)
+    moves = np.rint(f1[:, 2:4] * r).astype(int)
     disp = np.array([(p[0] - prev[int(i)][0], p[1] - prev[int(i)][1]) for i, p in zip(ids1, xy1)])
     assert np.mean(np.all(moves == disp, 1)) > 0.99  # merges may hand an id on
     ctx.close()
+
+
+def _params(seed, bias=0.05):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(M.N_PARAMS, np.float32)
+    for sl, fan_in in ((M.SL_W1, 10), (M.SL_W2, 64), (M.SL_W3, 64)):
+        p[sl] = rng.normal(0, np.sqrt(2.0 / fan_in), sl.stop - sl.start)
+    for sl in (M.SL_B1, M.SL_B2, M.SL_B3):
+        p[sl] = rng.normal(bias, 0.05, sl.stop - sl.start)
+    return p
+
+
+def _samples(seed, rows):
+    rng = np.random.default_rng(seed)
+    f = rng.normal(0, 1, (rows, 10)).astype(np.float32)
+    y = np.stack([0.8 * f[:, 0] - 0.3 * f[:, 2] + 0.2 * np.abs(f[:, 8]),
+                  0.5 * f[:, 1] + 0.4 * f[:, 3] - 0.1 * f[:, 9]], 1)
+    y += rng.normal(0, 0.1, y.shape)
+    return np.concatenate([f, y.astype(np.float32)], 1)
+
+
+def test_cuda_core_forward_is_the_oracle_bit_for_bit(gcvt_lib, cuda_device):
+    # the CUDA-core forward runs the same FP32 fma chains as the oracle's
+    # "fp32" mode, so every bfloat16 rounding and the outputs agree exactly
+    p = _params(11)
+    f = np.random.default_rng(12).normal(0, 1.5, (20000, 10)).astype(np.float32)
+    got = gcvt_lib.mlp_forward(p, f, False)
+    want = M.forward(p, f, "fp32")["O"].astype(np.float32)
+    assert np.mean(got == want) > 0.9999
+    assert np.max(np.abs(got - want)) < 1e-3
+
+
+def test_mlp_gradient_matches_fp64_oracle(gcvt_lib, cuda_device):
+    p = _params(13)
+    s = _samples(14, 5000)
+    batch, seed, step = 2048, 3, 5
+    g, loss = gcvt_lib.mlp_gradient(s, p, batch, seed, step)
+    idx = M.sample_indices(seed, step, batch, len(s))
+    want_loss, want, scale = M.loss_and_gradient(p, s[idx, :10], s[idx, 10:])
+    # FP32 sums of 2048 terms per parameter (64 per block, then 32 block
+    # partials added by atomics): within 1e-4 of the sum of |terms|
+    assert abs(loss - want_loss) <= 1e-5 * want_loss
+    assert np.all(np.abs(g - want) <= 1e-4 * scale + 1e-7 * np.abs(want).max())
+    assert np.linalg.norm(g - want) <= 1e-5 * np.linalg.norm(want)
+    assert np.count_nonzero(want) > 0.8 * M.N_PARAMS  # most units see gradient
+
+
+def test_last_layer_gradient_matches_finite_differences(gcvt_lib, cuda_device):
+    # the loss is exactly quadratic in a last-layer weight or bias; with
+    # bfloat16-exact values and steps (multiples of 2^-6 below 4) the central
+    # difference of the kernel's own losses is its derivative
+    p = _params(15)
+    w3 = np.clip(np.rint(p[M.SL_W3] * 64), -200, 200) / 64
+    p[M.SL_W3] = w3
+    p[M.SL_B3] = 0.0
+    s = _samples(16, 3000)
+    batch, seed, step, h = 2048, 5, 0, 2.0 ** -6
+    g, _ = gcvt_lib.mlp_gradient(s, p, batch, seed, step)
+    for e in list(range(M.SL_W3.start, M.SL_W3.start + 16)) + [4992, 4993]:
+        q = p.copy()
+        q[e] += h
+        _, lp = gcvt_lib.mlp_gradient(s, q, batch, seed, step)
+        q[e] -= 2 * h
+        _, lm = gcvt_lib.mlp_gradient(s, q, batch, seed, step)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[e]) <= 2e-3 * abs(g[e]) + 2e-5, (e, fd, g[e])
+
+
+def test_adam_steps_match_oracle(gcvt_lib, cuda_device):
+    p0 = _params(17)
+    s = _samples(18, 20000)
+    lr, batch, seed = 1e-3, 1024, 4
+    p1, _ = gcvt_lib.mlp_train(s, p0, steps=1, batch=batch, lr=lr, seed=seed)
+    idx = M.sample_indices(seed, 0, batch, len(s))
+    _, g, _ = M.loss_and_gradient(p0, s[idx, :10], s[idx, 10:])
+    want = M.adam(p0.astype(np.float64), g, 0.0, 0.0, lr, 1)[0]
+    # first step: lr * g / (|g| + eps) per parameter; a sign can differ only
+    # where the gradient is at the level of its FP32 rounding
+    big = np.abs(g) > 1e-3 * np.abs(g).max()
+    assert big.mean() > 0.5
+    assert np.all(np.abs(p1 - want)[big] <= 1e-3 * lr + 1e-6)
+    assert np.all(np.abs(p1 - want) <= 2 * lr + 1e-6)
+    p3, loss3 = gcvt_lib.mlp_train(s, p0, steps=3, batch=batch, lr=lr, seed=seed)
+    w3, wloss = M.train(s, p0, 3, batch, lr, seed)
+    assert np.allclose(loss3, wloss, rtol=1e-3)
+    assert np.mean(np.abs(p3 - w3) <= 1e-2 * lr) > 0.99
