@@ -159,6 +159,38 @@ def max_over_ranks(values, ws, device=None):
     return t.tolist()
 
 
+def shard_charts(weights, ws, rank):
+    """The charts rank `rank` of `ws` runs: independent charts split by
+    weight (pixels), largest first onto the least-loaded rank (ties to the
+    lower rank), so every chart runs on exactly one rank; ascending indices."""
+    load = [0] * ws
+    owner = [0] * len(weights)
+    for i in sorted(range(len(weights)), key=lambda i: (-weights[i], i)):
+        r = min(range(ws), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += weights[i]
+    return [i for i in range(len(weights)) if owner[i] == rank]
+
+
+def gather_charts(mine, indices, ws, total):
+    """Per-chart results of every rank, in chart order, on rank 0 (None on the
+    other ranks); with one rank the list as it is.  One gather of Python
+    objects (gloo or NCCL): no data-path collective, the charts are
+    independent."""
+    if ws == 1:
+        return list(mine)
+    import torch.distributed as dist
+    parts = [None] * ws if dist.get_rank() == 0 else None
+    dist.gather_object((list(indices), list(mine)), parts, dst=0)
+    if parts is None:
+        return None
+    out = [None] * total
+    for idx, res in parts:
+        for i, r in zip(idx, res):
+            out[i] = r
+    return out
+
+
 def job_rate(units_per_step, steps, ws, seconds):
     """Whole-job throughput in G units per second: every replica processes
     units_per_step per step, the job takes the slowest replica's seconds."""
@@ -478,9 +510,16 @@ def run_batched(args):
     import torch
     import gcvt_gb300 as G
     from workloads import BATCH, batched_inputs
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
-    charts = batched_inputs(seed=SEED)
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:  # the charts are independent: each rank runs its own share
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    all_charts = batched_inputs(seed=SEED)
+    all_px = [int(s.shape[0]) ** 2 for s, _, _ in all_charts]
+    mine = shard_charts(all_px, ws, rank)
+    charts = [all_charts[i] for i in mine]
     stream = torch.cuda.Stream(device=dev)
     dev_in, ctxs = [], []
     for sites, rho, mask in charts:
@@ -528,21 +567,39 @@ def run_batched(args):
             ms.append(e0.elapsed_time(e1))
         return statistics.mean(ms)
 
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step_batched()
-        with ClockSampler(0) as clk:
+        barrier()
+        with ClockSampler(local) as clk:
             t_b = timed(step_batched, args.steps)
+        barrier()
         energies = [c.info()["energy"] for c in ctxs]
         for _ in range(1):
             step_solo()
         t_s = timed(step_solo, max(1, args.steps // 2))
         same = all(abs(c.info()["energy"] - e) == 0.0 for c, e in zip(ctxs, energies))
+    t_b, t_s, same_all = max_over_ranks([t_b, t_s, 0.0 if same else 1.0], ws, device=dev)
+    per_chart = gather_charts([{"n": int(s.shape[0]), "energy": e} for (s, _, _), e in
+                               zip(charts, energies)], mine, ws, len(all_charts))
+    if rank != 0:
+        batch.close()
+        for c in ctxs:
+            c.close()
+        return 0
+    px = sum(all_px)  # the whole job: every rank's charts
+    sites_total = sum(int((s[..., 0] != -32768).sum()) for s, _, _ in all_charts)
     line = {
         "metric": "Gpix-pass/s, batched uneven charts (64 charts, side 256-2048, 100 iterations)",
-        "value": px * (iters + 1) / (t_b / 1e3) / 1e9, "unit": UNIT, "n_gpus": 1,
+        "value": px * (iters + 1) / (t_b / 1e3) / 1e9, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak",
+        "vs_baseline": None,
         "dtype": "f32+int16", "data": "synthetic (seeded Gaussian densities on disks, uniform sites)",
         "config": {"workload": "batched_64", "charts": len(charts),
                    "sides": sorted({int(s.shape[0]) for s, _, _ in charts}),
@@ -550,7 +607,10 @@ def run_batched(args):
         "solo": {"ms_per_step": t_s, "value": px * (iters + 1) / (t_s / 1e3) / 1e9,
                  "what": "the same charts one after the other, gcvt_ctx_iterate each"},
         "batched_over_solo": t_s / t_b,
-        "same_energies_as_solo": same,
+        "same_energies_as_solo": same_all == 0.0,
+        "sharding": {"ranks": ws, "charts_per_rank": [len(shard_charts(all_px, ws, r))
+                                                      for r in range(ws)],
+                     "gathered_charts": sum(1 for r in per_chart if r is not None)},
         "clocks": clk.summary(),
     }
     if args.reference_gpu:  # 64 gCVT calls of the reference's kernels, one per chart
@@ -558,7 +618,7 @@ def run_batched(args):
         import oracle as orc
         if orc.ref_available():
             loop = total = 0.0
-            for sites, rho, mask in charts:
+            for sites, rho, mask in all_charts:
                 _, info = orc.ref_gcvt(sites, rho, mask, 1, iters, fixed_iters=iters)
                 loop += info["loop_ms"]
                 total += info["total_ms"]

@@ -17,14 +17,18 @@
 //     site came from the same word";
 //   * k_summary: per (band, column), the nearest site row above / below the
 //     band (a scan over bands, 32 columns x 32 band groups per block);
-//   * k_rows: one warp per row.  Lane j owns columns [j*S, (j+1)*S),
-//     S = n/32: it derives each column's candidate from the bitmap word and
-//     summaries (no column-nearest grid is ever written), pushes candidates
-//     (x, B = x^2 + g^2) onto a lower-hull stack in shared memory, five
-//     levels of bridge merges join the 32 hulls, and every lane walks the
-//     joint envelope across its own pixels with division-free breakpoint
-//     tests.  In label mode it writes label words; in Lloyd mode it fuses the
-//     per-site moment and energy accumulation (density read once, 4 B/px).
+//   * k_rows: one warp per row (one row per block).  The lanes derive the
+//     column candidates 32 columns at a time from the bitmap word and the
+//     summaries (no column-nearest grid is ever written); candidate (x, g)
+//     is the point (x, B = x^2 + g^2) and the pixels it wins lie under the
+//     lower convex hull of the points.  The hull is built in shared memory by
+//     rounds of simultaneous chord removal (every point strictly above the
+//     chord of its neighbours goes; the first round is fused into candidate
+//     generation; after 24 rounds a sequential monotone chain finishes any
+//     input), then the lanes write the row's label words from the hull's
+//     breakpoints.  The Lloyd iteration does not use this pass (cells.cu
+//     sums each site's cell directly); it gives the final label grid and the
+//     covering bound at a level's start.
 #include "gcvt_internal.cuh"
 
 namespace cvtgb {

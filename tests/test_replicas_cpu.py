@@ -1,9 +1,11 @@
-"""The multi-GPU path is replicas only (each rank runs the whole hot path on its
-own GPU, no data-path collective); what crosses ranks is the timing: a barrier
-around the timed region and the slowest rank's time, from which rank 0
-reports the whole job's throughput.  This checks that host logic with two
-`gloo` ranks on the CPU, each running a small replica of the labelling pass
-through the oracle."""
+"""The multi-GPU path runs independent work per rank with no data-path
+collective: replicas of one grid (each rank runs the whole hot path on its
+own GPU), or a batch of charts split between the ranks, whose per-chart
+results rank 0 gathers.  What crosses ranks is the timing (a barrier around
+the timed region and the slowest rank's time, from which rank 0 reports the
+whole job's throughput) and, for charts, one gather of their results.  This
+checks that host logic with two `gloo` ranks on the CPU, each running its
+share through the oracle."""
 import os
 import socket
 import sys
@@ -70,3 +72,62 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks([1.5, 2], 1) == [1.5, 2.0]
     assert bench.job_rate(10 ** 9, 2, 1, 4.0) == 0.5
+
+
+def _charts():
+    from workloads import small_case
+    out = []
+    for i, (n, m) in enumerate(((256, 300), (256, 150), (512, 900), (256, 500), (512, 400))):
+        out.append(small_case(n, m, seed=60 + i))
+    return out
+
+
+def _chart_result(oracle, sites, rho, mask):
+    labels, st = oracle.gcvt(sites, rho, mask, 1, 6, mode=oracle.EXACT, fixed_iters=6)
+    return {"n": int(sites.shape[0]), "iterations": int(st["iterations"]),
+            "energy": float(st["last_energy"]),
+            "labels": int(np.frombuffer(labels.tobytes(), np.uint32).astype(np.uint64).sum())}
+
+
+def _shard_main(rank, ws, port, out_dir):
+    import torch.distributed as dist
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"),
+                    os.path.join(ROOT, "surface-remesher_gb300", "python")]
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank,
+                            world_size=ws)
+    import bench
+    import oracle
+    charts = _charts()
+    weights = [int(c[0].shape[0]) ** 2 for c in charts]
+    mine = bench.shard_charts(weights, ws, rank)
+    res = [_chart_result(oracle, *charts[i]) for i in mine]
+    got = bench.gather_charts(res, mine, ws, len(charts))
+    if rank == 0:
+        np.save(os.path.join(out_dir, "gathered.npy"), np.array(got, dtype=object),
+                allow_pickle=True)
+    else:
+        assert got is None
+    dist.destroy_process_group()
+
+
+def test_charts_shard_across_two_gloo_ranks(tmp_path):
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"),
+                    os.path.join(ROOT, "surface-remesher_gb300", "python")]
+    import bench
+    import oracle
+    charts = _charts()
+    weights = [int(c[0].shape[0]) ** 2 for c in charts]
+    # every chart on exactly one rank, the heavy ones spread
+    parts = [bench.shard_charts(weights, 2, r) for r in range(2)]
+    assert sorted(parts[0] + parts[1]) == list(range(len(charts)))
+    loads = [sum(weights[i] for i in p) for p in parts]
+    assert max(loads) - min(loads) <= max(weights)
+    assert bench.shard_charts(weights, 1, 0) == list(range(len(charts)))
+    ws = 2
+    mp.start_processes(_shard_main, args=(ws, _free_port(), str(tmp_path)), nprocs=ws,
+                       join=True, start_method="spawn")
+    got = list(np.load(os.path.join(tmp_path, "gathered.npy"), allow_pickle=True))
+    want = [_chart_result(oracle, *c) for c in charts]
+    assert got == want
