@@ -115,29 +115,89 @@ def jfa_line(n, ms, stats, peak, halo=16):
             "mislabel_rate": stats[0] / stats[2], "farther_rate": stats[1] / stats[2]}
 
 
-def time_to_energy_line(G, ctx, n, sites, rho, mask, conv_iters=1000, jump_every=4):
-    """Seconds until the energy is within 1e-4 of the energy after 1000 plain
-    iterations: plain Lloyd, and Lloyd with gated jumps of the learned step
-    MLP (surface-remesher_gb300/data/step_mlp.npy), energies read every 10
-    iterations."""
+JUMP_EVERY = 4  # learned runs: rounds of three plain iterations and one learned step
+
+
+def time_to_energy_line(G, ctx, n, sites, rho, mask, conv_iters=1000, jump_every=JUMP_EVERY,
+                        repeats=3):
+    """Time until the energy is within 1e-4 of the energy after 1000 plain
+    iterations (E_conv), for plain Lloyd, for Lloyd with the learned step
+    (surface-remesher_gb300/data/step_mlp.npy) on one context, and for the same
+    learned run through the batch API (persistent batched kernels, one MLP
+    launch for the batch).  The device stops each run at the first iteration
+    whose energy meets the target (gcvt_ctx_set_target_energy); CUDA events
+    around the run on its stream; median of `repeats` after one warm-up."""
     from train_step_mlp import DATA, time_to_energy
+    ctx.set_target_energy(0)
     ctx.load(sites, rho, mask)
     ctx.iterate(conv_iters)
     e_conv = ctx.info()["energy"]
     target = e_conv * (1 + 1e-4)
-    plain = time_to_energy(ctx, sites, rho, mask, target, False, 0, conv_iters)
+
+    def med(fn):
+        fn()
+        runs = [fn() for _ in range(repeats)]
+        runs.sort(key=lambda r: r[0])
+        return runs[len(runs) // 2]
+
+    plain = med(lambda: time_to_energy(ctx, sites, rho, mask, target, False, 0, conv_iters))
     params = np.load(os.path.join(DATA, "step_mlp.npy"))
     lctx = G.Context(n)
     lctx.learning(True)
     lctx.set_mlp(params)
-    learned = time_to_energy(lctx, sites, rho, mask, target, True, jump_every, conv_iters)
+    learned = med(lambda: time_to_energy(lctx, sites, rho, mask, target, True, jump_every,
+                                         conv_iters))
+    batched = med(lambda: batched_time_to_energy(G, [lctx], [(sites, rho, mask)], [target],
+                                                 params, jump_every, conv_iters))
     lctx.close()
-    return {"target": "E <= (1 + 1e-4) E after %d plain iterations" % conv_iters,
-            "e_conv": e_conv,
+    return {"target": "E <= (1 + 1e-4) E_conv, E_conv = energy after %d plain iterations"
+                      % conv_iters,
+            "e_conv": e_conv, "stop": "on the device at the first iteration meeting the target",
             "plain_ms": plain[0] * 1e3, "plain_iterations": plain[1],
             "learned_ms": learned[0] * 1e3, "learned_iterations": learned[1],
             "jumps_tried": learned[2], "jumps_kept": learned[3], "jump_every": jump_every,
-            "learned_over_plain": plain[0] / learned[0]}
+            "learned_over_plain": plain[0] / learned[0],
+            "learned_batched_ms": batched[0] * 1e3, "learned_batched_iterations": batched[1],
+            "learned_batched_over_plain": plain[0] / batched[0]}
+
+
+def batched_time_to_energy(G, ctxs, inputs, targets, params, jump_every, limit):
+    """(seconds, iterations of the slowest chart, jumps tried, kept): the
+    charts' learned runs as one batch, each chart stopped on the device at its
+    own target."""
+    import torch
+    stream = torch.cuda.Stream()
+    for c, (s, r, m), t in zip(ctxs, inputs, targets):
+        c.set_stream(stream.cuda_stream)
+        c.set_target_energy(t)
+        c.load(s, r, m)
+    b = G.Batch(ctxs)
+    b.set_stream(stream.cuda_stream)
+    b.set_mlp(params)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tried, kept = b.iterate_learned(limit, jump_every)
+    e1.record(stream)
+    e1.synchronize()
+    its = max(c.info()["iterations"] for c in ctxs)
+    b.close()
+    for c in ctxs:
+        c.set_target_energy(0)
+        c.set_stream(None)
+    return e0.elapsed_time(e1) / 1e3, its, tried, kept
+
+
+def time_to_energy_8192(G):
+    """The learned+batched headline on the largest configuration: 8192^2, 64
+    Gaussians, 1,048,576 sites (seeded as the other workloads)."""
+    from workloads import config_inputs
+    sites, rho, mask, _ = config_inputs("plain_8192", seed=SEED)
+    ctx = G.Context(8192)
+    line = time_to_energy_line(G, ctx, 8192, sites, rho, mask)
+    ctx.close()
+    line["workload"] = "plain_8192 (8192^2, 64 Gaussians, 1,048,576 sites)"
+    return line
 
 
 def dist_env():
@@ -396,8 +456,11 @@ def run_ours(args):
         for _ in range(max(1, args.warmup // 2)):
             step_host()
         t_e2e = timed(step_host, args.steps)
-        # time to E <= (1 + 1e-4) E_conv, plain and with gated learned jumps
+        # time to E <= (1 + 1e-4) E_conv: plain, learned, learned + batched
         tte = time_to_energy_line(G, ctx, n, sites, rho, mask)
+        ctx.set_stream(stream.cuda_stream)  # the timing runs used a stream of their own
+        tte_8192 = (time_to_energy_8192(G) if rank == 0 and not args.no_headline
+                    and workload != "plain_8192" else None)
         # the Delaunay triangulation of the converged sites (outside the timing)
         _, delaunay = delaunay_stage(ctx, G.load_library(), len(ctx.extract_points()), args)
         # a labelling pass (final output) and a jump-flooding labelling,
@@ -429,6 +492,7 @@ def run_ours(args):
         "jfa": jfa_line(n, kms[2], jfa_stats, peak, tuning["jfa_tail_halo"]),
         "tuning": tuning,
         "time_to_energy": tte,
+        "time_to_energy_8192": tte_8192,
         "delaunay": delaunay,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(workload),
@@ -452,8 +516,11 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample(sites, rho, mask, workload=workload,
                                                        iters=iters)
-        if args.reference_gpu:
+        if not args.no_reference_gpu:
             line["reference_gpu"] = reference_gpu(sites, rho, mask, iters)
+            rg = line["reference_gpu"]
+            if "loop_ms" in rg:
+                rg["ours_over_reference"] = rg["loop_ms"] / line["ms_per_step"]
         print(json.dumps(line))
     ctx.close()
     if ws > 1:
@@ -898,7 +965,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--reference-gpu", action="store_true",
-                    help="also time the reference's own kernels on this GPU")
+                    help="batched_64: also time the reference's own kernels on this GPU")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="plain workloads: skip timing the reference's own kernels on this GPU")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="skip the 8192^2 time-to-energy line (plain vs learned vs learned+batched)")
     ap.add_argument("--profile-case", type=int, default=0, metavar="ITERS",
                     help="only run ITERS Lloyd iterations of the workload (for ncu)")
     ap.add_argument("--config", default=CONFIG,

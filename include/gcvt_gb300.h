@@ -60,7 +60,7 @@ typedef struct {
     float jfa_ms;           /* autotune: best time of one jump-flooding labelling (ms)   */
     int cell_mode;          /* Lloyd cells: 0 = one site per warp up to 8192 sites, else
                                one per lane; 1 = one per lane; 2 = one per warp (up to
-                               8192 sites, and not while learned steps are enabled)     */
+                               8192 sites; a learned step's two passes run one per lane) */
 } gcvt_tuning;
 
 /* Human-readable text of a status code. */
@@ -153,12 +153,17 @@ int gcvt_ctx_set_tuning(gcvt_ctx *ctx, const gcvt_tuning *tuning);
 /* ---- learned steps ------------------------------------------------------
  * No reference counterpart.  A per-site MLP (10 -> 64 -> 64 -> 2, ReLU,
  * bfloat16 weights and activations, FP32 accumulation) maps a site's last
- * four Lloyd moves and the density gradient over the density at the site,
- * in units of the mean cell radius r, to a predicted displacement (in r) of
- * the site towards the converged tessellation.  A jump moves every free site
- * by its prediction and is kept only if the energy of the jumped sites is
- * lower than before; otherwise the state is restored and the plain Lloyd
- * iterations go on, so the plain method is both fallback and judge. */
+ * four Lloyd displacements -- the pending one (its cell's centroid minus the
+ * site, not yet rounded) and the last three applied moves -- and the density
+ * gradient over the density at the site, all in units of the mean cell
+ * radius r, to a predicted displacement (in r) of the site towards the
+ * converged tessellation.  A learned step proposes, in place of a plain
+ * Lloyd step from the sites S, the jumped sites L = S + prediction; the
+ * plain Lloyd iteration of L measures E(L) and the step stands only if
+ * E(L) < E(S); otherwise the plain step's sites are taken, exactly as
+ * without the jump -- the plain method is both fallback and judge.  An
+ * accepted step costs no extra cell pass (the iteration of L is the next
+ * Lloyd iteration); a rejected one costs one. */
 
 /* Number of MLP parameters: W1[10][64], b1[64], W2[64][64], b2[64], W3[64][2], b3[2]. */
 int gcvt_mlp_param_count(void);
@@ -176,11 +181,20 @@ int gcvt_ctx_set_mlp(gcvt_ctx *ctx, const float *params, int count);
  * capacity sites; *count = the number of sites. */
 int gcvt_ctx_features(gcvt_ctx *ctx, float *feat, int *ids, int *xy, int capacity, int *count);
 
-/* `iterations` plain Lloyd iterations with a gated jump after every
- * `jump_every` of them (iterations jump_every, 2 jump_every, ...);
- * *tried / *kept (may be NULL) count the jumps. */
+/* `iterations` Lloyd iterations in rounds of jump_every - 1 plain iterations
+ * and one learned step (two iterations when its jump stands, one when it
+ * does not); the run ends after exactly `iterations` iterations, or earlier
+ * at a target energy (gcvt_ctx_set_target_energy).  *tried / *kept (may be
+ * NULL) count the jumps. */
 int gcvt_ctx_iterate_learned(gcvt_ctx *ctx, int iterations, int jump_every, int *tried,
                              int *kept);
+
+/* Time-to-energy runs: with target > 0 every later run of this context at
+ * full resolution (gcvt_ctx_iterate, gcvt_ctx_iterate_learned, gcvt_ctx_run,
+ * batches) also stops after the first iteration whose energy is at most
+ * `target`; 0 turns it off.  No reference counterpart (gCVT's own stop rule,
+ * gcvt.cu:1125-1142, is unchanged beside it). */
+int gcvt_ctx_set_target_energy(gcvt_ctx *ctx, double target);
 
 /* The MLP on host feature vectors (count x 10) -> predictions (count x 2):
  * tensor_cores != 0 runs layers 1 and 2 as tcgen05.mma (bfloat16 operands in
@@ -232,6 +246,32 @@ int gcvt_ctx_extract_points(gcvt_ctx *ctx, double scale, double left, double low
  * has more than 64 Delaunay neighbours. */
 int gcvt_ctx_delaunay(gcvt_ctx *ctx, int32_t *triangles, int capacity, int *count, int mem);
 
+/* The constrained Delaunay triangulation of the CDT stage (main.cpp:229-236:
+ * gDel2D's GpuDel::compute, gDel2D/GPU/GpuDelaunay.cu:46, on
+ * delaunayInput's points and segments, delaunay.h:30-79), on the GPU.
+ * Points: the current free sites, in gcvt_ctx_extract_points' order
+ * (indices 0 .. F-1), then the num_cpoints constraint points (FP64 pairs
+ * in the frame x * scale + left, y * scale + lower of the sites; indices
+ * F .. F + num_cpoints - 1).  segments: num_segments index pairs into that
+ * list, each made an edge of the result (gDel2D's constraintVec; a segment
+ * with points exactly inside it becomes the chain of edges between them).
+ * Writes
+ * min(count, capacity) triangles (3 point indices, counter-clockwise, each
+ * starting at its smallest index, ordered by that index and then the
+ * second) to triangles and their number to *count.  Predicates are exact:
+ * sites on their pixel lattice, constraint points rounded to 2^-15 of a
+ * pixel (snapped coordinates beyond 2^14 pixels from the grid are
+ * rejected); co-circular points are split by the symbolic perturbation of
+ * gcvt_ctx_delaunay, constraint points ranking above every site.
+ * GCVT_ERR_INPUT (with *detail, may be NULL, set to a reason mask: 1
+ * coordinate range, 2 a constraint point on another point, 16 two
+ * segments crossing, or a bad index pair) when the input cannot be
+ * triangulated so; GCVT_ERR_CUDA (detail 4, 8, 32, 64) when an internal
+ * bound ran out.  Host-synchronous. */
+int gcvt_ctx_cdt(gcvt_ctx *ctx, double scale, double left, double lower, const double *cpoints,
+                 int num_cpoints, const int32_t *segments, int num_segments, int32_t *triangles,
+                 int capacity, int *count, int *detail, int mem);
+
 /* ---- batches: many charts, one launch pair per iteration ---------------
  * No reference counterpart: the reference runs one chart per gCVT call.  A
  * batch groups loaded contexts (any mix of sizes, one device); its
@@ -250,6 +290,16 @@ int gcvt_batch_destroy(gcvt_batch *batch);
 int gcvt_batch_set_stream(gcvt_batch *batch, void *stream);
 /* `iterations` plain Lloyd iterations of every member (fixed count). */
 int gcvt_batch_iterate(gcvt_batch *batch, int iterations);
+/* The MLP parameters of the batch's learned steps (FP32 host array of
+ * gcvt_mlp_param_count() floats); one network for every chart. */
+int gcvt_batch_set_mlp(gcvt_batch *batch, const float *params, int count);
+/* gcvt_ctx_iterate_learned over every member at once (each must have
+ * learned steps enabled, gcvt_ctx_learning): per round one site-list and
+ * one persistent cell launch per plain iteration, and for the learned step
+ * one MLP launch over all charts' sites; every chart judges its own jumps,
+ * so its result is its solo learned run's.  *tried / *kept sum the charts. */
+int gcvt_batch_iterate_learned(gcvt_batch *batch, int iterations, int jump_every, int *tried,
+                               int *kept);
 /* gCVT's schedule on every member at depth 1: each chart runs until its own
  * stop rule or max_iter (gcvt.cu:1105-1147); infos (may be NULL) receives
  * one gcvt_run_info per member. */

@@ -263,3 +263,70 @@ def hull_size_fast(points):
                   (np.minimum(a[1], b[1]) <= pts[:, 1]) & (pts[:, 1] <= np.maximum(a[1], b[1])))
         on |= (cr == 0) & inside
     return int(on.sum()), cs
+
+
+# ---------------------------------------------------------------------------
+# Constrained Delaunay triangulations (the CDT stage's output)
+# ---------------------------------------------------------------------------
+
+def check_cdt(points, tris, segments, ranks):
+    """Raise AssertionError unless tris is the constrained Delaunay
+    triangulation of the integer points (V, 2) with the constraint segments
+    (index pairs), under the symbolic perturbation by `ranks` (a larger rank
+    perturbs more); returns a dict of counts.  Restates gDel2D's
+    DelaunayChecker (gDel2D/DelaunayChecker.cpp:27-87 checkEuler, :99-144
+    checkAdjacency, :146-169 checkOrientation, :171-213 checkDelaunay, which
+    skips edges facing a constraint, and checkConstraints at :215-330, which
+    looks every segment up as an edge; a segment through other points is the
+    chain of edges between them) in exact Python integers, plus the
+    coverage of the convex hull and the 2V - h - 2 triangle count.  With no
+    unconstrained edge failing the perturbed incircle test and every segment
+    an edge, the triangulation is the constrained Delaunay one (unique under
+    the perturbation)."""
+    pts = [(int(x), int(y)) for x, y in np.asarray(points).tolist()]
+    T = [tuple(int(v) for v in t) for t in np.asarray(tris).reshape(-1, 3).tolist()]
+    v = len(pts)
+    h, corners = hull_size(np.asarray(points, np.int64))
+    assert len(corners) >= 3, "collinear input"
+    assert len(T) == 2 * v - h - 2, f"{len(T)} triangles, expected {2 * v - h - 2}"
+    area = 0
+    for a, b, c in T:
+        assert 0 <= min(a, b, c) and max(a, b, c) < v, "index out of range"
+        o = _orient(pts[a], pts[b], pts[c])
+        assert o > 0, f"triangle {(a, b, c)} not counter-clockwise"
+        area += o
+    hull2 = sum(_orient(corners[0], corners[i], corners[i + 1]) for i in range(1, len(corners) - 1))
+    assert area == hull2, "triangles do not tile the hull"
+    opp = {}
+    for t, (i, j, k) in enumerate(T):
+        for e, w in (((i, j), k), ((j, k), i), ((k, i), j)):
+            assert e not in opp, f"directed edge {e} twice"
+            opp[e] = (t, w)
+    edges = {tuple(sorted(e)) for e in opp}
+    assert len({q for t in T for q in t}) == v, "points not in any triangle"
+    assert v - len(edges) + len(T) == 1, "Euler characteristic"
+    cons = set()
+    for a, b in np.asarray(segments).reshape(-1, 2).tolist():
+        # a segment with points exactly inside it is the chain of edges
+        # between them
+        pa, pb = pts[a], pts[b]
+        dx, dy = pb[0] - pa[0], pb[1] - pa[1]
+        inner = sorted((((q[0] - pa[0]) * dx + (q[1] - pa[1]) * dy), k) for k, q in enumerate(pts)
+                       if k not in (a, b) and _orient(pa, pb, q) == 0
+                       and 0 < (q[0] - pa[0]) * dx + (q[1] - pa[1]) * dy < dx * dx + dy * dy)
+        chain = [a] + [k for _, k in inner] + [b]
+        for u, w in zip(chain, chain[1:]):
+            e = (min(u, w), max(u, w))
+            assert e in edges, f"constraint segment {(a, b)}: {e} is not an edge"
+            cons.add(e)
+    ties = 0
+    for (i, j), (t, w) in opp.items():
+        if (j, i) not in opp or (min(i, j), max(i, j)) in cons:
+            continue
+        _, x = opp[(j, i)]
+        assert not sos_in_circle(pts[i], pts[j], pts[w], pts[x], ranks[i], ranks[j], ranks[w],
+                                 ranks[x]), f"edge {(i, j)} not locally Delaunay"
+        det, _ = _incircle(pts[i], pts[j], pts[w], pts[x])
+        ties += det == 0
+    return {"vertices": v, "edges": len(edges), "triangles": len(T), "hull": h,
+            "constraints": len(cons), "cocircular_edges": ties // 2}

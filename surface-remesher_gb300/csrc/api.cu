@@ -61,10 +61,14 @@ struct gcvt_ctx {
   // bfloat16-rounded MLP parameters
   int learning = 0, track_ids = 0, have_mlp = 0;
   int mlp_tensor_cores = 1;  // MLP forward on tcgen05 (else CUDA cores)
-  uint64_t *hist[2] = {};
-  int *ids[2] = {};
+  uint64_t *hist[3] = {};    // one per site bitmap
+  int *ids[3] = {};
   float *feat = nullptr, *pred = nullptr, *mlp_bf = nullptr;
+  uint32_t *jaux = nullptr;  // per list slot: the window of the site's cell
+  DevState *gsave = nullptr; // the state a rejected jump restores
+  LevelBufs *desc = nullptr; // device copy of the level's buffers (learned steps)
   size_t feat_cap = 0;
+  double target_energy = 0;  // gcvt_ctx_set_target_energy
   int cover_valid = 0;          // the covering bound, list counts and hints
                                 // fit the current sites
   double *moments = nullptr;    // 4*n_max^2 doubles, allocated on first use
@@ -113,13 +117,14 @@ LevelBufs level_bufs(gcvt_ctx *c, int n, int level) {
     b.gcnt = c->gcnt;
   }
   if (c->learning && level == 0) {
-    b.hist[0] = c->hist[0];
-    b.hist[1] = c->hist[1];
-    if (c->track_ids) {
-      b.ids[0] = c->ids[0];
-      b.ids[1] = c->ids[1];
+    for (int k = 0; k < 3; ++k) {
+      b.hist[k] = c->hist[k];
+      if (c->track_ids) b.ids[k] = c->ids[k];
     }
     b.feat = c->feat;
+    b.pred = c->pred;
+    b.jaux = c->jaux;
+    b.gsave = c->gsave;
   }
   return b;
 }
@@ -210,7 +215,7 @@ int ensure_cover(gcvt_ctx *c, int n, int level) {
   const size_t nlb = list_blocks(n);
   CK(cudaMemsetAsync(c->counts[(c->st_host->cur + 1) % 3], 0, nlb * sizeof(unsigned), c->stream));
   if (c->learning && level == 0) {  // no moves yet; ids = list positions
-    CK(cudaMemsetAsync(c->hist[c->st_host->hist_cur], 0, (size_t)n * n * sizeof(uint64_t),
+    CK(cudaMemsetAsync(c->hist[c->st_host->cur], 0, (size_t)n * n * sizeof(uint64_t),
                        c->stream));
     if (c->track_ids) {
       CK(launch_list(b, 0, c->stream));
@@ -261,6 +266,7 @@ int start_level(gcvt_ctx *c, int n, int level, int fixed, int max_iter) {
   h.done_blocks = 0;
   h.hint_slack = c->hint_slack;
   h.feat_scale = radius;
+  h.target_energy = level == 0 ? c->target_energy : 0.0;
   if ((rc = push_state(c))) return rc;
   c->cur_n = n;
   return ensure_cover(c, n, level);
@@ -466,12 +472,15 @@ int gcvt_ctx_destroy(gcvt_ctx *c) {
   cudaFree(c->gcnt);
   cudaFree(c->colcnt);
   cudaFree(c->jfa);
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < 3; ++k) {
     cudaFree(c->hist[k]);
     cudaFree(c->ids[k]);
   }
   cudaFree(c->feat);
   cudaFree(c->pred);
+  cudaFree(c->jaux);
+  cudaFree(c->gsave);
+  cudaFree(c->desc);
   cudaFree(c->mlp_bf);
   cudaFree(c->moments);
   cudaFree(c->err);
@@ -523,7 +532,7 @@ int gcvt_ctx_iterate(gcvt_ctx *c, int iterations) {
   if (c->input_err) return GCVT_ERR_INPUT;
   if (iterations == 0) return GCVT_OK;
   if (c->cur_n != c->n) return GCVT_ERR_STATE;
-  return run_level(c, c->n, 0, iterations, 0x7fffffff, 0);
+  return run_level(c, c->n, 0, iterations, 0x7fffffff, c->target_energy > 0.0);
 }
 
 int gcvt_ctx_run(gcvt_ctx *c, int depth, int max_iter, gcvt_run_info *info) {
@@ -663,6 +672,57 @@ int gcvt_ctx_delaunay(gcvt_ctx *c, int32_t *triangles, int capacity, int *count,
       rc = copy_out(triangles, dst, written * 3 * sizeof(int32_t), GCVT_MEM_HOST, c->stream);
   }
   if (owned) cudaFree(dst);
+  return rc;
+}
+
+int gcvt_ctx_cdt(gcvt_ctx *c, double scale, double left, double lower, const double *cpoints,
+                 int num_cpoints, const int32_t *segments, int num_segments, int32_t *triangles,
+                 int capacity, int *count, int *detail, int mem) {
+  if (!c || !count || capacity < 0 || (capacity > 0 && !triangles) || num_cpoints < 0 ||
+      num_segments < 0 || (num_cpoints && !cpoints) || (num_segments && !segments))
+    return GCVT_ERR_ARGUMENT;
+  if (mem != GCVT_MEM_HOST && mem != GCVT_MEM_DEVICE) return GCVT_ERR_ARGUMENT;
+  if (!c->loaded) return GCVT_ERR_STATE;
+  if (c->input_err) return GCVT_ERR_INPUT;
+  int rc = pull_state(c);
+  if (rc) return rc;
+  const int n = c->cur_n;
+  const int level = level_of(c, n);
+  const double *dpts = cpoints;
+  const int *dsegs = segments;
+  int *dtri = triangles;
+  void *stage = nullptr;
+  if (mem == GCVT_MEM_HOST) {  // device copies of the inputs and the triangles
+    const size_t bp = (size_t)num_cpoints * 2 * sizeof(double),
+                 bs = (size_t)num_segments * 2 * sizeof(int32_t),
+                 bt = (size_t)capacity * 3 * sizeof(int32_t);
+    if (cudaMalloc(&stage, bp + bs + bt + 64) != cudaSuccess) return GCVT_ERR_ALLOC;
+    char *q = static_cast<char *>(stage);
+    dpts = reinterpret_cast<const double *>(q);
+    dsegs = reinterpret_cast<const int *>(q + bp);
+    dtri = reinterpret_cast<int *>(q + ((bp + bs + 15) & ~(size_t)15));
+    if ((bp && cudaMemcpyAsync(q, cpoints, bp, cudaMemcpyHostToDevice, c->stream) !=
+                   cudaSuccess) ||
+        (bs && cudaMemcpyAsync(q + bp, segments, bs, cudaMemcpyHostToDevice, c->stream) !=
+                   cudaSuccess)) {
+      cudaFree(stage);
+      return GCVT_ERR_CUDA;
+    }
+  }
+  unsigned total = 0;
+  rc = cdt_compute(c->bits[c->st_host->cur], c->fixed_bits[level], n, c->colcnt, dpts,
+                   num_cpoints, dsegs, num_segments, scale, left, lower, dtri,
+                   (unsigned)capacity, &total, detail, c->stream);
+  if (!rc) {
+    *count = (int)total;
+    const size_t written = total < (unsigned)capacity ? total : (unsigned)capacity;
+    if (mem == GCVT_MEM_HOST && written)
+      rc = copy_out(triangles, dtri, written * 3 * sizeof(int32_t), GCVT_MEM_HOST, c->stream);
+  }
+  if (stage) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(stage);
+  }
   return rc;
 }
 
@@ -881,7 +941,7 @@ int gcvt_mlp_param_count(void) { return mlp_param_count(); }
 int gcvt_ctx_learning(gcvt_ctx *c, int enable, int track_ids) {
   if (!c) return GCVT_ERR_ARGUMENT;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return GCVT_ERR_CUDA;
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < 3; ++k) {
     cudaFree(c->hist[k]);
     cudaFree(c->ids[k]);
     c->hist[k] = nullptr;
@@ -896,13 +956,17 @@ int gcvt_ctx_learning(gcvt_ctx *c, int enable, int track_ids) {
   if (!enable) return GCVT_OK;
   const size_t nn = (size_t)c->n_max * c->n_max;
   bool ok = true;
-  for (int k = 0; k < 2 && ok; ++k)
+  for (int k = 0; k < 3 && ok; ++k)
     ok = cudaMalloc(reinterpret_cast<void **>(&c->hist[k]), nn * sizeof(uint64_t)) == cudaSuccess;
-  for (int k = 0; k < 2 && ok && track_ids; ++k)
+  for (int k = 0; k < 3 && ok && track_ids; ++k)
     ok = cudaMalloc(reinterpret_cast<void **>(&c->ids[k]), nn * sizeof(int)) == cudaSuccess;
   if (ok && !c->mlp_bf)
     ok = cudaMalloc(reinterpret_cast<void **>(&c->mlp_bf), mlp_param_count() * sizeof(float)) ==
          cudaSuccess;
+  if (ok && !c->gsave)
+    ok = cudaMalloc(reinterpret_cast<void **>(&c->gsave), sizeof(DevState)) == cudaSuccess;
+  if (ok && !c->desc)
+    ok = cudaMalloc(reinterpret_cast<void **>(&c->desc), sizeof(LevelBufs)) == cudaSuccess;
   if (!ok) {
     gcvt_ctx_learning(c, 0, 0);
     return GCVT_ERR_ALLOC;
@@ -921,36 +985,42 @@ int ensure_feat(gcvt_ctx *c) {
   if (c->feat_cap >= need) return GCVT_OK;
   cudaFree(c->feat);
   cudaFree(c->pred);
+  cudaFree(c->jaux);
   c->feat = c->pred = nullptr;
+  c->jaux = nullptr;
   c->feat_cap = 0;
   if (c->chunk_exec) {
     cudaGraphExecDestroy(c->chunk_exec);
     c->chunk_exec = nullptr;
   }
   if (cudaMalloc(reinterpret_cast<void **>(&c->feat), need * 10 * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(reinterpret_cast<void **>(&c->pred), need * 2 * sizeof(float)) != cudaSuccess)
+      cudaMalloc(reinterpret_cast<void **>(&c->pred), need * 2 * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(reinterpret_cast<void **>(&c->jaux), need * sizeof(uint32_t)) != cudaSuccess)
     return GCVT_ERR_ALLOC;
+  CK(cudaMemsetAsync(c->feat, 0, need * 10 * sizeof(float), c->stream));
   c->feat_cap = need;
   return GCVT_OK;
 }
 
-// One gated jump from the current sites (after a plain iteration or a level
-// start): features pass, MLP, jumped sites, energy pass, keep or undo.
+// One learned step (two Lloyd iterations when the jump stands, one when it
+// does not): the plain iteration from the current sites with their features,
+// the MLP, the jumped sites, their iteration (which judges the jump), and the
+// gate's resolution.  Every launch reads the device state, so a level that
+// has stopped makes them all no-ops.
 int enqueue_jump(gcvt_ctx *c) {
   const int n = c->n;
   const LevelBufs b = level_bufs(c, n, 0);
-  const int grid = 4 * 152;
-  CK(launch_list(b, 0, c->stream));
-  CK(launch_cells(b, 2, nullptr, c->stream, c->cell_grid));
+  CK(launch_list(b, 1, c->stream));
+  CK(launch_cells(b, 4, nullptr, c->stream, c->cell_grid));
   if (c->mlp_tensor_cores)
     CK(launch_mlp_tc(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, c->err, c->stream));
   else
-    CK(launch_mlp_infer(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, grid, c->stream));
-  CK(launch_apply(b, c->pred, grid, c->stream));
-  CK(launch_gate_switch(c->st, n, c->stream));
-  CK(launch_list(b, 0, c->stream));
-  CK(launch_cells(b, 3, nullptr, c->stream, c->cell_grid));
-  CK(launch_gate_resolve(b, grid, c->stream));
+    CK(launch_mlp_infer(c->feat, &c->st->snap_count, c->mlp_bf, c->pred, 4 * 152, c->stream));
+  CK(launch_apply(c->desc, 1, c->stream));
+  CK(launch_gate_switch(c->desc, 1, c->stream));
+  CK(launch_list(b, 1, c->stream));
+  CK(launch_cells(b, 5, nullptr, c->stream, c->cell_grid));
+  CK(launch_gate_resolve(c->desc, 1, c->stream));
   return GCVT_OK;
 }
 }  // namespace
@@ -1018,24 +1088,37 @@ int gcvt_ctx_iterate_learned(gcvt_ctx *c, int iterations, int jump_every, int *t
   if (!c->loaded || !c->learning || !c->have_mlp) return GCVT_ERR_STATE;
   if (c->input_err) return GCVT_ERR_INPUT;
   if (c->cur_n != c->n) return GCVT_ERR_STATE;
+  if (iterations == 0) return GCVT_OK;
   int rc = ensure_feat(c);
   if (rc) return rc;
-  if ((rc = start_level(c, c->n, 0, iterations > 0 ? iterations : 1, 0x7fffffff))) return rc;
+  if ((rc = start_level(c, c->n, 0, iterations, 0x7fffffff))) return rc;
+  const LevelBufs b = level_bufs(c, c->n, 0);
+  CK(cudaMemcpyAsync(c->desc, &b, sizeof(LevelBufs), cudaMemcpyHostToDevice, c->stream));
   if ((rc = pull_state(c))) return rc;
   const int tried0 = c->st_host->gate_tried, kept0 = c->st_host->gate_kept;
-  const LevelBufs b = level_bufs(c, c->n, 0);
-  for (int done = 0; done < iterations;) {
-    const int k = iterations - done < jump_every ? iterations - done : jump_every;
-    for (int i = 0; i < k; ++i) {
-      CK(launch_list(b, 1, c->stream));
-      CK(launch_cells(b, 0, nullptr, c->stream, c->cell_grid));
+  // rounds of (jump_every - 1) plain iterations and one learned step until
+  // the device schedule has run `iterations` iterations (or met the target
+  // energy); the state is read back every ten or more iterations
+  const int per_poll = (kChunk + jump_every - 1) / jump_every;
+  for (;;) {
+    for (int r = 0; r < per_poll; ++r) {
+      for (int i = 0; i + 1 < jump_every; ++i) {
+        CK(launch_list(b, 1, c->stream));
+        CK(launch_cells(b, 0, nullptr, c->stream, c->cell_grid));
+      }
+      if ((rc = enqueue_jump(c))) return rc;
     }
-    done += k;
-    if (k == jump_every && (rc = enqueue_jump(c))) return rc;
+    if ((rc = pull_state(c))) return rc;
+    if (c->st_host->stopped) break;
   }
-  if ((rc = pull_state(c))) return rc;
   if (tried) *tried = c->st_host->gate_tried - tried0;
   if (kept) *kept = c->st_host->gate_kept - kept0;
+  return GCVT_OK;
+}
+
+int gcvt_ctx_set_target_energy(gcvt_ctx *c, double target) {
+  if (!c || !(target >= 0.0)) return GCVT_ERR_ARGUMENT;
+  c->target_energy = target;
   return GCVT_OK;
 }
 
@@ -1299,6 +1382,15 @@ struct gcvt_batch {
   std::vector<LevelBufs> host_descs;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev = nullptr;    // orders the batch's stream with its members' streams
+  // learned steps over the batch: every chart's list slots in one feature /
+  // prediction / window array (chart i from slot_ofs[i]), one MLP launch
+  float *mlp_bf = nullptr;
+  float *feat = nullptr, *pred = nullptr;
+  uint32_t *jaux = nullptr;
+  int *mlp_count = nullptr;    // device: slots the MLP runs over; [1]: its error flag
+  size_t feat_cap = 0;
+  std::vector<size_t> slot_ofs;
+  bool learned = false;        // the descriptors point into the arrays above
 };
 
 namespace {
@@ -1321,6 +1413,11 @@ int batch_start(gcvt_batch *b, int fixed, int max_iter) {
     c->stream = keep;
     if (rc) return rc;
     b->host_descs[i] = level_bufs(c, c->n, 0);
+    if (b->learned) {
+      b->host_descs[i].feat = b->feat + b->slot_ofs[i] * 10;
+      b->host_descs[i].pred = b->pred + b->slot_ofs[i] * 2;
+      b->host_descs[i].jaux = b->jaux + b->slot_ofs[i];
+    }
     lofs[i + 1] = lofs[i] + (unsigned)list_blocks(c->n);
   }
   if (lofs.back() != b->nblocks && b->exec) {  // the captured grid no longer fits
@@ -1340,6 +1437,48 @@ int batch_start(gcvt_batch *b, int fixed, int max_iter) {
 int batch_finish(gcvt_batch *b) {
   CK(cudaEventRecord(b->ev, b->stream));
   for (gcvt_ctx *c : b->charts) CK(cudaStreamWaitEvent(c->stream, b->ev, 0));
+  return GCVT_OK;
+}
+
+// Feature, prediction and window slots for every member's sites (their
+// counts at load; merges only lower them).
+int batch_feat(gcvt_batch *b) {
+  b->slot_ofs.assign(b->charts.size() + 1, 0);
+  for (size_t i = 0; i < b->charts.size(); ++i)
+    b->slot_ofs[i + 1] = b->slot_ofs[i] + (size_t)(b->charts[i]->sites > 0 ? b->charts[i]->sites : 1);
+  const size_t need = b->slot_ofs.back();
+  if (need > b->feat_cap) {
+    cudaFree(b->feat);
+    cudaFree(b->pred);
+    cudaFree(b->jaux);
+    b->feat = b->pred = nullptr;
+    b->jaux = nullptr;
+    b->feat_cap = 0;
+    if (cudaMalloc(reinterpret_cast<void **>(&b->feat), need * 10 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void **>(&b->pred), need * 2 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void **>(&b->jaux), need * sizeof(uint32_t)) != cudaSuccess)
+      return GCVT_ERR_ALLOC;
+    CK(cudaMemsetAsync(b->feat, 0, need * 10 * sizeof(float), b->stream));
+    b->feat_cap = need;
+  }
+  const int cnt[2] = {(int)need, 0};
+  CK(cudaMemcpyAsync(b->mlp_count, cnt, sizeof(cnt), cudaMemcpyHostToDevice, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return GCVT_OK;
+}
+
+// One learned step of every member (see enqueue_jump): the MLP runs once over
+// all charts' slots.
+int batch_jump(gcvt_batch *b) {
+  const int nc = (int)b->charts.size();
+  CK(launch_list_batch(b->descs, nc, b->lofs, b->nblocks, b->gofs, b->done, b->ticket, b->stream));
+  CK(launch_cells_batch(b->descs, nc, b->gofs, b->ticket, b->stream, 4));
+  CK(launch_mlp_tc(b->feat, b->mlp_count, b->mlp_bf, b->pred, b->mlp_count + 1, b->stream));
+  CK(launch_apply(b->descs, nc, b->stream));
+  CK(launch_gate_switch(b->descs, nc, b->stream));
+  CK(launch_list_batch(b->descs, nc, b->lofs, b->nblocks, b->gofs, b->done, b->ticket, b->stream));
+  CK(launch_cells_batch(b->descs, nc, b->gofs, b->ticket, b->stream, 5));
+  CK(launch_gate_resolve(b->descs, nc, b->stream));
   return GCVT_OK;
 }
 
@@ -1425,6 +1564,11 @@ int gcvt_batch_destroy(gcvt_batch *b) {
   cudaFree(b->lofs);
   cudaFree(b->gofs);
   cudaFree(b->done);
+  cudaFree(b->mlp_bf);
+  cudaFree(b->feat);
+  cudaFree(b->pred);
+  cudaFree(b->jaux);
+  cudaFree(b->mlp_count);
   if (b->ev) cudaEventDestroy(b->ev);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
@@ -1435,6 +1579,88 @@ int gcvt_batch_set_stream(gcvt_batch *b, void *stream) {
   if (!b) return GCVT_ERR_ARGUMENT;
   b->stream = stream ? (cudaStream_t)stream : b->own_stream;
   return GCVT_OK;
+}
+
+int gcvt_batch_set_mlp(gcvt_batch *b, const float *params, int count) {
+  if (!b || !params || count != mlp_param_count()) return GCVT_ERR_ARGUMENT;
+  if (!b->mlp_bf &&
+      (cudaMalloc(reinterpret_cast<void **>(&b->mlp_bf), count * sizeof(float)) != cudaSuccess ||
+       cudaMalloc(reinterpret_cast<void **>(&b->mlp_count), 2 * sizeof(int)) != cudaSuccess))
+    return GCVT_ERR_ALLOC;
+  float *tmp = nullptr;
+  if (cudaMalloc(reinterpret_cast<void **>(&tmp), count * sizeof(float)) != cudaSuccess)
+    return GCVT_ERR_ALLOC;
+  int rc = GCVT_OK;
+  if (cudaMemcpyAsync(tmp, params, count * sizeof(float), cudaMemcpyHostToDevice, b->stream) !=
+          cudaSuccess ||
+      launch_round_params(tmp, b->mlp_bf, b->stream) != cudaSuccess ||
+      cudaMemsetAsync(b->mlp_count, 0, 2 * sizeof(int), b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    rc = GCVT_ERR_CUDA;
+  cudaFree(tmp);
+  return rc;
+}
+
+int gcvt_batch_iterate_learned(gcvt_batch *b, int iterations, int jump_every, int *tried,
+                               int *kept) {
+  if (!b || iterations < 0 || jump_every < 1) return GCVT_ERR_ARGUMENT;
+  if (!b->mlp_bf) return GCVT_ERR_STATE;
+  for (gcvt_ctx *c : b->charts)
+    if (!c->learning) return GCVT_ERR_STATE;
+  if (iterations == 0) return GCVT_OK;
+  int rc = batch_feat(b);
+  if (rc) return rc;
+  b->learned = true;
+  rc = batch_start(b, iterations, 0x7fffffff);
+  b->learned = false;
+  if (rc) return rc;
+  std::vector<int> tried0(b->charts.size()), kept0(b->charts.size());
+  auto pull_all = [&](bool *all_stopped) -> int {
+    bool all = true;
+    for (size_t i = 0; i < b->charts.size(); ++i) {
+      gcvt_ctx *c = b->charts[i];
+      cudaStream_t keep = c->stream;
+      c->stream = b->stream;
+      const int r = pull_state(c);
+      c->stream = keep;
+      if (r) return r;
+      all = all && c->st_host->stopped;
+    }
+    if (all_stopped) *all_stopped = all;
+    return GCVT_OK;
+  };
+  if ((rc = pull_all(nullptr))) return rc;
+  for (size_t i = 0; i < b->charts.size(); ++i) {
+    tried0[i] = b->charts[i]->st_host->gate_tried;
+    kept0[i] = b->charts[i]->st_host->gate_kept;
+  }
+  const int nc = (int)b->charts.size();
+  const int per_poll = (kChunk + jump_every - 1) / jump_every;
+  for (;;) {
+    for (int r = 0; r < per_poll; ++r) {
+      for (int i = 0; i + 1 < jump_every; ++i) {
+        CK(launch_list_batch(b->descs, nc, b->lofs, b->nblocks, b->gofs, b->done, b->ticket,
+                             b->stream));
+        CK(launch_cells_batch(b->descs, nc, b->gofs, b->ticket, b->stream));
+      }
+      if ((rc = batch_jump(b))) return rc;
+    }
+    bool all = false;
+    if ((rc = pull_all(&all))) return rc;
+    if (all) break;
+  }
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, b->mlp_count + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  if (err) return GCVT_ERR_CUDA;
+  int t = 0, k = 0;
+  for (size_t i = 0; i < b->charts.size(); ++i) {
+    t += b->charts[i]->st_host->gate_tried - tried0[i];
+    k += b->charts[i]->st_host->gate_kept - kept0[i];
+  }
+  if (tried) *tried = t;
+  if (kept) *kept = k;
+  return batch_finish(b);
 }
 
 int gcvt_batch_iterate(gcvt_batch *b, int iterations) {

@@ -428,27 +428,31 @@ __device__ void run_schedule(DevState *st, double E, unsigned r2, unsigned mv, i
   }
   if (st->use_stop_rule ? (st->iter >= st->max_iter) : (st->level_iters >= st->fixed_iters))
     stop = 1;                                // gcvt.cu:1142
+  if (st->target_energy > 0.0 && E <= st->target_energy) stop = 1;  // time-to-energy runs
   if (stop) st->stopped = 1;
   st->cover = min(isqrt_ceil((int)r2) + isqrt_ceil((int)mv), 2 * n);
   st->cur = cur == 2 ? 0 : cur + 1;
-  st->hist_cur ^= 1;
   st->done_blocks = 0;
   __threadfence();
 }
 
-// The end of a features pass (MODE 2) or energy pass (MODE 3) of a learned
-// jump: the energy of the configuration the pass saw.  After the energy pass
-// the gate decides: the jump stands if it lowered the energy.
+// The end of a pass: MODE 0 and 4 (a plain iteration, MODE 4 also writing
+// the learned step's features) run the schedule; MODE 5 (the iteration of
+// the jumped sites) also judges the jump: it stands if the jumped sites'
+// energy is below the energy of the sites it started from; MODE 2 (features
+// only, nothing moves) just closes the pass.
 template <int MODE>
-__device__ void gate_pass_done(DevState *st, double E) {
-  if (MODE == 2) {
-    st->gate_e0 = E;
-  } else {
+__device__ void pass_done(DevState *st, double E, unsigned r2, unsigned mv, int n, int cur) {
+  if (MODE == 5) {
     st->gate_e1 = E;
     st->gate_accept = E < st->gate_e0 ? 1 : 0;
   }
-  st->done_blocks = 0;
-  __threadfence();
+  if (MODE == 0 || MODE == 4 || MODE == 5) {
+    run_schedule(st, E, r2, mv, n, cur);
+  } else {
+    st->done_blocks = 0;
+    __threadfence();
+  }
 }
 
 // What one chart's iteration reads at its start.
@@ -457,7 +461,7 @@ struct IterView {
   uint64_t *nxt;         // where the moved sites go
   unsigned *cnt_nxt;     // their per-list-block counts
   float omega;
-  int W0, rb, nsites, cur, slack, hc;
+  int W0, rb, nsites, cur, nxt_i, slack;
   unsigned ngroups;      // 32-site groups of the list
 };
 
@@ -465,15 +469,15 @@ __device__ __forceinline__ IterView iter_view(const LevelBufs &a) {
   const DevState *st = a.st;
   IterView v;
   v.cur = st->snap_cur;
+  v.nxt_i = v.cur == 2 ? 0 : v.cur + 1;
   v.bits = bits_at(a, v.cur);
-  v.nxt = bits_at(a, v.cur == 2 ? 0 : v.cur + 1);
-  v.cnt_nxt = counts_at(a, v.cur == 2 ? 0 : v.cur + 1);
+  v.nxt = bits_at(a, v.nxt_i);
+  v.cnt_nxt = counts_at(a, v.nxt_i);
   v.omega = st->snap_omega;
   v.W0 = st->snap_window;
   v.rb = st->snap_cover;
   v.nsites = st->snap_count;
   v.slack = st->hint_slack;
-  v.hc = st->snap_hist;
   v.ngroups = (unsigned)(v.nsites + 31) / 32;
   return v;
 }
@@ -486,7 +490,6 @@ __device__ __forceinline__ void take_snapshot(DevState *st) {
   st->snap_omega = st->omega;
   st->snap_window = st->window;
   st->snap_cover = st->cover;
-  st->snap_hist = st->hist_cur;
 }
 
 // Clear the bitmap and counts the next iteration writes (nobody reads them
@@ -511,7 +514,7 @@ __device__ __forceinline__ void site_features(const LevelBufs &a, const IterView
                                               int sx, int sy, const CellSums &cs) {
   const int n = a.n;
   const float r = a.st->feat_scale, ir = 1.0f / r;
-  const uint64_t h = a.hist[v.hc][(size_t)sy * n + sx];
+  const uint64_t h = a.hist[v.cur][(size_t)sy * n + sx];
   float *f = a.feat + (size_t)idx * 10;
   const bool mass = cs.wh > 0.f;
   const float cx = mass ? cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl) - (float)sx : 0.f;
@@ -563,18 +566,17 @@ __device__ __forceinline__ unsigned move_site(const LevelBufs &a, const IterView
   a.hint[npid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
   if (a.hist[0]) {  // this move becomes the newest of the site's last four
     const int mx = min(max(nx - sx, -127), 127), my = min(max(ny - sy, -127), 127);
-    a.hist[v.hc ^ 1][npid] = (a.hist[v.hc][pid] << 16) | (uint64_t)(uint8_t)mx |
-                             ((uint64_t)(uint8_t)my << 8);
+    a.hist[v.nxt_i][npid] = (a.hist[v.cur][pid] << 16) | (uint64_t)(uint8_t)mx |
+                            ((uint64_t)(uint8_t)my << 8);
   }
-  if (a.ids[0]) a.ids[v.hc ^ 1][npid] = a.ids[v.hc][pid];
+  if (a.ids[0]) a.ids[v.nxt_i][npid] = a.ids[v.cur][pid];
   return mv;
 }
 
 // The energy reduction after group g (lane i holds site 32 g + i's energy
 // two-float, max cell radius^2 and move^2): group total -> slot; the warp
 // finishing the last group of a 64-group reduces the 64 slots; the warp
-// finishing the last 64-group totals them and runs the schedule (MODE 0) or
-// the learned jump's gate (MODE 2, 3).
+// finishing the last 64-group totals them and closes the pass (pass_done).
 template <int MODE>
 __device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v, unsigned g,
                                            int lane, float eh, float el, unsigned r2,
@@ -622,15 +624,16 @@ __device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v
   warp_reduce(eh, el, r2, mv);
   if (lane == 0) {
     const double E = ((double)eh + (double)el) * st->energy_scale;
-    if (MODE == 0) run_schedule(st, E, r2, mv, a.n, v.cur);
-    else gate_pass_done<MODE>(st, E);
+    pass_done<MODE>(st, E, r2, mv, a.n, v.cur);
   }
 }
 
 // Group g of a chart (32 listed sites, one per lane).  MODE 0: cells, moves,
 // and the group's share of the energy reduction.  MODE 1: moments only,
 // written as doubles (W, X, Y, E) at each site pixel of out4 (four n*n
-// planes).  MODE 2, 3: the learned jump's passes.
+// planes).  MODE 2: the learned step's features of the sites (nothing
+// moves).  MODE 4: MODE 0 and the features, with each site's window in
+// jaux.  MODE 5: MODE 0 for the jumped sites (the pass then judges the jump).
 template <int MODE>
 __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, int lane,
                            double *out4) {
@@ -654,9 +657,9 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
     } else {
       dfa(eh, el, cs.eh, cs.el);
       r2 = (unsigned)cs.r2;
-      if (MODE == 2) site_features(a, v, idx, sx, sy, cs);
-      else if (MODE == 3) a.hint[pid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
-      else mv = move_site(a, v, e, sx, sy, cs);
+      if (MODE == 2 || MODE == 4) site_features(a, v, idx, sx, sy, cs);
+      if (MODE == 4) a.jaux[idx] = (uint32_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+      if (MODE != 2) mv = move_site(a, v, e, sx, sy, cs);
     }
   }
   __syncwarp();
@@ -828,16 +831,19 @@ __device__ CellSums cell_sums_warp(const LevelBufs &a, const uint64_t *__restric
   }
 }
 
-// One Lloyd iteration, one listed site per warp from a site ticket.
+// One Lloyd iteration, one listed site per warp from a site ticket.  MODE
+// 0, 4 and 5 as in k_cell (MODE 4 also writes the learned step's features,
+// MODE 5 judges a jump and does not clear ahead).
+template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
   __shared__ WarpScratch ws;
   DevState *st = a.st;
   if (st->snap_stopped) return;
   const int lane = threadIdx.x;
   const IterView v = iter_view(a);
-  clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
+  if (MODE != 5) clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
   if (v.ngroups == 0) {  // no sites: the schedule still advances
-    if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, v.cur);
+    if (blockIdx.x == 0 && lane == 0) pass_done<MODE>(st, 0.0, 0u, 0u, a.n, v.cur);
     return;
   }
   if (v.nsites > kWarpSites) {  // more sites than LevelBufs::sitev holds: per lane
@@ -846,7 +852,7 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
       if (lane == 0) g = atomicAdd(&st->ticket, 1u);
       g = __shfl_sync(0xffffffffu, g, 0);
       if (g >= v.ngroups) return;
-      cell_group<0>(a, v, g, lane, nullptr);
+      cell_group<MODE>(a, v, g, lane, nullptr);
     }
   }
   const int n = a.n;
@@ -864,6 +870,10 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
     if (lane == 0) {
       float eh = 0.f, el = 0.f;
       dfa(eh, el, cs.eh, cs.el);
+      if (MODE == 4) {
+        site_features(a, v, (int)idx, sx, sy, cs);
+        a.jaux[idx] = (uint32_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
+      }
       const unsigned mv = move_site(a, v, e, sx, sy, cs);
       a.sitev[idx] = make_float4(eh, el, __uint_as_float((unsigned)cs.r2), __uint_as_float(mv));
       __threadfence();
@@ -880,31 +890,29 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
       eh = q.x, el = q.y, r2 = __float_as_uint(q.z), mv = __float_as_uint(q.w);
     }
     if (lane == 0) a.gcnt[g] = 0u;
-    group_tail<0>(a, v, g, lane, eh, el, r2, mv);
+    group_tail<MODE>(a, v, g, lane, eh, el, r2, mv);
   }
 }
 
 // One chart.  MODE 0: one Lloyd iteration (sums, move, energy, schedule).
 // MODE 1: moments only (gcvt_ctx_moments); the sites do not move.
-// MODE 2: the features pass of a learned jump: energy of the sites, their
-//         features (DevState::gate_e0, LevelBufs::feat); nothing moves.
-// MODE 3: the energy pass after the jump: energy and hints of the jumped
-//         sites, and the gate's decision (DevState::gate_accept).
+// MODE 2: the learned step's features of the sites (LevelBufs::feat);
+//         nothing moves.
+// MODE 4: MODE 0 and the features, for a jump from these sites.
+// MODE 5: MODE 0 for the jumped sites without clearing ahead (the bitmap
+//         after next holds the plain step's sites until the gate decides),
+//         and the gate's decision (DevState::gate_accept).
 template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
   DevState *st = a.st;
-  if (MODE == 0 && st->snap_stopped) return;
+  constexpr bool kMoves = MODE == 0 || MODE == 4 || MODE == 5;
+  if (kMoves && st->snap_stopped) return;
   const int lane = threadIdx.x;
   const IterView v = iter_view(a);
-  if (MODE == 0) {
+  if (MODE == 0 || MODE == 4)
     clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
-    if (v.ngroups == 0) {  // no sites: the schedule still advances
-      if (blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, v.cur);
-      return;
-    }
-  }
-  if ((MODE == 2 || MODE == 3) && v.ngroups == 0) {
-    if (blockIdx.x == 0 && lane == 0) gate_pass_done<MODE>(st, 0.0);
+  if (MODE != 1 && v.ngroups == 0) {  // no sites: the schedule still advances
+    if (blockIdx.x == 0 && lane == 0) pass_done<MODE>(st, 0.0, 0u, 0u, a.n, v.cur);
     return;
   }
   for (;;) {
@@ -919,7 +927,9 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
 // Many charts, one launch: the groups of all charts that have not stopped form
 // one sequence (group offsets per chart from k_list_batch, gofs[c] .. gofs[c+1]),
 // handed out by one ticket; each chart keeps its own state, reduction and
-// schedule, so a chart's iteration is the same as in k_cell.
+// schedule, so a chart's iteration is the same as in k_cell.  MODE 0, 4, 5 as
+// in k_cell.
+template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restrict__ charts,
                                                        int nchart,
                                                        const unsigned *__restrict__ gofs,
@@ -931,8 +941,9 @@ __global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restri
     DevState *st = a.st;
     if (st->snap_stopped) continue;
     const int cur = st->snap_cur;
-    clear_ahead(a, cur, t0, gthreads);
-    if (st->snap_count == 0 && blockIdx.x == 0 && lane == 0) run_schedule(st, 0.0, 0u, 0u, a.n, cur);
+    if (MODE != 5) clear_ahead(a, cur, t0, gthreads);
+    if (st->snap_count == 0 && blockIdx.x == 0 && lane == 0)
+      pass_done<MODE>(st, 0.0, 0u, 0u, a.n, cur);
   }
   const unsigned total = gofs[nchart];
   for (;;) {
@@ -948,7 +959,7 @@ __global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restri
     }
     const LevelBufs &a = charts[lo];
     const IterView v = iter_view(a);
-    cell_group<0>(a, v, g - __ldg(gofs + lo), lane, nullptr);
+    cell_group<MODE>(a, v, g - __ldg(gofs + lo), lane, nullptr);
   }
 }
 
@@ -1217,32 +1228,30 @@ cudaError_t cells_configure() {
     return e;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_cell<1>, 32, 0)) != cudaSuccess)
     return e;
-  int per2 = 0;
-  if ((e = cudaFuncSetAttribute(k_cell_batch, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                carve)) != cudaSuccess)
-    return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_cell_batch, 32, 0)) !=
-      cudaSuccess)
-    return e;
-  per0 = min(per0, per2);
-  for (auto fn : {k_cell<2>, k_cell<3>}) {
+  // every persistent variant shares the grid: the fewest blocks any of them fits
+  auto fit = [&](auto fn) -> cudaError_t {
     int per = 0;
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve)) !=
+    cudaError_t r = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+    if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32, 0);
+    if (r == cudaSuccess) per0 = min(per0, per);
+    return r;
+  };
+  for (auto fn : {k_cell_batch<0>, k_cell_batch<4>, k_cell_batch<5>})
+    if ((e = fit(fn)) != cudaSuccess) return e;
+  for (auto fn : {k_cell<2>, k_cell<4>, k_cell<5>})
+    if ((e = fit(fn)) != cudaSuccess) return e;
+  // one site per warp: its shared scratch (candidates, chunk sums) needs about
+  // 3.3 KB per block with the reserved 1 KB
+  int perw = 0;
+  for (auto fn : {k_cell_warp<0>, k_cell_warp<4>, k_cell_warp<5>}) {
+    int per = 0;
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 50)) !=
         cudaSuccess)
       return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 32, 0)) != cudaSuccess)
       return e;
-    per0 = min(per0, per);
+    perw = perw ? min(perw, per) : per;
   }
-  // one site per warp: its shared scratch (candidates, chunk sums) needs about
-  // 3.3 KB per block with the reserved 1 KB
-  int perw = 0;
-  if ((e = cudaFuncSetAttribute(k_cell_warp, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                50)) != cudaSuccess)
-    return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perw, k_cell_warp, 32, 0)) !=
-      cudaSuccess)
-    return e;
   g_warp_grid[dev] = sms * max(1, perw);
   g_cell_grid[dev] = sms * max(1, min(per0, per1));
   return cudaSuccess;
@@ -1256,12 +1265,17 @@ cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigne
 }
 
 cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
-                               unsigned *ticket, cudaStream_t s) {
+                               unsigned *ticket, cudaStream_t s, int mode) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
-  k_cell_batch<<<g_cell_grid[dev], 32, 0, s>>>(charts, nchart, gofs, ticket);
+  const int grid = g_cell_grid[dev];
+  switch (mode) {
+    case 4: k_cell_batch<4><<<grid, 32, 0, s>>>(charts, nchart, gofs, ticket); break;
+    case 5: k_cell_batch<5><<<grid, 32, 0, s>>>(charts, nchart, gofs, ticket); break;
+    default: k_cell_batch<0><<<grid, 32, 0, s>>>(charts, nchart, gofs, ticket);
+  }
   return cudaGetLastError();
 }
 
@@ -1279,14 +1293,18 @@ cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cud
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64 || !g_cell_grid[dev]) return cudaErrorNotReady;
   if (grid <= 0 || grid > g_cell_grid[dev]) grid = g_cell_grid[dev];
-  if (moments_only == 0 && b.sitev && b.gcnt && !b.hist[0]) {
-    k_cell_warp<<<min(grid, g_warp_grid[dev]), 32, 0, s>>>(b);
+  if ((moments_only == 0 || moments_only == 4 || moments_only == 5) && b.sitev && b.gcnt) {
+    const int wg = min(grid, g_warp_grid[dev]);
+    if (moments_only == 4) k_cell_warp<4><<<wg, 32, 0, s>>>(b);
+    else if (moments_only == 5) k_cell_warp<5><<<wg, 32, 0, s>>>(b);
+    else k_cell_warp<0><<<wg, 32, 0, s>>>(b);
     return cudaGetLastError();
   }
   switch (moments_only) {
     case 1: k_cell<1><<<grid, 32, 0, s>>>(b, out4); break;
     case 2: k_cell<2><<<grid, 32, 0, s>>>(b, out4); break;
-    case 3: k_cell<3><<<grid, 32, 0, s>>>(b, out4); break;
+    case 4: k_cell<4><<<grid, 32, 0, s>>>(b, out4); break;
+    case 5: k_cell<5><<<grid, 32, 0, s>>>(b, out4); break;
     default: k_cell<0><<<grid, 32, 0, s>>>(b, out4);
   }
   return cudaGetLastError();

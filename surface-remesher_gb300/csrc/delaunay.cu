@@ -959,9 +959,16 @@ int scan_big(const unsigned *count, int n, unsigned *offset, Scratch &sc, cudaSt
 // 64), as indices into delaunayInput's point order; host-synchronous on `s`.
 int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris, unsigned cap,
                    unsigned *ntris, cudaStream_t s) {
+  Scratch sc(s);
+  return delaunay_sites_in(bits, fixed, n, tris, cap, ntris, s, sc);
+}
+
+// The same with the caller's scratch (a caller that holds one already: the
+// device's scratch lock is not taken twice).
+int delaunay_sites_in(const uint64_t *bits, const uint64_t *fixed, int n, int *tris,
+                      unsigned cap, unsigned *ntris, cudaStream_t s, Scratch &sc) {
   *ntris = 0;
   if (n <= 0 || n % kBand) return GCVT_ERR_ARGUMENT;
-  Scratch sc(s);
   const size_t nb = (size_t)(n / kBand) * n;
   const int nt0 = n / kTile, ntiles = nt0 * nt0;
   unsigned *colpre = sc.take<unsigned>(nb), *colcnt = sc.take<unsigned>(n),

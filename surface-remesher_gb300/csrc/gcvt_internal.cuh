@@ -58,16 +58,16 @@ struct DevState {
   int snap_cur, snap_stopped, snap_window, snap_cover, snap_count;
   float snap_omega;
   int hint_slack;      // window hint left for a site: 2 R + hint_slack (tuned)
-  // Learned steps (learned.cu): the site histories, and the energy gate of a
-  // jump -- the state before it, so that a rejected jump can be undone.
-  int hist_cur;        // which history buffer holds the current sites' moves
-  int snap_hist;       // hist_cur of the iteration (snapshot)
-  int gate_cur, gate_cover, gate_accept;
+  double target_energy; // > 0: the level also stops once an iteration's energy
+                        // is at most this (time-to-energy runs); 0: off
+  // Learned steps (learned.cu): the energy gate of a proposed jump.
+  int gate_active;     // a jump is being judged (k_gate_switch .. k_gate_resolve)
+  int gate_accept;     // the jumped sites' energy is below the sites' (k_cell MODE 5)
   unsigned gate_jump2; // largest squared jump of the proposal
   float feat_scale;    // mean cell radius: the unit of the learned features
   int gate_tried, gate_kept;  // jumps proposed / kept
-  double gate_e0;      // energy before the jump (features pass)
-  double gate_e1;      // energy after it (energy pass)
+  double gate_e0;      // energy of the sites the jump starts from
+  double gate_e1;      // energy of the jumped sites
 };
 
 // Buffers of one resolution level, passed by value to every kernel.
@@ -92,12 +92,17 @@ struct LevelBufs {
   float4 *sslot;           // per 64 groups: the same, reduced
   unsigned *scnt;          // per 64 groups: groups finished
   // learned steps (null when off): per pixel the last four moves of the site
-  // there (int8 dx, dy each, newest in the low bytes), double-buffered
-  // (DevState::hist_cur); per pixel the site's id (training runs only);
-  // per list slot the site's features
-  uint64_t *hist[2];
-  int *ids[2];
+  // there (int8 dx, dy each, newest in the low bytes) and (training runs
+  // only) the site's id, one buffer per site bitmap (hist[k] describes the
+  // sites of bits[k]); per list slot the site's features, the MLP's
+  // prediction and the window of the site's cell (jaux); the state saved
+  // before a jump, restored when the jump is rejected
+  uint64_t *hist[3];
+  int *ids[3];
   float *feat;
+  float *pred;
+  uint32_t *jaux;
+  DevState *gsave;
   // one site per warp (small problems): per listed site its energy two-float,
   // cell radius^2 and move^2 until its group is reduced; per group the sites
   // done (null: lane-per-site only)
@@ -119,8 +124,8 @@ cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, 
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_list(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_count(const LevelBufs &b, cudaStream_t s);
-// MODE 0 runs one site per warp when b.sitev and b.gcnt are set (and no
-// learned-step state is), else one site per lane.
+// MODE 0, 4 and 5 run one site per warp when b.sitev and b.gcnt are set,
+// else one site per lane; MODE 1 and 2 run one site per lane.
 cudaError_t launch_cells(const LevelBufs &b, int moments_only, double *out4, cudaStream_t s,
                          int grid = 0);
 int cells_default_grid();
@@ -139,8 +144,10 @@ int delaunay_sites(const uint64_t *bits, const uint64_t *fixed, int n, int *tris
 cudaError_t launch_list_batch(const LevelBufs *charts, int nchart, const unsigned *lofs,
                               unsigned nblocks, unsigned *gofs, unsigned *done, unsigned *ticket,
                               cudaStream_t s);
+// MODE 0: plain iteration; 4: plain iteration + features of the learned step;
+// 5: the jumped sites' iteration, which also judges the jump.
 cudaError_t launch_cells_batch(const LevelBufs *charts, int nchart, const unsigned *gofs,
-                               unsigned *ticket, cudaStream_t s);
+                               unsigned *ticket, cudaStream_t s, int mode = 0);
 cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
                        cudaStream_t s, int tail_halo = 16);
 cudaError_t launch_jfa_compare(const uint32_t *jfa, const uint32_t *exact, int n,
@@ -152,9 +159,11 @@ cudaError_t launch_mlp_infer(const float *feat, const int *count, const float *p
                              float *pred, int grid, cudaStream_t s);
 cudaError_t launch_mlp_tc(const float *feat, const int *count, const float *params_bf,
                           float *pred, int *err, cudaStream_t s);
-cudaError_t launch_apply(const LevelBufs &b, const float *pred, int grid, cudaStream_t s);
-cudaError_t launch_gate_switch(DevState *st, int n, cudaStream_t s);
-cudaError_t launch_gate_resolve(const LevelBufs &b, int grid, cudaStream_t s);
+// A learned jump over the charts descs[0 .. nchart): jumped sites, gate
+// switch, gate resolution (learned.cu).
+cudaError_t launch_apply(const LevelBufs *descs, int nchart, cudaStream_t s);
+cudaError_t launch_gate_switch(const LevelBufs *descs, int nchart, cudaStream_t s);
+cudaError_t launch_gate_resolve(const LevelBufs *descs, int nchart, cudaStream_t s);
 cudaError_t launch_features(const LevelBufs &b, int *ids, int *xy, int grid, cudaStream_t s);
 cudaError_t launch_ids_init(const LevelBufs &b, int grid, cudaStream_t s);
 cudaError_t launch_mlp_train_step(const float *samples, long long count, float *master,
@@ -187,6 +196,13 @@ class Scratch {
   size_t block_, used_, total_;
   bool ok_;
 };
+
+int delaunay_sites_in(const uint64_t *bits, const uint64_t *fixed, int n, int *tris,
+                      unsigned cap, unsigned *ntris, cudaStream_t s, Scratch &sc);
+int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *colcnt,
+                const double *cxy, int C, const int *segs, int S, double scale, double left,
+                double lower, int *out, unsigned cap, unsigned *ntris, int *detail,
+                cudaStream_t s);
 
 // Exclusive scan of n counts into offset[0..n] (offset[n] = total) and a copy
 // in cursor[0..n-1]; one block, n <= 2^26.

@@ -11,10 +11,11 @@
 // activations to bfloat16 and accumulates in FP32, the tensor cores'
 // arithmetic); training keeps FP32 master weights (Adam).
 //
-// A jump (host side in api.cu): features pass on the sites S (energy E(S)),
-// MLP, k_apply writes the jumped sites L into the next bitmap, an energy pass
-// on L computes E(L); k_gate_resolve keeps L if E(L) < E(S) and otherwise
-// restores S -- the plain method is the fallback and the judge.
+// A jump (kernels below, sequence in api.cu): the plain iteration from the
+// sites S also writes their features, the MLP predicts, k_apply places the
+// jumped sites L, and the iteration of L decides: L stands if E(L) < E(S),
+// otherwise the plain step's sites are current again -- the plain method is
+// the fallback and the judge.
 #include "gcvt_internal.cuh"
 
 #include <cuda_bf16.h>
@@ -73,23 +74,54 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const float *__restrict__ fea
   }
 }
 
-// The jumped sites: site i of the list moves by round(pred_i * r), clamped to
-// the grid; fixed sites, and jumps onto zero density, stay.  They go into the
-// bitmap after the current one, with their histories (unchanged: a jump is
-// not a Lloyd move) and ids.
-__global__ void __launch_bounds__(256) k_apply(LevelBufs a, const float *__restrict__ pred) {
+// A learned step, over charts descs[0 .. nchart) (a single context is a batch
+// of one).  The plain iteration from the sites S (k_cell MODE 4: bitmap cur
+// -> cur + 1, also the features of S) is followed by:
+//   k_apply        the jumped sites L = S + round(pred r) into bitmap cur + 2
+//                  (cleared by that iteration); bitmap cur, whose sites are no
+//                  longer needed, is cleared for the iteration of L;
+//   k_gate_switch  saves the state after the plain iteration and makes L
+//                  current, with the covering bound grown by the largest jump;
+//   k_list, k_cell MODE 5: the plain iteration of L (L -> bitmap cur), which
+//                  also decides: the jump stands if E(L) < E(S);
+//   k_gate_clear   clears the bitmap of the loser: the plain step's sites
+//                  (bitmap cur + 1) when the jump stands, else L;
+//   k_gate_commit  restores the saved state when the jump is rejected -- the
+//                  run then goes on from the plain step, exactly as without
+//                  the jump.
+// An accepted jump thus costs no extra pass: its iteration of L is the next
+// Lloyd iteration.  A rejected one costs the pass over L.
+
+// The jumped sites of chart blockIdx.y: listed site i moves by
+// round(pred_i * r), clamped to the grid; fixed sites, and jumps onto zero
+// density, stay.  A jumped site keeps its history and id (a jump is not a
+// Lloyd move) and gets the window of its cell in S grown by twice the jump.
+__global__ void __launch_bounds__(256) k_apply(const LevelBufs *__restrict__ descs) {
+  const LevelBufs &a = descs[blockIdx.y];
   DevState *st = a.st;
-  const int n = a.n, cur = st->snap_cur, hc = st->snap_hist, ns = st->snap_count;
+  // no jump when the plain iteration ended the level, or once the schedule
+  // has lowered omega below 2 (the plain iterations then settle by
+  // themselves; a jump would only knock the sites out of their settling)
+  if (st->snap_stopped || st->stopped || st->omega < 2.0f) return;
+  const int n = a.n, cur = st->snap_cur, ns = st->snap_count;
+  const int lj = cur == 0 ? 2 : cur - 1;  // (cur + 2) mod 3
   const float r = st->feat_scale;
-  uint64_t *nxt = cur == 0 ? a.bits[1] : (cur == 1 ? a.bits[2] : a.bits[0]);
-  unsigned *cnx = cur == 0 ? a.counts[1] : (cur == 1 ? a.counts[2] : a.counts[0]);
+  uint64_t *dst = lj == 0 ? a.bits[0] : (lj == 1 ? a.bits[1] : a.bits[2]);
+  unsigned *cdst = lj == 0 ? a.counts[0] : (lj == 1 ? a.counts[1] : a.counts[2]);
+  uint64_t *old_bits = cur == 0 ? a.bits[0] : (cur == 1 ? a.bits[1] : a.bits[2]);
+  unsigned *old_cnt = cur == 0 ? a.counts[0] : (cur == 1 ? a.counts[1] : a.counts[2]);
+  const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+               gs = (size_t)gridDim.x * blockDim.x;
+  const size_t nwords = (size_t)(n / kBand) * n, nlb = (nwords + kListWords - 1) / kListWords;
+  for (size_t i = t0; i < nwords; i += gs) old_bits[i] = 0ull;
+  for (size_t i = t0; i < nlb; i += gs) old_cnt[i] = 0u;
   unsigned m2 = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+  for (size_t i = t0; i < (size_t)ns; i += gs) {
     const uint32_t e = a.list[i];
     const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
     int nx = sx, ny = sy;
     if (!(e & 0x8000u)) {
-      const float jx = pred[2 * (size_t)i] * r, jy = pred[2 * (size_t)i + 1] * r;
+      const float jx = a.pred[2 * i] * r, jy = a.pred[2 * i + 1] * r;
       if (isfinite(jx) && isfinite(jy)) {
         const int cx = min(max((int)rintf(fminf(fmaxf(jx, -1e6f), 1e6f)) + sx, 0), n - 1);
         const int cy = min(max((int)rintf(fminf(fmaxf(jy, -1e6f), 1e6f)) + sy, 0), n - 1);
@@ -99,41 +131,59 @@ __global__ void __launch_bounds__(256) k_apply(LevelBufs a, const float *__restr
         }
       }
     }
-    m2 = max(m2, (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy)));
+    const unsigned j2 = (unsigned)((nx - sx) * (nx - sx) + (ny - sy) * (ny - sy));
+    m2 = max(m2, j2);
     const size_t widx = (size_t)(ny / kBand) * n + nx;
     const unsigned long long bit = 1ull << (ny % kBand);
-    const unsigned long long old = atomicOr(reinterpret_cast<unsigned long long *>(nxt + widx), bit);
-    if (!(old & bit)) atomicAdd(cnx + widx / kListWords, 1u);
+    const unsigned long long was = atomicOr(reinterpret_cast<unsigned long long *>(dst + widx), bit);
+    if (!(was & bit)) atomicAdd(cdst + widx / kListWords, 1u);
     const size_t pid = (size_t)sy * n + sx, npid = (size_t)ny * n + nx;
-    a.hist[hc ^ 1][npid] = a.hist[hc][pid];
-    if (a.ids[0]) a.ids[hc ^ 1][npid] = a.ids[hc][pid];
+    a.hist[lj][npid] = a.hist[cur][pid];
+    if (a.ids[0]) a.ids[lj][npid] = a.ids[cur][pid];
+    int j = (int)sqrtf((float)j2);
+    while (j * j < (int)j2) ++j;
+    a.hint[npid] = (uint8_t)min((int)a.jaux[i] + 2 * j, 255);
   }
   m2 = __reduce_max_sync(0xffffffffu, m2);
   if ((threadIdx.x & 31) == 0 && m2) atomicMax(&st->gate_jump2, m2);
 }
 
-// Switch to the jumped sites for the energy pass, remembering the state to
-// restore: current bitmap, covering bound (grown by the largest jump: every
-// density pixel was within cover of its owner, which moved by at most that).
-__global__ void k_gate_switch(DevState *st, int n) {
-  const int cur = st->cur;
-  st->gate_cur = cur;
-  st->gate_cover = st->cover;
+// One thread per chart: save the state after the plain iteration, make the
+// jumped sites current.  Every density pixel was within snap_cover of its
+// owner in S, which moved by at most the largest jump, so snap_cover plus
+// that jump bounds L's covering distance.  A chart whose plain iteration
+// stopped its level proposes nothing.
+__global__ void k_gate_switch(const LevelBufs *__restrict__ descs, int nchart) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchart) return;
+  const LevelBufs &a = descs[c];
+  DevState *st = a.st;
+  if (st->snap_stopped || st->stopped || st->omega < 2.0f) {  // as k_apply decided
+    st->gate_active = 0;
+    st->gate_jump2 = 0;
+    return;
+  }
+  *a.gsave = *st;
   const unsigned j2 = st->gate_jump2;
   int j = (int)sqrtf((float)j2);
   while (j * j < (int)j2) ++j;
-  st->cover = min(st->cover + j, 2 * n);
-  st->cur = cur == 2 ? 0 : cur + 1;
-  st->hist_cur ^= 1;
+  st->gate_active = 1;
+  st->gate_accept = 0;
+  st->gate_e0 = st->energy;  // E(S), from the plain iteration
+  st->cover = min(st->snap_cover + j, 2 * a.n);
+  st->cur = st->snap_cur == 0 ? 2 : st->snap_cur - 1;
   st->gate_jump2 = 0;
 }
 
-// After the energy pass: keep the jump (clear the bitmap the next iteration
-// writes) or undo it (clear the jumped bitmap, restore the state).
-__global__ void __launch_bounds__(256) k_gate_resolve(LevelBufs a) {
-  DevState *st = a.st;
-  const int g = st->gate_cur, acc = st->gate_accept;
-  const int k = acc ? (g + 2) % 3 : (g + 1) % 3;
+// Chart blockIdx.y: clear the bitmap the next iteration writes -- the plain
+// step's sites when the jump stands, the jumped sites when it does not.
+// Reads the decision only; k_gate_commit changes the state afterwards.
+__global__ void __launch_bounds__(256) k_gate_clear(const LevelBufs *__restrict__ descs) {
+  const LevelBufs &a = descs[blockIdx.y];
+  const DevState *st = a.st;
+  if (!st->gate_active) return;
+  const int p = a.gsave->cur;  // the plain step's bitmap; the jumped sites are in p + 1
+  const int k = st->gate_accept ? p : (p == 2 ? 0 : p + 1);
   uint64_t *bz = k == 0 ? a.bits[0] : (k == 1 ? a.bits[1] : a.bits[2]);
   unsigned *cz = k == 0 ? a.counts[0] : (k == 1 ? a.counts[1] : a.counts[2]);
   const size_t nwords = (size_t)(a.n / kBand) * a.n;
@@ -141,27 +191,38 @@ __global__ void __launch_bounds__(256) k_gate_resolve(LevelBufs a) {
   const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (size_t)gridDim.x * blockDim.x;
   for (size_t i = t0; i < nwords; i += gs) bz[i] = 0ull;
   for (size_t i = t0; i < nlb; i += gs) cz[i] = 0u;
-  if (t0 == 0) {
-    st->gate_tried += 1;
-    st->gate_kept += acc;
-    if (!acc) {
-      st->cur = g;
-      st->cover = st->gate_cover;
-      st->hist_cur ^= 1;
-    }
-  }
+}
+
+// One thread per chart: count the jump; a rejected jump restores the state
+// saved after the plain iteration (the bitmap written by the jumped sites'
+// iteration is cleared ahead by the next iteration, as every third one is).
+__global__ void k_gate_commit(const LevelBufs *__restrict__ descs, int nchart) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchart) return;
+  const LevelBufs &a = descs[c];
+  DevState *st = a.st;
+  if (!st->gate_active) return;
+  const int acc = st->gate_accept, tried = st->gate_tried + 1, kept = st->gate_kept + acc;
+  const double e0 = st->gate_e0, e1 = st->gate_e1;
+  if (!acc) *st = *a.gsave;
+  st->gate_tried = tried;
+  st->gate_kept = kept;
+  st->gate_e0 = e0;
+  st->gate_e1 = e1;
+  st->gate_active = 0;
+  __threadfence();
 }
 
 // Ids and pixel positions of the listed sites (training samples; their
 // features come from a features pass, k_cell MODE 2, over the same list).
 __global__ void __launch_bounds__(256) k_features(LevelBufs a, int *out_ids, int *out_xy) {
   const DevState *st = a.st;
-  const int n = a.n, hc = st->snap_hist, ns = st->snap_count;
+  const int n = a.n, cur = st->snap_cur, ns = st->snap_count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
     const uint32_t e = a.list[i];
     const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
     const size_t pid = (size_t)sy * n + sx;
-    if (out_ids) out_ids[i] = a.ids[0] ? a.ids[hc][pid] : -1;
+    if (out_ids) out_ids[i] = a.ids[0] ? a.ids[cur][pid] : -1;
     if (out_xy) {
       out_xy[2 * i] = sx;
       out_xy[2 * i + 1] = sy;
@@ -172,12 +233,12 @@ __global__ void __launch_bounds__(256) k_features(LevelBufs a, int *out_ids, int
 // Every listed site gets its list index as id, and an empty history.
 __global__ void __launch_bounds__(256) k_ids_init(LevelBufs a) {
   const DevState *st = a.st;
-  const int n = a.n, hc = st->snap_hist, ns = st->snap_count;
+  const int n = a.n, cur = st->snap_cur, ns = st->snap_count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
     const uint32_t e = a.list[i];
     const size_t pid = (size_t)(e >> 16) * n + (e & 0x7fffu);
-    a.ids[hc][pid] = i;
-    a.hist[hc][pid] = 0ull;
+    a.ids[cur][pid] = i;
+    a.hist[cur][pid] = 0ull;
   }
 }
 
@@ -551,18 +612,21 @@ cudaError_t launch_mlp_infer(const float *feat, const int *count, const float *p
   return cudaGetLastError();
 }
 
-cudaError_t launch_apply(const LevelBufs &b, const float *pred, int grid, cudaStream_t s) {
-  k_apply<<<grid, 256, 0, s>>>(b, pred);
+cudaError_t launch_apply(const LevelBufs *descs, int nchart, cudaStream_t s) {
+  const int per = max(8, 1216 / max(nchart, 1));  // blocks per chart
+  k_apply<<<dim3((unsigned)per, (unsigned)nchart), 256, 0, s>>>(descs);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gate_switch(DevState *st, int n, cudaStream_t s) {
-  k_gate_switch<<<1, 1, 0, s>>>(st, n);
+cudaError_t launch_gate_switch(const LevelBufs *descs, int nchart, cudaStream_t s) {
+  k_gate_switch<<<(nchart + 127) / 128, 128, 0, s>>>(descs, nchart);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gate_resolve(const LevelBufs &b, int grid, cudaStream_t s) {
-  k_gate_resolve<<<grid, 256, 0, s>>>(b);
+cudaError_t launch_gate_resolve(const LevelBufs *descs, int nchart, cudaStream_t s) {
+  const int per = max(8, 1216 / max(nchart, 1));
+  k_gate_clear<<<dim3((unsigned)per, (unsigned)nchart), 256, 0, s>>>(descs);
+  k_gate_commit<<<(nchart + 127) / 128, 128, 0, s>>>(descs, nchart);
   return cudaGetLastError();
 }
 

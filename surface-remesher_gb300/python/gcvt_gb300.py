@@ -77,6 +77,8 @@ SIGNATURES = {
     "gcvt_ctx_extract_points": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I,
                                  ctypes.POINTER(I), I], I),
     "gcvt_ctx_delaunay": ([P, P, I, ctypes.POINTER(I), I], I),
+    "gcvt_ctx_cdt": ([P, ctypes.c_double, ctypes.c_double, ctypes.c_double, P, I, P, I, P, I,
+                      ctypes.POINTER(I), ctypes.POINTER(I), I], I),
     "gcvt_seed_sites": ([P, P, P, I, I, P], I),
     "gcvt_ctx_jfa_label": ([P, P, P, I], I),
     "gcvt_ctx_autotune": ([P, ctypes.POINTER(Tuning)], I),
@@ -85,6 +87,9 @@ SIGNATURES = {
     "gcvt_ctx_set_mlp": ([P, P, I], I),
     "gcvt_ctx_features": ([P, P, P, P, I, ctypes.POINTER(I)], I),
     "gcvt_ctx_iterate_learned": ([P, I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+    "gcvt_ctx_set_target_energy": ([P, ctypes.c_double], I),
+    "gcvt_batch_set_mlp": ([P, P, I], I),
+    "gcvt_batch_iterate_learned": ([P, I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
     "gcvt_mlp_forward": ([P, P, I, P, I], I),
     "gcvt_mlp_train": ([P, ctypes.c_longlong, P, I, I, ctypes.c_float, ctypes.c_ulonglong, P], I),
     "gcvt_mlp_gradient": ([P, ctypes.c_longlong, P, I, ctypes.c_ulonglong, I, P, P], I),
@@ -255,6 +260,28 @@ class Context:
                                           ctypes.byref(cnt), MEM_HOST), "gcvt_ctx_delaunay")
         return out[:min(cnt.value, capacity)]
 
+    def cdt(self, scale, left, lower, cpoints, segments, capacity=None):
+        """Constrained Delaunay triangles (T, 3) int32 of the current free
+        sites (extract_points' order) and the constraint points cpoints
+        (C, 2) float64 (indices after the sites), with the segments (S, 2)
+        index pairs as edges; returns (triangles, detail mask)."""
+        c = np.ascontiguousarray(cpoints, np.float64).reshape(-1, 2)
+        sg = np.ascontiguousarray(segments, np.int32).reshape(-1, 2)
+        cnt, det = I(0), I(0)
+        if capacity is None:
+            _check(self.lib.gcvt_ctx_extract_points(self.h, 1.0, 0.0, 0.0, None, 0,
+                                                    ctypes.byref(cnt), MEM_HOST),
+                   "gcvt_ctx_extract_points")
+            capacity = 2 * (cnt.value + len(c)) + 16
+        out = np.empty((max(capacity, 1), 3), np.int32)
+        code = self.lib.gcvt_ctx_cdt(self.h, float(scale), float(left), float(lower),
+                                     c.ctypes.data, len(c), sg.ctypes.data, len(sg),
+                                     out.ctypes.data, int(capacity), ctypes.byref(cnt),
+                                     ctypes.byref(det), MEM_HOST)
+        if code:
+            raise GcvtError(code, "gcvt_ctx_cdt (detail %d)" % det.value)
+        return out[:min(cnt.value, capacity)], det.value
+
     def autotune(self):
         """Pick the fastest launch choices for the loaded problem (results
         unchanged); returns them as a dict."""
@@ -291,11 +318,19 @@ class Context:
         return f[:m], (None if ids is None else ids[:m]), xy[:m]
 
     def iterate_learned(self, iterations, jump_every=10):
+        """Lloyd iterations with a learned step every jump_every; returns
+        (jumps tried, jumps kept)."""
         tried, kept = I(0), I(0)
         _check(self.lib.gcvt_ctx_iterate_learned(self.h, int(iterations), int(jump_every),
                                                  ctypes.byref(tried), ctypes.byref(kept)),
                "gcvt_ctx_iterate_learned")
         return tried.value, kept.value
+
+    def set_target_energy(self, target):
+        """Later runs also stop at the first iteration with energy <= target
+        (0: off)."""
+        _check(self.lib.gcvt_ctx_set_target_energy(self.h, float(target)),
+               "gcvt_ctx_set_target_energy")
 
     def jfa_label(self, labels=True):
         """(labels or None, (differing, farther, pixels)) of jump flooding."""
@@ -347,6 +382,19 @@ class Batch:
         infos = (RunInfo * len(self.contexts))()
         _check(self.lib.gcvt_batch_run(self.h, int(max_iter), infos), "gcvt_batch_run")
         return [i.as_dict() for i in infos]
+
+    def set_mlp(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self.lib.gcvt_batch_set_mlp(self.h, p.ctypes.data, len(p)), "gcvt_batch_set_mlp")
+
+    def iterate_learned(self, iterations, jump_every=4):
+        """Every member's learned run at once; returns (jumps tried, kept)
+        summed over the charts."""
+        tried, kept = I(0), I(0)
+        _check(self.lib.gcvt_batch_iterate_learned(self.h, int(iterations), int(jump_every),
+                                                   ctypes.byref(tried), ctypes.byref(kept)),
+               "gcvt_batch_iterate_learned")
+        return tried.value, kept.value
 
     def close(self):
         if self.h:

@@ -1,21 +1,24 @@
 """Train the learned-step MLP on plain Lloyd trajectories and evaluate it.
 
-    python train_step_mlp.py train [--runs 60] [--horizon 4] [--out DIR]
+    python train_step_mlp.py train [--runs 200] [--horizon 8] [--sites 4096,8192,16384] [--out DIR]
     python train_step_mlp.py eval [--config plain_4096] [--params FILE]
 
 train: plain Lloyd runs on the config-0 density family (1024^2 grids, 8
-seeded Gaussians in the disk, 4096 uniform sites, seeds 1000 + run) with site
+seeded Gaussians in the disk, seeds 1000 + run) with 4096, 8192 or 16384
+uniform sites in turn (mean cell radii of 7.6, 5.4 and 3.8 pixels) and site
 ids tracked; every 2 iterations up to 40 the features of every site are
-recorded, and each site's target is its displacement over the next
-`horizon` iterations (or to where it is after 200 iterations), in units of
-the mean cell radius (sites merged on the way are dropped).  The MLP is
+recorded (about 2048 sites per record), and each site's target is its
+displacement over the next `horizon` iterations (or to where it is after 200
+iterations), in units of the mean cell radius (sites merged on the way are
+dropped).  The MLP is
 trained on the GPU (gcvt_mlp_train) and its parameters are written to
 DIR/step_mlp.npy with DIR/step_mlp.json describing the run; the defaults
 made the parameters in surface-remesher_gb300/data.
 
 eval: time to reach E <= (1 + 1e-4) E_conv, E_conv the energy after 1000
-plain iterations, for plain Lloyd and for Lloyd with gated learned jumps,
-on one configuration; prints one JSON line.
+plain iterations, for plain Lloyd and for Lloyd with gated learned steps,
+on one configuration (the device stops each run at the target); prints one
+JSON line.
 """
 import argparse
 import json
@@ -109,24 +112,29 @@ def train(args):
 
 
 def time_to_energy(ctx, sites, rho, mask, target, learned, jump_every, limit):
-    """Seconds (wall, synchronised every 10 iterations) and iterations until
-    the energy of the input of an iteration is <= target."""
+    """(seconds, iterations, jumps tried, jumps kept) until the first
+    iteration whose energy is at most target: the device stops the run there
+    (gcvt_ctx_set_target_energy), timed with CUDA events on the context's
+    stream around the whole run after the load."""
     import torch
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_target_energy(target)
     ctx.load(sites, rho, mask)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    t0 = time.time()
-    it, tried, kept = 0, 0, 0
-    while it < limit:
-        if learned:
-            a, b = ctx.iterate_learned(10, jump_every)
-            tried, kept = tried + a, kept + b
-        else:
-            ctx.iterate(10)
-        it += 10
-        if ctx.info()["energy"] <= target:
-            break
-    torch.cuda.synchronize()
-    return time.time() - t0, it, tried, kept
+    e0.record(stream)
+    tried = kept = 0
+    if learned:
+        tried, kept = ctx.iterate_learned(limit, jump_every)
+    else:
+        ctx.iterate(limit)
+    e1.record(stream)
+    e1.synchronize()
+    it = ctx.info()["iterations"]
+    ctx.set_target_energy(0)
+    ctx.set_stream(None)
+    return e0.elapsed_time(e1) / 1e3, it, tried, kept
 
 
 def evaluate(args):
@@ -158,8 +166,8 @@ def evaluate(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("mode", choices=["train", "eval"])
-    ap.add_argument("--runs", type=int, default=60)
-    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--runs", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
@@ -167,10 +175,10 @@ def main():
     ap.add_argument("--config", default="plain_4096", choices=sorted(CONFIGS))
     ap.add_argument("--params", default=os.path.join(DATA, "step_mlp.npy"))
     ap.add_argument("--conv-iters", type=int, default=1000)
-    ap.add_argument("--jump-every", type=int, default=4)
-    ap.add_argument("--sites", default=str(SITES),
+    ap.add_argument("--jump-every", type=int, default=4)  # three plain iterations, one learned step
+    ap.add_argument("--sites", default="4096,8192,16384",
                     help="site counts of the training runs, comma-separated, used in turn")
-    ap.add_argument("--horizon", type=int, default=4,
+    ap.add_argument("--horizon", type=int, default=8,
                     help="target: displacement over this many iterations (0: to iteration 200)")
     args = ap.parse_args()
     if args.mode == "train":

@@ -61,11 +61,12 @@ def gaussian_density(n, k, a_max, s_lo, s_hi, seed, radius=0.48):
     mu = np.stack([0.5 + rr * np.cos(th), 0.5 + rr * np.sin(th)], 1)
     s = rng.uniform(s_lo, s_hi, k)
     c = (np.arange(n, dtype=np.float64) + 0.5) / n
-    rho = np.ones((n, n), np.float64)
-    for j in range(k):
-        gx = np.exp(-((c - mu[j, 0]) ** 2) / (2 * s[j] ** 2))
-        gy = np.exp(-((c - mu[j, 1]) ** 2) / (2 * s[j] ** 2))
-        rho += a[j] * np.outer(gy, gx)
+    # each Gaussian is separable: the sum over k is one (n x k) (k x n)
+    # product in float64 (the float32 grid equals the term-by-term sum's on
+    # the benchmark configurations; checked at 1024^2, 4096^2 and 8192^2)
+    gx = np.exp(-((c[:, None] - mu[None, :, 0]) ** 2) / (2 * s ** 2))
+    gy = np.exp(-((c[:, None] - mu[None, :, 1]) ** 2) / (2 * s ** 2))
+    rho = 1.0 + (gy * a) @ gx.T
     rho[~disk_mask(n, radius)] = 0.0
     return rho.astype(np.float32)
 
@@ -176,6 +177,24 @@ def raster_inputs(P, n):
     scale = (u - b) / (n - 1) if (u - b) > (r - l) else (r - l) / (n - 1)
     Q = np.ascontiguousarray(np.stack([P[:, 0] - l, P[:, 1] - b], 1))
     return Q, scale, l, b
+
+
+def mesh_constraints(uv, tris, scale, left, lower):
+    """The CDT constraints of a disk mesh, as the reference's pipeline takes
+    them: its boundary vertices are the constraint points and its boundary
+    edges the constraint segments (detect_constrains, main.cpp:211-214), and
+    each constraint point's pixel becomes a fixed site (generateMask,
+    gcvt.h:141-158: x = int((p.x - left) / scale)).  Returns (bv: the
+    boundary vertex ids, be: the boundary edges as vertex id pairs, px, py:
+    the fixed pixels)."""
+    e = np.concatenate([tris[:, [0, 1]], tris[:, [1, 2]], tris[:, [2, 0]]]).astype(np.int64)
+    key = np.sort(e, 1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    be = e[cnt[inv.ravel()] == 1]
+    bv = np.unique(be)
+    px = ((uv[bv, 0] - left) / scale).astype(np.int64)
+    py = ((uv[bv, 1] - lower) / scale).astype(np.int64)
+    return bv, be, px, py
 
 
 def small_case(n, m, seed, k=6, a_max=4.0):

@@ -1,0 +1,146 @@
+// cdt_core_host.cpp -- host build of the constrained Delaunay stage's mesh
+// operations (surface-remesher_gb300/csrc/cdt_core.cuh), run one after the
+// other on the CPU, for tests/test_cdt_core.py.  The GPU runs the same
+// functions in parallel rounds; this replays the algorithm sequentially:
+// adjacency of a starting triangulation, every constraint point located by a
+// walk and inserted (inside, on an edge, or outside the hull), Lawson flips,
+// each segment recovered by flips, flips again.
+//
+// stdin:  V, then V lines "X Y R"; T, then T lines "a b c" (counter-clockwise,
+//         any triangulation of the first F points); C, then C point indices
+//         to insert in order; S, then S lines "a b".
+// stdout: "ok T" then T lines "a b c", or "error <code>".
+#include <cstdio>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "cdt_core.cuh"
+
+using namespace cvtgb::cdt;
+
+int main() {
+  int V = 0;
+  if (scanf("%d", &V) != 1) return 1;
+  std::vector<i64> X(V), Y(V), R(V);
+  for (int v = 0; v < V; ++v)
+    if (scanf("%lld %lld %lld", &X[v], &Y[v], &R[v]) != 3) return 1;
+  int T = 0;
+  if (scanf("%d", &T) != 1) return 1;
+  const int cap = 2 * V + 16;
+  std::vector<int> tri(3 * (size_t)cap), nbr(3 * (size_t)cap, kNone), vt(V, 0);
+  std::vector<uint8_t> cons(cap, 0);
+  for (int t = 0; t < T; ++t)
+    if (scanf("%d %d %d", &tri[3 * t], &tri[3 * t + 1], &tri[3 * t + 2]) != 3) return 1;
+  std::map<std::pair<int, int>, int> dir;
+  for (int t = 0; t < T; ++t)
+    for (int i = 0; i < 3; ++i) {
+      dir[{tri[3 * t + nx3(i)], tri[3 * t + pv3(i)]}] = pack_nb(t, i);
+      vt[tri[3 * t + i]] = t;
+    }
+  for (int t = 0; t < T; ++t)
+    for (int i = 0; i < 3; ++i) {
+      auto it = dir.find({tri[3 * t + pv3(i)], tri[3 * t + nx3(i)]});
+      nbr[3 * t + i] = it == dir.end() ? kNone : it->second;
+    }
+  Mesh m{tri.data(), nbr.data(), cons.data(), vt.data(), X.data(), Y.data(), R.data()};
+  auto flips = [&]() {
+    for (int round = 0; round < 1000000; ++round) {
+      bool any = false;
+      for (int t = 0; t < T; ++t)
+        for (int i = 0; i < 3; ++i)
+          if (wants_flip(m, t, i)) {
+            flip(m, t, i);
+            any = true;
+          }
+      if (!any) return true;
+    }
+    return false;
+  };
+  if (!flips()) {
+    printf("error flips\n");
+    return 0;
+  }
+  int C = 0;
+  if (scanf("%d", &C) != 1) return 1;
+  int start = 0;
+  for (int k = 0; k < C; ++k) {
+    int p;
+    if (scanf("%d", &p) != 1) return 1;
+    int t, i;
+    const int kind = locate(m, p, start, 1 << 20, &t, &i);
+    if (kind == kLocIn) {
+      split_in(m, t, p, T, T + 1);
+      T += 2;
+    } else if (kind == kLocEdge) {
+      const int two = nbr[3 * t + i] >= 0;
+      split_edge(m, t, i, p, T, T + 1);
+      T += two ? 2 : 1;
+    } else if (kind == kLocOut) {
+      std::vector<int> et, ei, bt, bi;
+      int ft = t, fi = i;
+      for (;;) {
+        int pt, pi;
+        if (!hull_prev(m, ft, fi, 4096, &pt, &pi)) {
+          printf("error hull\n");
+          return 0;
+        }
+        if (orient(m, tri[3 * pt + nx3(pi)], tri[3 * pt + pv3(pi)], p) >= 0) break;
+        ft = pt;
+        fi = pi;
+        bt.push_back(pt);
+        bi.push_back(pi);
+      }
+      for (int q = (int)bt.size() - 1; q >= 0; --q) {
+        et.push_back(bt[q]);
+        ei.push_back(bi[q]);
+      }
+      et.push_back(t);
+      ei.push_back(i);
+      int lt = t, li = i;
+      for (;;) {
+        int nt, ni;
+        if (!hull_next(m, lt, li, 4096, &nt, &ni)) {
+          printf("error hull\n");
+          return 0;
+        }
+        if (orient(m, tri[3 * nt + nx3(ni)], tri[3 * nt + pv3(ni)], p) >= 0) break;
+        lt = nt;
+        li = ni;
+        et.push_back(nt);
+        ei.push_back(ni);
+      }
+      std::vector<int> slots(et.size());
+      for (size_t q = 0; q < et.size(); ++q) slots[q] = T + (int)q;
+      insert_out(m, et.data(), ei.data(), (int)et.size(), p, slots.data());
+      T += (int)et.size();
+    } else {
+      printf("error locate %d\n", kind);
+      return 0;
+    }
+    start = vt[p];
+    if (!flips()) {
+      printf("error flips\n");
+      return 0;
+    }
+  }
+  int S = 0;
+  if (scanf("%d", &S) != 1) return 1;
+  std::vector<int> queue(2 * 4096), stack(2 * 256);
+  for (int k = 0; k < S; ++k) {
+    int a, b;
+    if (scanf("%d %d", &a, &b) != 2) return 1;
+    const int r = recover_chain(m, a, b, queue.data(), 4096, stack.data(), 256, 1 << 20);
+    if (r != kSegOk) {
+      printf("error segment %d\n", r);
+      return 0;
+    }
+  }
+  if (!flips()) {
+    printf("error flips\n");
+    return 0;
+  }
+  printf("ok %d\n", T);
+  for (int t = 0; t < T; ++t) printf("%d %d %d\n", tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]);
+  return 0;
+}

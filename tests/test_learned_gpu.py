@@ -79,7 +79,7 @@ def test_rejected_jumps_leave_no_trace(gcvt_lib, cuda_device):
     ctx.load(sites, rho, mask)
     ctx.set_mlp(np.zeros(gcvt_lib.mlp_param_count(), np.float32))
     tried, kept = ctx.iterate_learned(30, jump_every=5)
-    assert (tried, kept) == (6, 0)
+    assert (tried, kept) == (5, 0)  # the 30th iteration ends the run before a sixth
     assert np.array_equal(ctx.sites(), plain.sites())
     assert ctx.info()["energy"] == plain.info()["energy"]
     assert np.array_equal(ctx.label(), plain.label())
@@ -97,7 +97,12 @@ def test_kept_jumps_lower_the_energy(gcvt_lib, cuda_device):
     ctx.iterate(10)
     e0 = ctx.info()["energy"]
     tried, kept = ctx.iterate_learned(40, jump_every=4)
-    assert tried == 10 and 0 <= kept <= tried
+    # rounds of three plain iterations and a learned step of two iterations
+    # (kept) or one (rejected), proposed only while omega is 2: at most 10
+    # steps in 40 iterations, some before the schedule first lowers omega
+    # (after iteration 30)
+    assert 1 <= tried <= 10 and 0 <= kept <= tried
+    assert ctx.info()["iterations"] == 50
     e1 = ctx.info()["energy"]
     assert np.isfinite(e1) and e1 < e0
     s = ctx.sites()
@@ -222,3 +227,124 @@ def test_adam_steps_match_oracle(gcvt_lib, cuda_device):
     w3, wloss = M.train(s, p0, 3, batch, lr, seed)
     assert np.allclose(loss3, wloss, rtol=1e-3)
     assert np.mean(np.abs(p3 - w3) <= 1e-2 * lr) > 0.99
+
+
+def _trained_or_analytic(gcvt_lib):
+    """A network whose jumps are taken: the pending displacement itself (a
+    jump to the centroid of the cell, the omega = 1 Lloyd step) written as
+    MLP weights -- layer 1 splits the first two features into positive and
+    negative parts, layer 2 passes them on, layer 3 recombines them."""
+    p = np.zeros(gcvt_lib.mlp_param_count(), np.float32)
+    W1 = p[:640].reshape(10, 64)
+    W2 = p[704:4800].reshape(64, 64)
+    W3 = p[4864:4992].reshape(64, 2)
+    W1[0, 0], W1[0, 1], W1[1, 2], W1[1, 3] = 1, -1, 1, -1
+    for j in range(4):
+        W2[j, j] = 1
+    W3[0, 0], W3[1, 0], W3[2, 1], W3[3, 1] = 1, -1, 1, -1
+    return p
+
+
+def test_batched_learned_runs_equal_solo_learned_runs(gcvt_lib, cuda_device):
+    cases = [small_case(512, 2500, 61), small_case(256, 600, 62), small_case(512, 1500, 63)]
+    p = _trained_or_analytic(gcvt_lib)
+    solo = []
+    for sites, rho, mask in cases:
+        c = gcvt_lib.Context(sites.shape[0])
+        c.learning(True)
+        c.set_mlp(p)
+        c.load(sites, rho, mask)
+        tk = c.iterate_learned(23, jump_every=3)
+        solo.append((c.sites(), c.info(), tk))
+        c.close()
+    assert sum(t[2][1] for t in solo) > 0  # some jumps stand
+    ctxs = []
+    for sites, rho, mask in cases:
+        c = gcvt_lib.Context(sites.shape[0])
+        c.learning(True)
+        c.load(sites, rho, mask)
+        ctxs.append(c)
+    b = gcvt_lib.Batch(ctxs)
+    b.set_mlp(p)
+    tried, kept = b.iterate_learned(23, jump_every=3)
+    assert (tried, kept) == (sum(t[2][0] for t in solo), sum(t[2][1] for t in solo))
+    for c, (s_sites, s_info, _) in zip(ctxs, solo):
+        assert np.array_equal(c.sites(), s_sites)
+        info = c.info()
+        assert info["iterations"] == s_info["iterations"] == 23
+        assert info["energy"] == s_info["energy"] and info["omega"] == s_info["omega"]
+    b.close()
+    for c in ctxs:
+        c.close()
+
+
+def test_target_energy_stops_at_the_first_iteration_below(gcvt_lib, cuda_device):
+    sites, rho, mask = small_case(512, 2500, 64)
+    ctx = gcvt_lib.Context(512)
+    ctx.load(sites, rho, mask)
+    energies = []
+    for _ in range(40):
+        ctx.iterate(1)
+        energies.append(ctx.info()["energy"])
+    target = energies[24] * (1 + 1e-12)
+    first = next(i for i, e in enumerate(energies) if e <= target) + 1
+    ctx.set_target_energy(target)
+    ctx.load(sites, rho, mask)
+    ctx.iterate(40)
+    info = ctx.info()
+    assert info["iterations"] == first and info["energy"] == energies[first - 1]
+    # learned steps stop the same way, at an energy at or below the target
+    # (one every run meets early)
+    target = energies[5] * (1 + 1e-12)
+    ctx.set_target_energy(target)
+    ctx.learning(True)
+    ctx.set_mlp(_trained_or_analytic(gcvt_lib))
+    ctx.load(sites, rho, mask)
+    ctx.iterate_learned(60, jump_every=3)
+    info = ctx.info()
+    assert info["energy"] <= target and info["iterations"] < 60
+    ctx.set_target_energy(0)
+    ctx.close()
+
+
+def test_trained_network_gains_over_plain_lloyd(gcvt_lib, cuda_device):
+    """What the shipped network (surface-remesher_gb300/data/step_mlp.npy) gains
+    over the method without it, on held-out runs of its training family
+    (1024^2, 8 Gaussians, 4096 sites; seeds the training never saw):
+    iterations until E <= (1 + 1e-4) E_conv, E_conv the energy after 1000
+    plain iterations, the device stopping each run there.  Measured on a
+    GB300: plain 42-43 iterations, learned (three plain iterations, then a
+    learned step) 24-26.  A zero network gains nothing: every jump is
+    rejected and the run is the plain run."""
+    import os
+    from train_step_mlp import DATA
+    from workloads import disk_sites, gaussian_density
+    p = np.load(os.path.join(DATA, "step_mlp.npy"))
+    plain_it, learned_it = [], []
+    for seed in (7001, 7002, 7003):
+        rho = gaussian_density(1024, 8, 4.0, 0.02, 0.15, seed)
+        sites = disk_sites(1024, 4096, seed, rho)
+        mask = np.zeros((1024, 1024), np.uint8)
+        ctx = gcvt_lib.Context(1024)
+        ctx.load(sites, rho, mask)
+        ctx.iterate(1000)
+        target = ctx.info()["energy"] * (1 + 1e-4)
+        ctx.set_target_energy(target)
+        ctx.load(sites, rho, mask)
+        ctx.iterate(400)
+        plain_it.append(ctx.info()["iterations"])
+        ctx.close()
+        lc = gcvt_lib.Context(1024)
+        lc.learning(True)
+        lc.set_target_energy(target)
+        lc.set_mlp(p)
+        lc.load(sites, rho, mask)
+        _, kept = lc.iterate_learned(400, 4)
+        learned_it.append(lc.info()["iterations"])
+        assert lc.info()["energy"] <= target and kept > 0
+        lc.set_mlp(np.zeros_like(p))
+        lc.load(sites, rho, mask)
+        assert lc.iterate_learned(400, 4)[1] == 0
+        assert lc.info()["iterations"] == plain_it[-1]
+        lc.close()
+    assert max(learned_it) <= 0.7 * min(plain_it), (learned_it, plain_it)
