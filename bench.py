@@ -188,15 +188,18 @@ def batched_time_to_energy(G, ctxs, inputs, targets, params, jump_every, limit):
     return e0.elapsed_time(e1) / 1e3, its, tried, kept
 
 
-def time_to_energy_8192(G):
-    """The learned+batched headline on the largest configuration: 8192^2, 64
-    Gaussians, 1,048,576 sites (seeded as the other workloads)."""
+def time_to_energy_config(G, workload):
+    """time_to_energy_line on another plain workload: plain_8192 (8192^2, 64
+    Gaussians, 1,048,576 sites: the learned+batched headline configuration)
+    or plain_1024 (1024^2, 8 Gaussians, 4096 sites: the learned step's
+    training family, held-out seed)."""
     from workloads import config_inputs
-    sites, rho, mask, _ = config_inputs("plain_8192", seed=SEED)
-    ctx = G.Context(8192)
-    line = time_to_energy_line(G, ctx, 8192, sites, rho, mask)
+    sites, rho, mask, _ = config_inputs(workload, seed=SEED)
+    n = sites.shape[0]
+    ctx = G.Context(n)
+    line = time_to_energy_line(G, ctx, n, sites, rho, mask)
     ctx.close()
-    line["workload"] = "plain_8192 (8192^2, 64 Gaussians, 1,048,576 sites)"
+    line["workload"] = workload
     return line
 
 
@@ -459,8 +462,11 @@ def run_ours(args):
         # time to E <= (1 + 1e-4) E_conv: plain, learned, learned + batched
         tte = time_to_energy_line(G, ctx, n, sites, rho, mask)
         ctx.set_stream(stream.cuda_stream)  # the timing runs used a stream of their own
-        tte_8192 = (time_to_energy_8192(G) if rank == 0 and not args.no_headline
+        headline = rank == 0 and not args.no_headline
+        tte_8192 = (time_to_energy_config(G, "plain_8192") if headline
                     and workload != "plain_8192" else None)
+        tte_1024 = (time_to_energy_config(G, "plain_1024") if headline
+                    and workload != "plain_1024" else None)
         # the Delaunay triangulation of the converged sites (outside the timing)
         _, delaunay = delaunay_stage(ctx, G.load_library(), len(ctx.extract_points()), args)
         # a labelling pass (final output) and a jump-flooding labelling,
@@ -493,6 +499,7 @@ def run_ours(args):
         "tuning": tuning,
         "time_to_energy": tte,
         "time_to_energy_8192": tte_8192,
+        "time_to_energy_1024": tte_1024,
         "delaunay": delaunay,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(workload),
@@ -702,13 +709,20 @@ def run_batched(args):
 def run_mesh(args):
     """Mesh-driven density (256 x 256-vertex jittered disk mesh with a height
     field, per-vertex area-ratio weights): rasterised to 2048^2 on the GPU,
-    65,536 sites drawn over it, 100 Lloyd iterations + labels per step."""
+    65,536 sites drawn over it and the mesh's boundary vertices as fixed
+    sites (the constraint points), 100 Lloyd iterations + labels per step;
+    then the constrained Delaunay triangulation and the lift."""
     import torch
     import gcvt_gb300 as G
-    from workloads import disk_sites, mesh_inputs
+    from workloads import disk_sites, disk_surface, mesh_constraints, mesh_inputs, raster_inputs
     torch.cuda.set_device(0)
     n, m, iters = 2048, 65536, 100
-    (pts, w, tris, scale), mask = mesh_inputs(256, n, seed=2)
+    (pts, w, tris, scale), _ = mesh_inputs(256, n, seed=2)
+    uv, _, _ = disk_surface(256, seed=2)
+    _, _, left, lower = raster_inputs(uv, n)
+    bv, be, fx, fy = mesh_constraints(uv, tris, scale, left, lower)
+    mask = np.zeros((n, n), np.uint8)
+    mask[fy, fx] = 1  # generateMask (gcvt.h:141-158)
     lib = G.load_library()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     rho = G.rasterize(pts, w, tris, scale, n)  # warm-up
@@ -728,6 +742,8 @@ def run_mesh(args):
         raster_ms.append(ev[0].elapsed_time(ev[1]))
     rho = d_rho.cpu().numpy()
     sites = disk_sites(n, m, 3, rho)
+    sites[fy, fx, 0] = fx  # putConstrains (gcvt.h:106-122): the fixed sites
+    sites[fy, fx, 1] = fy
     stream = torch.cuda.Stream()
     ctx = G.Context(n)
     ctx.set_stream(stream.cuda_stream)
@@ -754,7 +770,7 @@ def run_mesh(args):
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
     t = statistics.mean(ms)
-    lift = lift_stage(ctx, n, args)
+    lift = lift_stage(ctx, n, args, constraints=(bv, be))
     ref = None
     if args.reference_gpu:  # the reference's rasteriser and gCVT kernels on this mesh
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -779,7 +795,8 @@ def run_mesh(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 raster, f32+int16 Lloyd",
         "data": "synthetic (seeded jittered disk mesh, height field, area-ratio weights)",
         "config": {"workload": "mesh_2048", "n": n, "triangles": int(len(tris)),
-                   "vertices": int(len(w)), "sites": m, "iterations": iters},
+                   "vertices": int(len(w)), "sites": m, "fixed_sites": int(mask.sum()),
+                   "constraint_segments": int(len(be)), "iterations": iters},
         "raster_ms": statistics.median(raster_ms),
         "lift": lift,
         "reference_gpu": ref,
@@ -821,13 +838,43 @@ def delaunay_stage(ctx, lib, npts, args):
     return d_tri[:cnt.value], res
 
 
-def lift_stage(ctx, n, args):
+def cdt_stage(ctx, lib, scale, left, lower, cpts, segs, args):
+    """The constrained Delaunay triangulation of the final free sites and the
+    constraint points with the constraint segments (gcvt_ctx_cdt, device
+    output; host-synchronous, so timed on the host clock)."""
+    import ctypes
+    import torch
+    import gcvt_gb300 as G
+    F = len(ctx.extract_points())
+    cap = 2 * (F + len(cpts)) + 16
+    d_tri = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+    d_c = torch.from_numpy(np.ascontiguousarray(cpts, np.float64)).cuda()
+    d_s = torch.from_numpy(np.ascontiguousarray(segs, np.int32)).cuda()
+    cnt, det = ctypes.c_int(0), ctypes.c_int(0)
+    times = []
+    for r in range(max(3, args.warmup) + max(3, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G._check(lib.gcvt_ctx_cdt(ctx.h, float(scale), float(left), float(lower), d_c.data_ptr(),
+                                  len(cpts), d_s.data_ptr(), len(segs), d_tri.data_ptr(), cap,
+                                  ctypes.byref(cnt), ctypes.byref(det), G.MEM_DEVICE),
+                 "gcvt_ctx_cdt")
+        if r >= max(3, args.warmup):
+            times.append((time.perf_counter() - t0) * 1e3)
+    return d_tri[:cnt.value], {"triangles": int(cnt.value), "ms": statistics.median(times),
+                               "free_sites": F, "constraint_points": int(len(cpts)),
+                               "segments": int(len(segs))}
+
+
+def lift_stage(ctx, n, args, constraints=None):
     """The stages after the Lloyd loop: the final sites, extracted as CDT
-    input points (delaunay.h:46-57), triangulated on the GPU
-    (gcvt_ctx_delaunay), lifted onto the surface and the triangles filtered
-    (recover.h:98-157) by gcvt_lift, device buffers, CUDA events.  Beside it,
-    the oracle's single-thread restatement of recover() -- the reference's
-    O(queries x faces) scan -- timed on 400 queries and scaled to all."""
+    input points (delaunay.h:46-57), triangulated on the GPU -- with the
+    constraint points and segments (bv, be: boundary vertices and edges of
+    the mesh) by gcvt_ctx_cdt, else gcvt_ctx_delaunay -- lifted onto the
+    surface and the triangles filtered (recover.h:98-157) by gcvt_lift,
+    device buffers, CUDA events.  Beside it, the oracle's single-thread
+    restatement of recover() -- the reference's O(queries x faces) scan --
+    timed on 400 queries and scaled to all."""
     import torch
     import gcvt_gb300 as G
     from workloads import disk_surface, raster_inputs
@@ -835,16 +882,28 @@ def lift_stage(ctx, n, args):
     _, scale, left, lower = raster_inputs(uv, n)
     pts = ctx.extract_points(scale, left, lower)
     lib = G.load_library()
-    d_cdt, dstage = delaunay_stage(ctx, lib, len(pts), args)
+    fixed = np.zeros(0, np.int32)
+    if constraints is not None:
+        bv, be = constraints
+        F = len(pts)
+        pos = {int(v): k for k, v in enumerate(bv)}
+        segs = np.array([(F + pos[int(a)], F + pos[int(b)]) for a, b in be], np.int32)
+        d_cdt, dstage = cdt_stage(ctx, lib, scale, left, lower, uv[bv], segs, args)
+        pts = np.concatenate([pts, uv[bv]])
+        fixed = np.ascontiguousarray(bv, np.int32)
+    else:
+        d_cdt, dstage = delaunay_stage(ctx, lib, len(pts), args)
     cdt = d_cdt.cpu().numpy()
     d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (uv, xyz, tris, pts)] + [d_cdt]
+    d_fix = torch.from_numpy(fixed).cuda() if len(fixed) else None
     out = torch.empty((len(pts), 3), dtype=torch.float64, device="cuda")
     face = torch.empty(len(pts), dtype=torch.int32, device="cuda")
     keep = torch.empty(len(cdt), dtype=torch.uint8, device="cuda")
 
     def call():
         G._check(lib.gcvt_lift(d[0].data_ptr(), d[1].data_ptr(), len(uv), d[2].data_ptr(),
-                               len(tris), d[3].data_ptr(), len(pts), 0, None, d[4].data_ptr(),
+                               len(tris), d[3].data_ptr(), len(pts), len(fixed),
+                               None if d_fix is None else d_fix.data_ptr(), d[4].data_ptr(),
                                len(cdt), out.data_ptr(), face.data_ptr(), keep.data_ptr(),
                                G.MEM_DEVICE), "gcvt_lift")
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -859,7 +918,8 @@ def lift_stage(ctx, n, args):
             times.append(ev[0].elapsed_time(ev[1]))
     res = {"points": int(len(pts)), "faces": int(len(tris)), "cdt_triangles": int(len(cdt)),
            "kept": int(keep.sum().item()), "located": int((face >= 0).sum().item()),
-           "lift_ms": statistics.median(times), "delaunay": dstage}
+           "lift_ms": statistics.median(times),
+           ("cdt" if constraints is not None else "delaunay"): dstage}
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as orc

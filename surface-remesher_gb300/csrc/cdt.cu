@@ -380,44 +380,25 @@ __global__ void k_segments(Mesh m, const int *__restrict__ segs, int S, int V, i
 
 // ---- output ----------------------------------------------------------------
 
-// Triangle t rotated to start at its smallest vertex: that vertex owns it.
-__device__ __forceinline__ void canon(const int *v, int &a, int &b, int &c) {
-  if (v[0] < v[1] && v[0] < v[2]) { a = v[0]; b = v[1]; c = v[2]; }
-  else if (v[1] < v[2]) { a = v[1]; b = v[2]; c = v[0]; }
-  else { a = v[2]; b = v[0]; c = v[1]; }
-}
-
 __global__ void k_emit_count(Mesh m, int T, int *cnt) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int a, b, c;
-  canon(m.tri + 3 * t, a, b, c);
+  cdt::canon(m.tri + 3 * t, a, b, c);
   atomicAdd(cnt + a, 1);
 }
 
-// Rank of triangle t among its owner's triangles by their second vertex
-// (the owner's triangles lie around it: rotate both ways).
+// Triangle t at its owner's offset plus its rank among the owner's
+// triangles (cdt_core.cuh owner_rank).
 __global__ void k_emit(Mesh m, int T, const int *__restrict__ off, int *out, int cap, int *err) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int a, b, c;
-  canon(m.tri + 3 * t, a, b, c);
-  int rank = 0;
-  for (int dir = 0; dir < 2; ++dir) {
-    int ct = t, s = 0;
-    for (; s < kRotate; ++s) {
-      const int *v = m.tri + 3 * ct;
-      const int k = v[0] == a ? 0 : (v[1] == a ? 1 : 2);
-      const int nb = m.nbr[3 * ct + (dir == 0 ? cdt::nx3(k) : cdt::pv3(k))];
-      if (nb < 0) break;
-      ct = cdt::nb_tri(nb);
-      if (ct == t) break;
-      int x, y, z;
-      canon(m.tri + 3 * ct, x, y, z);
-      if (x == a && y < b) ++rank;
-    }
-    if (s == kRotate) atomicOr(err, kErrWalk);
-    if (ct == t) break;  // a full turn: every triangle around a seen
+  cdt::canon(m.tri + 3 * t, a, b, c);
+  const int rank = cdt::owner_rank(m, t, kRotate);
+  if (rank < 0) {
+    atomicOr(err, kErrWalk);
+    return;
   }
   const int pos = off[a] + rank;
   if (pos < cap) {

@@ -485,6 +485,47 @@ CDT_HD int recover_segment(const Mesh &m, int a, int b, int *queue, int qcap, in
   return mark_constraint(m, a, b, max_steps) ? kSegOk : kSegBroken;
 }
 
+// Triangle t rotated to start at its smallest vertex (its owner).
+CDT_HD void canon(const int *v, int &a, int &b, int &c) {
+  if (v[0] < v[1] && v[0] < v[2]) {
+    a = v[0]; b = v[1]; c = v[2];
+  } else if (v[1] < v[2]) {
+    a = v[1]; b = v[2]; c = v[0];
+  } else {
+    a = v[2]; b = v[0]; c = v[1];
+  }
+}
+
+// The rank of triangle t among the triangles its owner a owns, by their
+// second vertex (they all lie around a: rotate both ways from t); -1 if a
+// rotation runs past max_steps.
+CDT_HD int owner_rank(const Mesh &m, int t, int max_steps) {
+  int a, b, c;
+  canon(m.tri + 3 * t, a, b, c);
+  int rank = 0;
+  for (int dir = 0; dir < 2; ++dir) {
+    int ct = t, s = 0;
+    bool full = false;
+    for (; s < max_steps; ++s) {
+      const int *v = m.tri + 3 * ct;
+      const int k = v[0] == a ? 0 : (v[1] == a ? 1 : 2);
+      const int nb = m.nbr[3 * ct + (dir == 0 ? nx3(k) : pv3(k))];
+      if (nb < 0) break;
+      ct = nb_tri(nb);
+      if (ct == t) {
+        full = true;
+        break;
+      }
+      int x, y, z;
+      canon(m.tri + 3 * ct, x, y, z);
+      if (x == a && y < b) ++rank;
+    }
+    if (s == max_steps) return -1;
+    if (full) break;  // every triangle around a seen in one direction
+  }
+  return rank;
+}
+
 // The segment (a, b) made a chain of constraint edges: recovered whole, or,
 // where vertices lie inside it, piece by piece between them (stack: scratch
 // of scap pairs).

@@ -439,11 +439,12 @@ __device__ void run_schedule(DevState *st, double E, unsigned r2, unsigned mv, i
 // The end of a pass: MODE 0 and 4 (a plain iteration, MODE 4 also writing
 // the learned step's features) run the schedule; MODE 5 (the iteration of
 // the jumped sites) also judges the jump: it stands if the jumped sites'
-// energy is below the energy of the sites it started from; MODE 2 (features
-// only, nothing moves) just closes the pass.
+// energy is below the energy of the sites it started from (when no jump was
+// proposed, MODE 5 is a plain iteration); MODE 2 (features only, nothing
+// moves) just closes the pass.
 template <int MODE>
 __device__ void pass_done(DevState *st, double E, unsigned r2, unsigned mv, int n, int cur) {
-  if (MODE == 5) {
+  if (MODE == 5 && st->gate_active) {
     st->gate_e1 = E;
     st->gate_accept = E < st->gate_e0 ? 1 : 0;
   }
@@ -841,7 +842,8 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
   if (st->snap_stopped) return;
   const int lane = threadIdx.x;
   const IterView v = iter_view(a);
-  if (MODE != 5) clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
+  if (MODE != 5 || !st->gate_active)
+    clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
   if (v.ngroups == 0) {  // no sites: the schedule still advances
     if (blockIdx.x == 0 && lane == 0) pass_done<MODE>(st, 0.0, 0u, 0u, a.n, v.cur);
     return;
@@ -901,7 +903,8 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
 // MODE 4: MODE 0 and the features, for a jump from these sites.
 // MODE 5: MODE 0 for the jumped sites without clearing ahead (the bitmap
 //         after next holds the plain step's sites until the gate decides),
-//         and the gate's decision (DevState::gate_accept).
+//         and the gate's decision (DevState::gate_accept); when no jump was
+//         proposed (DevState::gate_active 0), exactly MODE 0.
 template <int MODE>
 __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
   DevState *st = a.st;
@@ -909,7 +912,9 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
   if (kMoves && st->snap_stopped) return;
   const int lane = threadIdx.x;
   const IterView v = iter_view(a);
-  if (MODE == 0 || MODE == 4)
+  // MODE 5 keeps the bitmap after next (the plain step's sites) while a jump
+  // is judged; without a jump it is a plain iteration
+  if (MODE == 0 || MODE == 4 || (MODE == 5 && !st->gate_active))
     clear_ahead(a, v.cur, (size_t)blockIdx.x * 32 + lane, (size_t)gridDim.x * 32);
   if (MODE != 1 && v.ngroups == 0) {  // no sites: the schedule still advances
     if (blockIdx.x == 0 && lane == 0) pass_done<MODE>(st, 0.0, 0u, 0u, a.n, v.cur);
@@ -941,7 +946,7 @@ __global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restri
     DevState *st = a.st;
     if (st->snap_stopped) continue;
     const int cur = st->snap_cur;
-    if (MODE != 5) clear_ahead(a, cur, t0, gthreads);
+    if (MODE != 5 || !st->gate_active) clear_ahead(a, cur, t0, gthreads);
     if (st->snap_count == 0 && blockIdx.x == 0 && lane == 0)
       pass_done<MODE>(st, 0.0, 0u, 0u, a.n, cur);
   }

@@ -140,7 +140,28 @@ int main() {
     printf("error flips\n");
     return 0;
   }
+  // the GPU's output order: by owner (smallest vertex), then second vertex
+  std::vector<int> cnt(V + 1, 0), off(V + 1, 0), out(3 * (size_t)T, -1);
+  for (int t = 0; t < T; ++t) {
+    int a, b, c;
+    canon(&tri[3 * t], a, b, c);
+    ++cnt[a];
+  }
+  for (int v = 0; v < V; ++v) off[v + 1] = off[v] + cnt[v];
+  for (int t = 0; t < T; ++t) {
+    int a, b, c;
+    canon(&tri[3 * t], a, b, c);
+    const int r = owner_rank(m, t, 4096);
+    const int pos = off[a] + r;
+    if (r < 0 || pos >= T || out[3 * pos] != -1) {
+      printf("error emit\n");
+      return 0;
+    }
+    out[3 * pos] = a;
+    out[3 * pos + 1] = b;
+    out[3 * pos + 2] = c;
+  }
   printf("ok %d\n", T);
-  for (int t = 0; t < T; ++t) printf("%d %d %d\n", tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]);
+  for (int t = 0; t < T; ++t) printf("%d %d %d\n", out[3 * t], out[3 * t + 1], out[3 * t + 2]);
   return 0;
 }
