@@ -8,12 +8,17 @@
 //   1. the sites' Delaunay triangulation (delaunay.cu, exact on the lattice);
 //   2. adjacency from a hash of directed edges;
 //   3. the constraint points inserted in rounds: every point locates itself
-//      by a walk, claims the triangles its split changes (atomicMin of its
-//      index), and the points that won all their claims split (1 -> 3 inside
+//      by a walk, claims the triangles its split changes (atomicMin of a
+//      priority, a fixed bijective hash of its index: claims by plain index
+//      let only the first of a run of neighbours win each round), and the points that won all their claims split (1 -> 3 inside
 //      a triangle, 2 -> 4 on an edge, a fan over the visible hull edges
 //      outside the hull); after each round, Delaunay flip rounds;
 //   4. each segment made an edge by flipping the edges that cross it
-//      (Sloan's method, cdt_core.cuh recover_segment) and marked;
+//      (Sloan's method, cdt_core.cuh recover_segment) and marked: segments
+//      already edges at once, the others in rounds where each claims the
+//      triangles around the vertices of its crossing edges and the winners
+//      are recovered side by side, the rare long ones (or ones with a vertex
+//      inside) by one thread;
 //   5. flip rounds that restore the Delaunay property on every edge that is
 //      not a constraint: the result is the constrained Delaunay
 //      triangulation;
@@ -53,9 +58,14 @@ constexpr int kWalk = 1 << 20;    // steps of one point location
 constexpr int kRotate = 4096;     // triangles around one vertex
 constexpr int kChain = 64;        // visible hull edges from one outside point
 constexpr int kFlipRounds = 1 << 16;
+constexpr int kFlipPoll = 4;      // flip rounds between read-backs
 constexpr int kInsertRounds = 1 << 12;
 constexpr int kSegQueue = 4096;   // crossing edges of one segment
 constexpr int kSegStack = 256;    // pieces of one segment split by vertices inside it
+constexpr int kCorr = 8;          // crossing edges of a segment recovered in the parallel rounds
+constexpr int kClaim = 128;       // triangles one such segment claims
+constexpr int kSegWindow = 1 << 15;  // segments per window of parallel rounds
+constexpr int kSegRounds = 1 << 12;
 
 enum CdtErr {
   kErrCoord = 1,       // a constraint point beyond the supported coordinate range
@@ -168,21 +178,23 @@ struct Loc {
   int et[kChain], ei[kChain];
 };
 
-__device__ __forceinline__ void claim(int *cl, int t, int id) { atomicMin(cl + t, id); }
-__device__ __forceinline__ void claim_nbrs(const Mesh &m, int *cl, int t, int id) {
-  claim(cl, t, id);
+// Claims hold priorities (cdt_core.cuh prio): the smallest wins.
+__device__ __forceinline__ void claim(unsigned *cl, int t, unsigned pr) { atomicMin(cl + t, pr); }
+__device__ __forceinline__ void claim_nbrs(const Mesh &m, unsigned *cl, int t, unsigned pr) {
+  claim(cl, t, pr);
   for (int i = 0; i < 3; ++i) {
     const int nb = m.nbr[3 * t + i];
-    if (nb >= 0) claim(cl, cdt::nb_tri(nb), id);
+    if (nb >= 0) claim(cl, cdt::nb_tri(nb), pr);
   }
 }
 
 // Locate every pending point and claim what its insertion changes.
 __global__ void k_ins_locate(Mesh m, const int *__restrict__ pend, int np, int *start, Loc *loc,
-                             int *cl, int *err) {
+                             unsigned *cl, int *err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   const int p = pend[q];
+  const unsigned pr = cdt::prio((unsigned)p);
   Loc L;
   L.kind = cdt::locate(m, p, start[q], kWalk, &L.t, &L.i);
   L.cnt = 0;
@@ -191,11 +203,11 @@ __global__ void k_ins_locate(Mesh m, const int *__restrict__ pend, int np, int *
   } else if (L.kind == cdt::kLocVertex) {
     atomicOr(err, kErrDuplicate);
   } else if (L.kind == cdt::kLocIn) {
-    claim_nbrs(m, cl, L.t, p);
+    claim_nbrs(m, cl, L.t, pr);
   } else if (L.kind == cdt::kLocEdge) {
-    claim_nbrs(m, cl, L.t, p);
+    claim_nbrs(m, cl, L.t, pr);
     const int nb = m.nbr[3 * L.t + L.i];
-    if (nb >= 0) claim_nbrs(m, cl, cdt::nb_tri(nb), p);
+    if (nb >= 0) claim_nbrs(m, cl, cdt::nb_tri(nb), pr);
   } else {  // outside: the visible hull edges around the exit edge
     int ft = L.t, fi = L.i, back = 0, ok = 1;
     int bt[kChain], bi[kChain];  // the edges before the exit edge, nearest first
@@ -254,22 +266,22 @@ __global__ void k_ins_locate(Mesh m, const int *__restrict__ pend, int np, int *
       // claim the chain and the hull edges just before and after it, so that
       // two points never extend the hull next to each other in one round
       L.cnt = cnt;
-      for (int k = 0; k < cnt; ++k) claim(cl, L.et[k], p);
-      if (L.before >= 0) claim(cl, L.before, p);
-      if (L.after >= 0) claim(cl, L.after, p);
+      for (int k = 0; k < cnt; ++k) claim(cl, L.et[k], pr);
+      if (L.before >= 0) claim(cl, L.before, pr);
+      if (L.after >= 0) claim(cl, L.after, pr);
     }
   }
   loc[q] = L;
 }
 
-__device__ __forceinline__ bool owns(const Mesh &m, const int *cl, int t, int id) {
-  return cl[t] == id;
+__device__ __forceinline__ bool owns(const Mesh &m, const unsigned *cl, int t, unsigned pr) {
+  return cl[t] == pr;
 }
-__device__ bool owns_nbrs(const Mesh &m, const int *cl, int t, int id) {
-  if (!owns(m, cl, t, id)) return false;
+__device__ bool owns_nbrs(const Mesh &m, const unsigned *cl, int t, unsigned pr) {
+  if (!owns(m, cl, t, pr)) return false;
   for (int i = 0; i < 3; ++i) {
     const int nb = m.nbr[3 * t + i];
-    if (nb >= 0 && !owns(m, cl, cdt::nb_tri(nb), id)) return false;
+    if (nb >= 0 && !owns(m, cl, cdt::nb_tri(nb), pr)) return false;
   }
   return true;
 }
@@ -277,16 +289,17 @@ __device__ bool owns_nbrs(const Mesh &m, const int *cl, int t, int id) {
 // Insert the points that won every claim; the others stay pending (their
 // walk starts next round from the triangle they reached).
 __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *start,
-                            const Loc *__restrict__ loc, const int *cl, int *ntri, int cap,
+                            const Loc *__restrict__ loc, const unsigned *cl, int *ntri, int cap,
                             int *done, int *err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   const int p = pend[q];
+  const unsigned pr = cdt::prio((unsigned)p);
   const Loc &L = loc[q];
   if (L.kind == cdt::kLocFail || L.kind == cdt::kLocVertex) return;
   start[q] = L.t;
   if (L.kind == cdt::kLocIn) {
-    if (!owns_nbrs(m, cl, L.t, p)) return;
+    if (!owns_nbrs(m, cl, L.t, pr)) return;
     const int s = atomicAdd(ntri, 2);
     if (s + 2 > cap) {
       atomicOr(err, kErrCapacity);
@@ -294,9 +307,9 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
     }
     cdt::split_in(m, L.t, p, s, s + 1);
   } else if (L.kind == cdt::kLocEdge) {
-    if (!owns_nbrs(m, cl, L.t, p)) return;
+    if (!owns_nbrs(m, cl, L.t, pr)) return;
     const int nb = m.nbr[3 * L.t + L.i];
-    if (nb >= 0 && !owns_nbrs(m, cl, cdt::nb_tri(nb), p)) return;
+    if (nb >= 0 && !owns_nbrs(m, cl, cdt::nb_tri(nb), pr)) return;
     const int k = nb >= 0 ? 2 : 1;
     const int s = atomicAdd(ntri, k);
     if (s + k > cap) {
@@ -305,8 +318,8 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
     }
     cdt::split_edge(m, L.t, L.i, p, s, s + 1);
   } else {
-    bool won = (L.before < 0 || owns(m, cl, L.before, p)) && (L.after < 0 || owns(m, cl, L.after, p));
-    for (int k = 0; k < L.cnt && won; ++k) won = owns(m, cl, L.et[k], p);
+    bool won = (L.before < 0 || owns(m, cl, L.before, pr)) && (L.after < 0 || owns(m, cl, L.after, pr));
+    for (int k = 0; k < L.cnt && won; ++k) won = owns(m, cl, L.et[k], pr);
     if (!won) return;
     const int s = atomicAdd(ntri, L.cnt);
     if (s + L.cnt > cap) {
@@ -325,8 +338,8 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
 
 // Each triangle: the first of its edges towards a higher-numbered neighbour
 // that wants a flip; the flip claims both triangles and the four outer
-// neighbours with the id 3 t + i.
-__global__ void k_flip_mark(Mesh m, int T, int *cand, int *cl, int *found) {
+// neighbours with the priority of 3 t + i.
+__global__ void k_flip_mark(Mesh m, int T, int *cand, unsigned *cl, int *found) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int c = 0;
@@ -341,37 +354,116 @@ __global__ void k_flip_mark(Mesh m, int T, int *cand, int *cl, int *found) {
   cand[t] = c;
   if (!c) return;
   atomicAdd(found, 1);
-  const int i = c - 1, id = 3 * t + i;
+  const int i = c - 1;
+  const unsigned pr = cdt::prio((unsigned)(3 * t + i));
   const int t2 = cdt::nb_tri(m.nbr[3 * t + i]);
-  claim_nbrs(m, cl, t, id);
-  claim_nbrs(m, cl, t2, id);
+  claim_nbrs(m, cl, t, pr);
+  claim_nbrs(m, cl, t2, pr);
 }
 
-__global__ void k_flip_apply(Mesh m, int T, const int *cand, const int *cl, int *flips) {
+__global__ void k_flip_apply(Mesh m, int T, const int *cand, const unsigned *cl, int *flips) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T || !cand[t]) return;
-  const int i = cand[t] - 1, id = 3 * t + i;
+  const int i = cand[t] - 1;
+  const unsigned pr = cdt::prio((unsigned)(3 * t + i));
   const int t2 = cdt::nb_tri(m.nbr[3 * t + i]);
-  if (!owns_nbrs(m, cl, t, id) || !owns_nbrs(m, cl, t2, id)) return;
+  if (!owns_nbrs(m, cl, t, pr) || !owns_nbrs(m, cl, t2, pr)) return;
   cdt::flip(m, t, i);
   atomicAdd(flips, 1);
 }
 
 // ---- segments --------------------------------------------------------------
 
-// The segments one after the other (they share vertices and crossing edges):
-// one thread.  A segment with vertices inside it becomes the chain of edges
-// between them (as constrained Delaunay triangulations split such segments);
-// bad index pairs and crossing segments set err.
-__global__ void k_segments(Mesh m, const int *__restrict__ segs, int S, int V, int *queue,
-                           int *stack, int *err) {
+enum SegState { kSegPending = 0, kSegDone = 1, kSegSerial = 2 };
+
+// Segments that are already edges are marked at once (atomic bit sets, the
+// mesh is otherwise read-only here); the others wait for the rounds.  Bad
+// index pairs set err.
+__global__ void k_seg_mark(Mesh m, const int *__restrict__ segs, int S, int V, int *state,
+                           int *err) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= S) return;
+  const int a = segs[2 * k], b = segs[2 * k + 1];
+  if (a < 0 || b < 0 || a >= V || b >= V || a == b) {
+    atomicOr(err, kErrSegment);
+    state[k] = kSegDone;
+    return;
+  }
+  state[k] = cdt::mark_constraint(m, a, b, kRotate) ? kSegDone : kSegPending;
+}
+
+// A pending segment of the window [base, base + W) claims, with its priority,
+// the triangles around its ends and around every end of the edges crossing
+// it: all that its recovery reads or writes (Sloan's flips stay inside the
+// triangles the segment crosses, whose vertices are those ends, and rewrite
+// the back links of their neighbours, which lie around the same vertices).
+// The claimed triangles are listed for the apply pass.  A segment that meets
+// a vertex or a constraint, or crosses more than kCorr edges, goes to the
+// one-thread pass.
+__global__ void k_seg_locate(Mesh m, const int *__restrict__ segs, int base, int W, int *state,
+                             int *list, int *lcnt, unsigned *cl) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= W) return;
+  const int k = base + w;
+  if (state[k] != kSegPending) return;
+  const int a = segs[2 * k], b = segs[2 * k + 1];
+  int q[2 * kCorr], on = -1, cnt = 0;
+  if (cdt::collect_crossings(m, a, b, q, kCorr, kWalk, &on, &cnt) != cdt::kSegOk) {
+    state[k] = kSegSerial;
+    return;
+  }
+  int *L = list + (size_t)w * kClaim;
+  int n = 0;
+  for (int e = -2; e < 2 * cnt; ++e) {
+    const int v = e == -2 ? a : (e == -1 ? b : q[e]);
+    bool seen = false;
+    for (int f = -2; f < e && !seen; ++f) seen = (f == -2 ? a : (f == -1 ? b : q[f])) == v;
+    if (seen) continue;
+    const int c = cdt::fan(m, v, kRotate, L + n, kClaim - n);
+    if (c < 0) {
+      state[k] = kSegSerial;
+      return;
+    }
+    n += c;
+  }
+  const unsigned pr = cdt::prio((unsigned)k);
+  for (int i = 0; i < n; ++i) claim(cl, L[i], pr);
+  lcnt[w] = n;
+}
+
+// The segments that won every claim are recovered (cdt_core.cuh
+// recover_segment); the others count themselves pending for the next round.
+__global__ void k_seg_apply(Mesh m, const int *__restrict__ segs, int base, int W, int *state,
+                            const int *__restrict__ list, const int *__restrict__ lcnt,
+                            const unsigned *cl, int *pending, int *err) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= W) return;
+  const int k = base + w;
+  if (state[k] != kSegPending) return;
+  const int *L = list + (size_t)w * kClaim;
+  const unsigned pr = cdt::prio((unsigned)k);
+  for (int i = 0, n = lcnt[w]; i < n; ++i)
+    if (cl[L[i]] != pr) {
+      atomicAdd(pending, 1);
+      return;
+    }
+  int q[2 * kCorr], on = -1;
+  const int r = cdt::recover_segment(m, segs[2 * k], segs[2 * k + 1], q, kCorr, kWalk, &on);
+  if (r == cdt::kSegCrosses) atomicOr(err, kErrSegment);
+  else if (r != cdt::kSegOk) atomicOr(err, kErrSegLimit);
+  state[k] = kSegDone;
+}
+
+// The segments left to one thread, one after the other (they may share
+// crossing edges): long ones, and those with vertices inside them, which
+// become the chain of edges between those vertices (as constrained Delaunay
+// triangulations split such segments).  Crossing segments set err.
+__global__ void k_segments(Mesh m, const int *__restrict__ segs, int S, const int *state,
+                           int *queue, int *stack, int *err) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   for (int k = 0; k < S; ++k) {
+    if (state[k] == kSegDone) continue;
     const int a = segs[2 * k], b = segs[2 * k + 1];
-    if (a < 0 || b < 0 || a >= V || b >= V || a == b) {
-      atomicOr(err, kErrSegment);
-      continue;
-    }
     const int r = cdt::recover_chain(m, a, b, queue, kSegQueue, stack, kSegStack, kWalk);
     if (r == cdt::kSegCrosses) atomicOr(err, kErrSegment);
     else if (r != cdt::kSegOk) atomicOr(err, kErrSegLimit);
@@ -505,15 +597,18 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
   double *sxy = sc.take<double>(2 * (size_t)F + 2);
   i64 *X = sc.take<i64>((size_t)V), *Y = sc.take<i64>((size_t)V), *R = sc.take<i64>((size_t)V);
   int *tri = sc.take<int>(3 * (size_t)cap_t), *nbr = sc.take<int>(3 * (size_t)cap_t);
-  uint8_t *cons = sc.take<uint8_t>((size_t)cap_t);
+  unsigned *cons = sc.take<unsigned>((size_t)cap_t);
   int *vt = sc.take<int>((size_t)V);
-  int *cl = sc.take<int>((size_t)cap_t), *cand = sc.take<int>((size_t)cap_t);
-  int *ctr = sc.take<int>(8);  // [0] error bits, [1] triangles, [2] found, [3] flips, [4] pending
+  unsigned *cl = sc.take<unsigned>((size_t)cap_t);
+  int *cand = sc.take<int>((size_t)cap_t);
+  // [0] error bits, [1] triangles, [2] flips wanted, [3] flips made, [4] points
+  // pending, [5] segments pending
+  int *ctr = sc.take<int>(8);
   if (!sxy || !X || !Y || !R || !tri || !nbr || !cons || !vt || !cl || !cand || !ctr)
     return GCVT_ERR_ALLOC;
   CCK(launch_extract(bits, fixed, n, colcnt, 1.0, 0.0, 0.0, sxy, F, colcnt + n, s));
   CCK(cudaMemsetAsync(ctr, 0, 8 * sizeof(int), s));
-  CCK(cudaMemsetAsync(cons, 0, (size_t)cap_t, s));
+  CCK(cudaMemsetAsync(cons, 0, (size_t)cap_t * sizeof(unsigned), s));
   k_cdt_coords<<<nblk(V, 256), 256, 0, s>>>(sxy, (int)F, cxy, C, scale, left, lower, n, X, Y, R,
                                             ctr);
   CCK(cudaGetLastError());
@@ -544,13 +639,16 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     CCK(cudaStreamSynchronize(s));
     return GCVT_OK;
   };
-  // Delaunay flip rounds until none is left
+  // Delaunay flip rounds until none is left, read back every kFlipPoll
+  // rounds (a round that finds nothing to flip changes nothing)
   auto flips = [&]() -> int {
-    for (int r = 0; r < kFlipRounds; ++r) {
-      CCK(cudaMemsetAsync(cl, 0x7f, (size_t)T * sizeof(int), s));
-      CCK(cudaMemsetAsync(ctr + 2, 0, 2 * sizeof(int), s));
-      k_flip_mark<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 2);
-      k_flip_apply<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 3);
+    for (int r = 0; r < kFlipRounds; r += kFlipPoll) {
+      for (int i = 0; i < kFlipPoll; ++i) {
+        CCK(cudaMemsetAsync(cl, 0xff, (size_t)T * sizeof(unsigned), s));
+        CCK(cudaMemsetAsync(ctr + 2, 0, 2 * sizeof(int), s));
+        k_flip_mark<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 2);
+        k_flip_apply<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 3);
+      }
       CCK(cudaGetLastError());
       if ((rc = pull())) return rc;
       if (h[0] || h[2] == 0) return GCVT_OK;
@@ -573,7 +671,7 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     {
       int np = C;
       for (int r = 0; r < kInsertRounds && np > 0; ++r) {
-        CCK(cudaMemsetAsync(cl, 0x7f, (size_t)cap_t * sizeof(int), s));
+        CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
         CCK(cudaMemsetAsync(done, 0, (size_t)np * sizeof(int), s));
         k_ins_locate<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr);
         k_ins_apply<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr + 1, cap_t,
@@ -594,11 +692,31 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
   }
   if ((rc = pull())) return rc;
   T = h[1];
-  // 4. segments, 5. flips that keep them
+  // 4. segments: those already edges marked at once, the others recovered
+  // in parallel rounds of claims (window by window), what is left by one
+  // thread; 5. flips that keep them
   if (!h[0] && S > 0) {
+    const int Wmax = S < kSegWindow ? S : kSegWindow;
+    int *state = sc.take<int>((size_t)S), *lcnt = sc.take<int>((size_t)Wmax);
+    int *list = sc.take<int>((size_t)Wmax * kClaim);
     int *queue = sc.take<int>(2 * (size_t)kSegQueue), *stack = sc.take<int>(2 * (size_t)kSegStack);
-    if (!queue || !stack) return GCVT_ERR_ALLOC;
-    k_segments<<<1, 32, 0, s>>>(m, segs, S, (int)V, queue, stack, ctr);
+    if (!state || !lcnt || !list || !queue || !stack) return GCVT_ERR_ALLOC;
+    k_seg_mark<<<nblk(S, 256), 256, 0, s>>>(m, segs, S, (int)V, state, ctr);
+    CCK(cudaGetLastError());
+    for (int base = 0; base < S; base += kSegWindow) {
+      const int W = S - base < kSegWindow ? S - base : kSegWindow;
+      for (int r = 0; r < kSegRounds; ++r) {
+        CCK(cudaMemsetAsync(cl, 0xff, (size_t)T * sizeof(unsigned), s));
+        CCK(cudaMemsetAsync(ctr + 5, 0, sizeof(int), s));
+        k_seg_locate<<<nblk(W, 128), 128, 0, s>>>(m, segs, base, W, state, list, lcnt, cl);
+        k_seg_apply<<<nblk(W, 128), 128, 0, s>>>(m, segs, base, W, state, list, lcnt, cl, ctr + 5,
+                                                 ctr);
+        CCK(cudaGetLastError());
+        if ((rc = pull())) return rc;
+        if (h[5] == 0) break;
+      }
+    }
+    k_segments<<<1, 32, 0, s>>>(m, segs, S, state, queue, stack, ctr);
     CCK(cudaGetLastError());
     if ((rc = pull())) return rc;
   }

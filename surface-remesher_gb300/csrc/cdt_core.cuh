@@ -40,10 +40,24 @@ constexpr int kNone = -1;
 struct Mesh {
   int *tri;
   int *nbr;
-  uint8_t *cons;
+  unsigned *cons;
   int *vt;
   const i64 *X, *Y, *R;
 };
+
+// The priority of an operation with id x in a round of claims (the
+// smallest wins): a bijection of 32-bit words (xor-shift and odd-multiplier
+// steps, each invertible; the "lowbias32" constants of C. Wellons' hash
+// prospector), so distinct ids never tie and neighbours along a list do not
+// win in index order.
+CDT_HD unsigned prio(unsigned x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
 
 CDT_HD int nb_tri(int v) { return v >> 2; }
 CDT_HD int nb_idx(int v) { return v & 3; }
@@ -154,9 +168,9 @@ CDT_HD void split_in(const Mesh &m, int t, int p, int n1, int n2) {
   set_tri(m, t, a, b, p);
   set_tri(m, n1, b, c, p);
   set_tri(m, n2, c, a, p);
-  m.cons[t] = (uint8_t)(((ct >> 2) & 1) << 2);  // (a, b)
-  m.cons[n1] = (uint8_t)((ct & 1) << 2);        // (b, c)
-  m.cons[n2] = (uint8_t)(((ct >> 1) & 1) << 2); // (c, a)
+  m.cons[t] = (unsigned)(((ct >> 2) & 1) << 2);  // (a, b)
+  m.cons[n1] = (unsigned)((ct & 1) << 2);        // (b, c)
+  m.cons[n2] = (unsigned)(((ct >> 1) & 1) << 2); // (c, a)
   m.nbr[3 * t] = pack_nb(n1, 1);
   m.nbr[3 * t + 1] = pack_nb(n2, 0);
   link(m, t, 2, nc);
@@ -191,8 +205,8 @@ CDT_HD void split_edge(const Mesh &m, int t, int i, int p, int n1, int n2) {
     m.nbr[3 * n1] = kNone;
     link(m, n1, 1, nca);
     m.nbr[3 * n1 + 2] = pack_nb(t, 1);
-    m.cons[t] = (uint8_t)(cbc | (cab << 2));
-    m.cons[n1] = (uint8_t)(cbc | (cca << 1));
+    m.cons[t] = (unsigned)(cbc | (cab << 2));
+    m.cons[n1] = (unsigned)(cbc | (cca << 1));
     m.vt[a] = t;
     m.vt[b] = t;
     m.vt[c] = n1;
@@ -220,10 +234,10 @@ CDT_HD void split_edge(const Mesh &m, int t, int i, int p, int n1, int n2) {
   m.nbr[3 * n2] = pack_nb(t, 0);
   link(m, n2, 1, nbd);
   m.nbr[3 * n2 + 2] = pack_nb(t2, 1);
-  m.cons[t] = (uint8_t)(cbc | (cab << 2));
-  m.cons[n1] = (uint8_t)(cbc | (cca << 1));
-  m.cons[t2] = (uint8_t)(cbc | (cdc << 2));
-  m.cons[n2] = (uint8_t)(cbc | (cbd << 1));
+  m.cons[t] = (unsigned)(cbc | (cab << 2));
+  m.cons[n1] = (unsigned)(cbc | (cca << 1));
+  m.cons[t2] = (unsigned)(cbc | (cdc << 2));
+  m.cons[n2] = (unsigned)(cbc | (cbd << 1));
   m.vt[a] = t;
   m.vt[b] = t;
   m.vt[c] = n1;
@@ -313,8 +327,8 @@ CDT_HD void flip(const Mesh &m, int t, int i) {
   link(m, t2, 0, ndc);
   link(m, t2, 1, nca);
   m.nbr[3 * t2 + 2] = pack_nb(t, 1);
-  m.cons[t] = (uint8_t)(cbd | (cab << 2));
-  m.cons[t2] = (uint8_t)(cdc | (cca << 1));
+  m.cons[t] = (unsigned)(cbd | (cab << 2));
+  m.cons[t2] = (unsigned)(cdc | (cca << 1));
   m.vt[a] = t;
   m.vt[b] = t;
   m.vt[d] = t;
@@ -356,39 +370,65 @@ CDT_HD bool find_edge(const Mesh &m, int u, int w, int max_steps, int *ot, int *
   return false;
 }
 
+// Set constraint bits of a triangle; atomic on the device, where segments
+// already present as edges are marked by many threads at once.
+CDT_HD void or_bits(unsigned *w, unsigned bits) {
+#ifdef __CUDA_ARCH__
+  atomicOr(w, bits);
+#else
+  *w |= bits;
+#endif
+}
+
 // Mark the edge {u, w} a constraint in both of its triangles; false if it is
 // not an edge.
 CDT_HD bool mark_constraint(const Mesh &m, int u, int w, int max_steps) {
   int t, k;
-  bool found = false;
-  if (find_edge(m, u, w, max_steps, &t, &k)) {  // (u, w) is opposite v[k+2]
-    m.cons[t] |= (uint8_t)(1u << pv3(k));
-    const int nb = m.nbr[3 * t + pv3(k)];
-    if (nb >= 0) m.cons[nb_tri(nb)] |= (uint8_t)(1u << nb_idx(nb));
-    found = true;
-  } else if (find_edge(m, w, u, max_steps, &t, &k)) {
-    m.cons[t] |= (uint8_t)(1u << pv3(k));
-    const int nb = m.nbr[3 * t + pv3(k)];
-    if (nb >= 0) m.cons[nb_tri(nb)] |= (uint8_t)(1u << nb_idx(nb));
-    found = true;
+  if (!find_edge(m, u, w, max_steps, &t, &k) && !find_edge(m, w, u, max_steps, &t, &k))
+    return false;
+  // the edge is opposite v[k+2] of t
+  or_bits(m.cons + t, 1u << pv3(k));
+  const int nb = m.nbr[3 * t + pv3(k)];
+  if (nb >= 0) or_bits(m.cons + nb_tri(nb), 1u << nb_idx(nb));
+  return true;
+}
+
+// The triangles around vertex v (from vt[v], counter-clockwise until the
+// start comes back or the hull is reached, then clockwise from the start):
+// their count, or -1 when they are more than cap or a rotation runs past
+// max_steps.
+CDT_HD int fan(const Mesh &m, int v, int max_steps, int *out, int cap) {
+  const int t0 = m.vt[v];
+  int cnt = 0;
+  for (int dir = 0; dir < 2; ++dir) {
+    int ct = t0, s = 0;
+    for (; s < max_steps; ++s) {
+      if (dir == 0 || ct != t0) {
+        if (cnt >= cap) return -1;
+        out[cnt++] = ct;
+      }
+      const int *w = m.tri + 3 * ct;
+      const int k = w[0] == v ? 0 : (w[1] == v ? 1 : 2);
+      const int nb = m.nbr[3 * ct + (dir == 0 ? nx3(k) : pv3(k))];
+      if (nb < 0) break;
+      ct = nb_tri(nb);
+      if (ct == t0) return cnt;  // all the way round
+    }
+    if (s == max_steps) return -1;
   }
-  return found;
+  return cnt;
 }
 
 enum { kSegOk = 0, kSegVertexOn = 1, kSegLimit = 2, kSegBroken = 3, kSegCrosses = 4 };
 
-// Make (a, b) an edge by flipping the edges that cross it (Sloan's method):
-// the crossing edges are collected by walking from a towards b, then taken
-// from a queue in turn -- an edge whose quadrilateral is strictly convex is
-// flipped (its new diagonal goes back into the queue if it still crosses
-// (a, b)), any other goes to the back.  Then (a, b) is marked a constraint.
-// queue: scratch of qcap vertex pairs.  kSegVertexOn (*on = the vertex) when
-// a vertex lies inside the segment: the caller recovers the two pieces
-// instead; kSegCrosses when the segment crosses a constraint already in
-// place (invalid input), kSegLimit when a bound runs out.
-CDT_HD int recover_segment(const Mesh &m, int a, int b, int *queue, int qcap, int max_steps,
-                           int *on) {
-  if (mark_constraint(m, a, b, max_steps)) return kSegOk;
+// The edges crossing the segment (a, b), which is not an edge, as vertex
+// pairs in queue[0 .. *cnt_out), walking from a towards b; read-only.
+// kSegVertexOn (*on = the vertex) when a vertex lies inside the segment,
+// kSegCrosses when a crossing edge is a constraint, kSegLimit when qcap or
+// max_steps runs out.
+CDT_HD int collect_crossings(const Mesh &m, int a, int b, int *queue, int qcap, int max_steps,
+                             int *on, int *cnt_out) {
+  *cnt_out = 0;
   // the triangle at a whose wedge holds the direction to b
   int t = m.vt[a], k = 0;
   bool got = false;
@@ -416,40 +456,59 @@ CDT_HD int recover_segment(const Mesh &m, int a, int b, int *queue, int qcap, in
   }
   if (!got) return kSegBroken;
   // walk to b collecting the crossing edges (left end l, right end r)
-  int head = 0, tail = 0, cnt = 0;
-  {
-    const int *v = m.tri + 3 * t;
-    int r = v[nx3(k)], l = v[pv3(k)];  // b is left of a->r and right of a->l
-    int ct = t, ce = k;                // the crossing edge (r, l) is opposite v[ce] of ct
-    for (int s = 0; s < max_steps; ++s) {
-      if (cnt >= qcap) return kSegLimit;
-      if ((m.cons[ct] >> ce) & 1) return kSegCrosses;
-      queue[2 * tail] = r;
-      queue[2 * tail + 1] = l;
-      tail = (tail + 1) % qcap;
-      ++cnt;
-      const int nb = m.nbr[3 * ct + ce];
-      if (nb < 0) return kSegBroken;
-      ct = nb_tri(nb);
-      const int j = nb_idx(nb);
-      const int y = m.tri[3 * ct + j];
-      if (y == b) break;
-      const int oy = orient(m, a, b, y);
-      if (oy == 0) {  // inside the segment: the walk stays between a and b
-        *on = y;
-        return kSegVertexOn;
-      }
-      // in ct = (y, l, r) (counter-clockwise), the next crossing edge is the
-      // one between y and the end on y's other side
-      if (oy < 0) {  // y right of a->b: replaces r; edge (y, l) is opposite r
-        r = y;
-        ce = pv3(j);
-      } else {       // y left: replaces l; edge (r, y) is opposite l
-        l = y;
-        ce = nx3(j);
-      }
+  int cnt = 0;
+  const int *v = m.tri + 3 * t;
+  int r = v[nx3(k)], l = v[pv3(k)];  // b is left of a->r and right of a->l
+  int ct = t, ce = k;                // the crossing edge (r, l) is opposite v[ce] of ct
+  for (int s = 0; s < max_steps; ++s) {
+    if (cnt >= qcap) return kSegLimit;
+    if ((m.cons[ct] >> ce) & 1) return kSegCrosses;
+    queue[2 * cnt] = r;
+    queue[2 * cnt + 1] = l;
+    ++cnt;
+    const int nb = m.nbr[3 * ct + ce];
+    if (nb < 0) return kSegBroken;
+    ct = nb_tri(nb);
+    const int j = nb_idx(nb);
+    const int y = m.tri[3 * ct + j];
+    if (y == b) {
+      *cnt_out = cnt;
+      return kSegOk;
+    }
+    const int oy = orient(m, a, b, y);
+    if (oy == 0) {  // inside the segment: the walk stays between a and b
+      *on = y;
+      return kSegVertexOn;
+    }
+    // in ct = (y, l, r) (counter-clockwise), the next crossing edge is the
+    // one between y and the end on y's other side
+    if (oy < 0) {  // y right of a->b: replaces r; edge (y, l) is opposite r
+      r = y;
+      ce = pv3(j);
+    } else {       // y left: replaces l; edge (r, y) is opposite l
+      l = y;
+      ce = nx3(j);
     }
   }
+  return kSegLimit;
+}
+
+// Make (a, b) an edge by flipping the edges that cross it (Sloan's method):
+// the crossing edges are collected by walking from a towards b, then taken
+// from a queue in turn -- an edge whose quadrilateral is strictly convex is
+// flipped (its new diagonal goes back into the queue if it still crosses
+// (a, b)), any other goes to the back.  Then (a, b) is marked a constraint.
+// queue: scratch of qcap vertex pairs.  kSegVertexOn (*on = the vertex) when
+// a vertex lies inside the segment: the caller recovers the two pieces
+// instead; kSegCrosses when the segment crosses a constraint already in
+// place (invalid input), kSegLimit when a bound runs out.
+CDT_HD int recover_segment(const Mesh &m, int a, int b, int *queue, int qcap, int max_steps,
+                           int *on) {
+  if (mark_constraint(m, a, b, max_steps)) return kSegOk;
+  int cnt = 0;
+  const int got = collect_crossings(m, a, b, queue, qcap, max_steps, on, &cnt);
+  if (got != kSegOk) return got;
+  int head = 0, tail = cnt % qcap;
   // Sloan's loop
   for (int s = 0; cnt > 0; ++s) {
     if (s >= max_steps) return kSegLimit;

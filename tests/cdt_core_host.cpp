@@ -9,8 +9,12 @@
 // stdin:  V, then V lines "X Y R"; T, then T lines "a b c" (counter-clockwise,
 //         any triangulation of the first F points); C, then C point indices
 //         to insert in order; S, then S lines "a b".
-// stdout: "ok T" then T lines "a b c", or "error <code>".
+// stdout: "ok T L" (L segments left to the one-at-a-time pass) then T lines
+//         "a b c", or "error <code>".
+// argv[1] == "rounds": the segments go through the GPU's claim rounds first.
+#include <algorithm>
 #include <cstdio>
+#include <string>
 #include <map>
 #include <utility>
 #include <vector>
@@ -19,7 +23,9 @@
 
 using namespace cvtgb::cdt;
 
-int main() {
+int main(int argc, char **argv) {
+  const bool rounds = argc > 1 && std::string(argv[1]) == "rounds";
+  int serial = 0;
   int V = 0;
   if (scanf("%d", &V) != 1) return 1;
   std::vector<i64> X(V), Y(V), R(V);
@@ -29,7 +35,7 @@ int main() {
   if (scanf("%d", &T) != 1) return 1;
   const int cap = 2 * V + 16;
   std::vector<int> tri(3 * (size_t)cap), nbr(3 * (size_t)cap, kNone), vt(V, 0);
-  std::vector<uint8_t> cons(cap, 0);
+  std::vector<unsigned> cons(cap, 0);
   for (int t = 0; t < T; ++t)
     if (scanf("%d %d %d", &tri[3 * t], &tri[3 * t + 1], &tri[3 * t + 2]) != 3) return 1;
   std::map<std::pair<int, int>, int> dir;
@@ -126,11 +132,97 @@ int main() {
   }
   int S = 0;
   if (scanf("%d", &S) != 1) return 1;
-  std::vector<int> queue(2 * 4096), stack(2 * 256);
+  std::vector<int> queue(2 * 4096), stack(2 * 256), sa(S), sb(S);
+  for (int k = 0; k < S; ++k)
+    if (scanf("%d %d", &sa[k], &sb[k]) != 2) return 1;
+  // rounds: the GPU's parallel segment rounds replayed (cdt.cu k_seg_mark,
+  // k_seg_locate, k_seg_apply); each winner's recovery must change only
+  // triangles it claimed and vt only of vertices it claimed around, and no
+  // two winners may share a claimed triangle
+  std::vector<int> state(S, 0);  // 0 pending, 1 done, 2 left to the one-at-a-time pass
+  if (rounds) {
+    const int kCorr = 8, kClaim = 128;
+    for (int k = 0; k < S; ++k) state[k] = mark_constraint(m, sa[k], sb[k], 4096) ? 1 : 0;
+    for (int round = 0; round < 100000; ++round) {
+      std::vector<unsigned> cl(T, 0xffffffffu);
+      std::vector<std::vector<int>> lists(S), verts(S);
+      for (int k = 0; k < S; ++k) {
+        if (state[k] != 0) continue;
+        int q[2 * kCorr], on = -1, cnt = 0;
+        if (collect_crossings(m, sa[k], sb[k], q, kCorr, 1 << 20, &on, &cnt) != kSegOk) {
+          state[k] = 2;
+          continue;
+        }
+        std::vector<int> L(kClaim);
+        int n = 0;
+        bool ok = true;
+        for (int e = -2; e < 2 * cnt && ok; ++e) {
+          const int v = e == -2 ? sa[k] : (e == -1 ? sb[k] : q[e]);
+          bool seen = false;
+          for (int f = -2; f < e && !seen; ++f)
+            seen = (f == -2 ? sa[k] : (f == -1 ? sb[k] : q[f])) == v;
+          if (seen) continue;
+          verts[k].push_back(v);
+          const int c = fan(m, v, 4096, L.data() + n, kClaim - n);
+          if (c < 0) ok = false;
+          else n += c;
+        }
+        if (!ok) {
+          state[k] = 2;
+          continue;
+        }
+        L.resize(n);
+        for (int t : L) cl[t] = std::min(cl[t], prio((unsigned)k));
+        lists[k] = L;
+      }
+      bool any = false;
+      std::vector<int> owner(T, -1);
+      for (int k = 0; k < S; ++k) {
+        if (state[k] != 0) continue;
+        bool won = true;
+        for (int t : lists[k]) won = won && cl[t] == prio((unsigned)k);
+        if (!won) continue;
+        for (int t : lists[k]) {
+          if (owner[t] >= 0 && owner[t] != k) {
+            printf("error shared claim\n");
+            return 0;
+          }
+          owner[t] = k;
+        }
+        const std::vector<int> tri0(tri.begin(), tri.begin() + 3 * T),
+            nbr0(nbr.begin(), nbr.begin() + 3 * T), vt0(vt);
+        const std::vector<unsigned> cons0(cons.begin(), cons.begin() + T);
+        int q[2 * kCorr], on = -1;
+        const int r = recover_segment(m, sa[k], sb[k], q, kCorr, 1 << 20, &on);
+        if (r != kSegOk) {
+          printf("error segment %d\n", r);
+          return 0;
+        }
+        for (int t = 0; t < T; ++t) {
+          bool changed = cons[t] != cons0[t];
+          for (int i = 0; i < 3; ++i)
+            changed = changed || tri[3 * t + i] != tri0[3 * t + i] || nbr[3 * t + i] != nbr0[3 * t + i];
+          if (changed && cl[t] != prio((unsigned)k)) {
+            printf("error unclaimed write\n");
+            return 0;
+          }
+        }
+        for (int v = 0; v < V; ++v)
+          if (vt[v] != vt0[v] &&
+              std::find(verts[k].begin(), verts[k].end(), v) == verts[k].end()) {
+            printf("error unclaimed vertex\n");
+            return 0;
+          }
+        state[k] = 1;
+        any = true;
+      }
+      if (!any) break;
+    }
+  }
   for (int k = 0; k < S; ++k) {
-    int a, b;
-    if (scanf("%d %d", &a, &b) != 2) return 1;
-    const int r = recover_chain(m, a, b, queue.data(), 4096, stack.data(), 256, 1 << 20);
+    if (state[k] == 1) continue;
+    if (state[k] == 2) ++serial;
+    const int r = recover_chain(m, sa[k], sb[k], queue.data(), 4096, stack.data(), 256, 1 << 20);
     if (r != kSegOk) {
       printf("error segment %d\n", r);
       return 0;
@@ -161,7 +253,7 @@ int main() {
     out[3 * pos + 1] = b;
     out[3 * pos + 2] = c;
   }
-  printf("ok %d\n", T);
+  printf("ok %d %d\n", T, serial);
   for (int t = 0; t < T; ++t) printf("%d %d %d\n", out[3 * t], out[3 * t + 1], out[3 * t + 2]);
   return 0;
 }

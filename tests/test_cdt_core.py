@@ -43,15 +43,21 @@ def start_triangulation(pts):
     return tri[o != 0]
 
 
-def run(binary, X, Y, R, tris, inserts, segs):
+def run(binary, X, Y, R, tris, inserts, segs, rounds=False, serial=None):
+    """The harness's triangles; with rounds=True the segments go through the
+    GPU's claim rounds (the harness checks every winner writes only what it
+    claimed) and `serial`, when given, receives how many were left to the
+    one-at-a-time pass."""
     lines = [str(len(X))] + ["%d %d %d" % (x, y, r) for x, y, r in zip(X, Y, R)]
     lines += [str(len(tris))] + ["%d %d %d" % tuple(t) for t in tris]
     lines += [str(len(inserts))] + [str(int(p)) for p in inserts]
     lines += [str(len(segs))] + ["%d %d" % tuple(s) for s in segs]
-    r = subprocess.run([binary], input="\n".join(lines) + "\n", capture_output=True, text=True,
-                       check=True)
+    r = subprocess.run([binary] + (["rounds"] if rounds else []), input="\n".join(lines) + "\n",
+                       capture_output=True, text=True, check=True)
     head, *rest = r.stdout.strip().split("\n")
     assert head.startswith("ok"), head
+    if serial is not None:
+        serial.append(int(head.split()[2]))
     return np.array([list(map(int, l.split())) for l in rest], np.int64)
 
 
@@ -176,3 +182,22 @@ def test_host_cdt_splits_a_segment_at_points_inside_it(host_bin):
     tris = run(host_bin, X, Y, R, start_triangulation(sp), [F, F + 1], segs)
     info = D.check_cdt(np.stack([X, Y], 1), tris, segs, R.tolist())
     assert len(on) >= 1 and info["constraints"] == len(on) + 1
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 21, 22])
+def test_claim_rounds_give_the_sequential_result(host_bin, seed):
+    # the GPU's parallel segment rounds, replayed: winners touch only what
+    # they claimed, and the result is the unique constrained Delaunay
+    # triangulation, the same as segment after segment
+    if seed < 20:
+        sp, X, Y, R, segs, F, C = disk_case(seed, ring=48, inner=0, ring_r=21.0)
+    else:
+        sp, X, Y, R, segs, F, C = disk_case(seed, sites=220, ring=12, inner=0, ring_r=21.5)
+    start = start_triangulation(sp)
+    ins = np.arange(F, F + C)
+    seq = run(host_bin, X, Y, R, start, ins, segs)
+    serial = []
+    par = run(host_bin, X, Y, R, start, ins, segs, rounds=True, serial=serial)
+    assert np.array_equal(seq, par)
+    D.check_cdt(np.stack([X, Y], 1), par, segs, R.tolist())
+    assert serial[0] < len(segs)  # most segments recovered in the rounds
