@@ -226,6 +226,19 @@ __device__ __forceinline__ void fold_chunk(CellSums &c, float rw, float rx, floa
   dfa(c.eh, c.el, qh, ql);
 }
 
+// Sums of row v = [da, db] (relative columns) into c: FP32 over chunks of at
+// most 16 pixels (relative error below 16 ulp of the chunk), chunks folded
+// into the two-float cell sums.
+__device__ __forceinline__ void row_sums(const float *__restrict__ row, int da, int db, int v,
+                                         CellSums &c) {
+  const float fv = (float)v, fv2 = (float)(v * v);
+  for (int u0 = da; u0 <= db; u0 += 16) {
+    float rw, rx, rq;
+    chunk_sums(row, u0, min(db, u0 + 15), rw, rx, rq);
+    fold_chunk(c, rw, rx, rq, fv, fv2);
+  }
+}
+
 // The pixels [da, db] of row v the cell with bounds [lo, hi] sums: clipped to
 // the density support and the covering disc; false when none.
 __device__ __forceinline__ bool row_span(const LevelBufs &a, int sx, int sy, int rb2, int v,
@@ -242,129 +255,13 @@ __device__ __forceinline__ bool row_span(const LevelBufs &a, int sx, int sy, int
   return true;
 }
 
-// The spans the row walk has found and not yet summed, in walk order: row
-// v with pixels [da, db] (relative columns) as {v, da | db << 16}.  The walk
-// bounds rows without touching the density; the sums then read the rows of
-// a batch together (sum_spans), so their loads are in flight at once.
-constexpr int kSpanRows = 32;
-
-struct SpanBuf {
-  int2 row[kSpanRows];
-  int cnt;
-};
-
-// Sums of one batch: chunk X = [ua, ua + la) of row va in slots 0 .. la - 1,
-// chunk Y = [ub, ub + lb) of row vb in slots 8 .. 8 + lb - 1 (lb = 0: none);
-// a chunk longer than 8 pixels is alone (wide) and fills slots 0 .. la - 1.
-// Every slot's load is issued before any sum; each chunk is summed in pixel
-// order as chunk_sums sums it and folded by fold_chunk in the walk's order,
-// as the one-site-per-warp path (cell_sums_warp) folds its rows' chunks: the
-// two paths' sums are equal bit for bit.
-__device__ __forceinline__ void sum_batch(const float *__restrict__ base, int n, int va, int ua,
-                                          int la, int vb, int ub, int lb, CellSums &c) {
-  const float *pa = base + (ptrdiff_t)va * n + ua;
-  const float *pb = base + (ptrdiff_t)vb * n + ub - 8;
-  const bool wide = la > 8;
-  float buf[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const bool in_a = k < 8 || wide;
-    const bool live = in_a ? k < la : k < 8 + lb;
-    buf[k] = live ? __ldg((in_a ? pa : pb) + k) : 0.f;
-  }
-  float rw = 0.f, rx = 0.f, rq = 0.f;
-#pragma unroll
-  for (int k = 0; k < 8; ++k)
-    if (k < la) {
-      const float dx = (float)(ua + k), t = __fmul_rn(dx, buf[k]);
-      rw = __fadd_rn(rw, buf[k]);
-      rx = __fadd_rn(rx, t);
-      rq = __fmaf_rn(t, dx, rq);
-    }
-  float sw = 0.f, sx = 0.f, sq = 0.f;
-  if (wide) {
-    sw = rw, sx = rx, sq = rq;
-  }
-  const int ulo = wide ? ua : ub - 8, lim = wide ? la : 8 + lb;
-#pragma unroll
-  for (int k = 8; k < 16; ++k)
-    if (k < lim) {
-      const float dx = (float)(ulo + k), t = __fmul_rn(dx, buf[k]);
-      sw = __fadd_rn(sw, buf[k]);
-      sx = __fadd_rn(sx, t);
-      sq = __fmaf_rn(t, dx, sq);
-    }
-  if (wide) {
-    fold_chunk(c, sw, sx, sq, (float)va, (float)(va * va));
-    return;
-  }
-  if (la > 0) fold_chunk(c, rw, rx, rq, (float)va, (float)(va * va));
-  if (lb > 0) fold_chunk(c, sw, sx, sq, (float)vb, (float)(vb * vb));
-}
-
-// The next chunk of the buffered spans from row i (pixel u onwards, cont:
-// u is set): its row, start and length (at most 16, chunks start at da +
-// 16 k, as in the one-site-per-warp path); false when none is left.
-__device__ __forceinline__ bool next_chunk(const SpanBuf &b, int &i, int &u, bool &cont, int &v,
-                                           int &u0, int &len) {
-  for (; i < b.cnt; ++i) {
-    const int2 r = b.row[i];
-    const int da = (int)(int16_t)(r.y & 0xffff), db = (int)(int16_t)((unsigned)r.y >> 16);
-    if (da > db) continue;
-    v = r.x;
-    u0 = cont ? u : da;
-    len = min(db - u0 + 1, 16);
-    if (u0 + len - 1 < db) {
-      cont = true;
-      u = u0 + len;
-    } else {
-      cont = false;
-      ++i;
-    }
-    return true;
-  }
-  return false;
-}
-
-// Sum the buffered spans into c in walk order and empty the buffer: chunks
-// of at most 8 pixels go two to a batch, longer ones one.  Out of line: the
-// walk's registers are free while it runs.
-__device__ __noinline__ void sum_spans(const LevelBufs &a, int n, int sx, int sy, SpanBuf &b,
-                                          CellSums &c) {
-  const float *base = a.density + (size_t)sy * n + sx;
-  int i = 0, u = 0;
-  bool cont = false;
-  int va, ua, la;
-  bool have = next_chunk(b, i, u, cont, va, ua, la);
-  while (have) {
-    int vb = 0, ub = 0, lb = 0;
-    if (la <= 8) {
-      have = next_chunk(b, i, u, cont, vb, ub, lb);
-      if (have && lb > 8) {  // too long to share: X alone, Y starts the next batch
-        sum_batch(base, n, va, ua, la, 0, 0, 0, c);
-        va = vb, ua = ub, la = lb;
-        continue;
-      }
-      if (!have) lb = 0;
-      sum_batch(base, n, va, ua, la, vb, ub, lb, c);
-      if (have) have = next_chunk(b, i, u, cont, va, ua, la);
-    } else {
-      sum_batch(base, n, va, ua, la, 0, 0, 0, c);
-      have = next_chunk(b, i, u, cont, va, ua, la);
-    }
-  }
-  b.cnt = 0;
-}
-
-// Row v of the cell with bounds [lo, hi]: its span into the buffer (summed
-// when the buffer is full), R2.
+// Row v of the cell with bounds [lo, hi]: its span, R2, its sums.
 __device__ __forceinline__ void take_row(const LevelBufs &a, int n, int sx, int sy, int rb2, int v,
-                                         int lo, int hi, int &R2, SpanBuf &b, CellSums &c) {
+                                         int lo, int hi, int &R2, CellSums &c) {
   int da, db;
   if (!row_span(a, sx, sy, rb2, v, lo, hi, da, db)) return;
   R2 = max(R2, max(da * da, db * db) + v * v);
-  b.row[b.cnt++] = make_int2(v, (int)(((unsigned)da & 0xffffu) | ((unsigned)db << 16)));
-  if (b.cnt == kSpanRows) sum_spans(a, n, sx, sy, b, c);
+  row_sums(a.density + (size_t)(sy + v) * n + sx, da, db, v, c);
 }
 
 // A site in s's own column at row offset B != 0: s keeps the rows strictly on
@@ -460,8 +357,6 @@ __device__ CellSums cell_sums(const LevelBufs &a, const uint64_t *__restrict__ b
     // |K - S v| <= 2 W^2 + 2 W rb: below 2^23 the reciprocal estimate is safe
     const bool fast = 2 * W2 + 2 * (long long)W * rb < (1ll << 23);
     c = CellSums{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
-    SpanBuf sb;
-    sb.cnt = 0;
     int R2 = 0;
     // rows outward from s, two per pass over the records: up from v = 0, down
     // from v = -1, inside the row limits
@@ -472,21 +367,16 @@ __device__ CellSums cell_sums(const LevelBufs &a, const uint64_t *__restrict__ b
         const RowPair p =
             row_bounds2(rec, cnt, ovf, fast, bits, n, sx, sy, x0, x1, b0, b1, y0, y1, Wc, v, dir);
         if (p.lo0 > p.hi0 + 1) break;  // the cell has ended in this direction
-        if (p.lo0 <= p.hi0) take_row(a, n, sx, sy, rb2, v, p.lo0, p.hi0, R2, sb, c);
+        if (p.lo0 <= p.hi0) take_row(a, n, sx, sy, rb2, v, p.lo0, p.hi0, R2, c);
         const int v1 = v + dir;
         if ((dir > 0 ? v1 > vend : v1 < vend) || p.lo1 > p.hi1 + 1) break;
-        if (p.lo1 <= p.hi1) take_row(a, n, sx, sy, rb2, v1, p.lo1, p.hi1, R2, sb, c);
+        if (p.lo1 <= p.hi1) take_row(a, n, sx, sy, rb2, v1, p.lo1, p.hi1, R2, c);
       }
     }
     c.r2 = R2;
-    // the sums wait for the certificate (R2 <= rb^2, so a window of 2 rb
-    // always passes); a window that grows discards them
-    if (!(whole || 4 * (long long)R2 <= W2)) {
-      W = min(min(2 * isqrt_ceil(R2) + 1, 2 * W), 2 * rb);
-      continue;
-    }
-    sum_spans(a, n, sx, sy, sb, c);
-    return c;
+    // R2 <= rb^2, so a window of 2 rb always passes
+    if (whole || 4 * (long long)R2 <= W2) return c;
+    W = min(min(2 * isqrt_ceil(R2) + 1, 2 * W), 2 * rb);
   }
 }
 
