@@ -286,11 +286,23 @@ __device__ bool owns_nbrs(const Mesh &m, const unsigned *cl, int t, unsigned pr)
   return true;
 }
 
+// Triangle t changed: it and its neighbours are tested by the next flip
+// round.  An edge whose opposite vertices changed belongs to a changed
+// triangle, so it is tested from whichever of its triangles has the smaller
+// index (k_flip_mark).
+__device__ __forceinline__ void touch(const Mesh &m, uint8_t *act, int t) {
+  act[t] = 1;
+  for (int i = 0; i < 3; ++i) {
+    const int nb = m.nbr[3 * t + i];
+    if (nb >= 0) act[cdt::nb_tri(nb)] = 1;
+  }
+}
+
 // Insert the points that won every claim; the others stay pending (their
 // walk starts next round from the triangle they reached).
 __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *start,
                             const Loc *__restrict__ loc, const unsigned *cl, int *ntri, int cap,
-                            int *done, int *err) {
+                            int *done, uint8_t *act, int *err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   const int p = pend[q];
@@ -306,6 +318,9 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
       return;
     }
     cdt::split_in(m, L.t, p, s, s + 1);
+    touch(m, act, L.t);
+    touch(m, act, s);
+    touch(m, act, s + 1);
   } else if (L.kind == cdt::kLocEdge) {
     if (!owns_nbrs(m, cl, L.t, pr)) return;
     const int nb = m.nbr[3 * L.t + L.i];
@@ -317,6 +332,12 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
       return;
     }
     cdt::split_edge(m, L.t, L.i, p, s, s + 1);
+    touch(m, act, L.t);
+    touch(m, act, s);
+    if (nb >= 0) {
+      touch(m, act, cdt::nb_tri(nb));
+      touch(m, act, s + 1);
+    }
   } else {
     bool won = (L.before < 0 || owns(m, cl, L.before, pr)) && (L.after < 0 || owns(m, cl, L.after, pr));
     for (int k = 0; k < L.cnt && won; ++k) won = owns(m, cl, L.et[k], pr);
@@ -329,6 +350,7 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
     int slots[kChain];
     for (int k = 0; k < L.cnt; ++k) slots[k] = s + k;
     cdt::insert_out(m, L.et, L.ei, L.cnt, p, slots);
+    for (int k = 0; k < L.cnt; ++k) touch(m, act, slots[k]);
     start[q] = s;
   }
   done[q] = 1;
@@ -336,12 +358,18 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *s
 
 // ---- flips ---------------------------------------------------------------
 
-// Each triangle: the first of its edges towards a higher-numbered neighbour
-// that wants a flip; the flip claims both triangles and the four outer
-// neighbours with the priority of 3 t + i.
-__global__ void k_flip_mark(Mesh m, int T, int *cand, unsigned *cl, int *found) {
+// Each changed triangle (act) of the *ntri in the mesh: the first of its
+// edges towards a higher-numbered neighbour that wants a flip; the flip
+// claims both triangles and the four outer neighbours with the priority of
+// 3 t + i.  A triangle with none is settled until a change touches it again.
+__global__ void k_flip_mark(Mesh m, const int *ntri, int *cand, unsigned *cl, uint8_t *act,
+                            int *found) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
+  if (t >= *ntri) return;
+  if (!act[t]) {
+    cand[t] = 0;
+    return;
+  }
   int c = 0;
   for (int i = 0; i < 3; ++i) {
     const int nb = m.nbr[3 * t + i];
@@ -352,7 +380,10 @@ __global__ void k_flip_mark(Mesh m, int T, int *cand, unsigned *cl, int *found) 
     }
   }
   cand[t] = c;
-  if (!c) return;
+  if (!c) {
+    act[t] = 0;
+    return;
+  }
   atomicAdd(found, 1);
   const int i = c - 1;
   const unsigned pr = cdt::prio((unsigned)(3 * t + i));
@@ -361,14 +392,17 @@ __global__ void k_flip_mark(Mesh m, int T, int *cand, unsigned *cl, int *found) 
   claim_nbrs(m, cl, t2, pr);
 }
 
-__global__ void k_flip_apply(Mesh m, int T, const int *cand, const unsigned *cl, int *flips) {
+__global__ void k_flip_apply(Mesh m, const int *ntri, const int *cand, const unsigned *cl,
+                             uint8_t *act, int *flips) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T || !cand[t]) return;
+  if (t >= *ntri || !cand[t]) return;
   const int i = cand[t] - 1;
   const unsigned pr = cdt::prio((unsigned)(3 * t + i));
   const int t2 = cdt::nb_tri(m.nbr[3 * t + i]);
   if (!owns_nbrs(m, cl, t, pr) || !owns_nbrs(m, cl, t2, pr)) return;
   cdt::flip(m, t, i);
+  touch(m, act, t);
+  touch(m, act, t2);
   atomicAdd(flips, 1);
 }
 
@@ -601,10 +635,11 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
   int *vt = sc.take<int>((size_t)V);
   unsigned *cl = sc.take<unsigned>((size_t)cap_t);
   int *cand = sc.take<int>((size_t)cap_t);
+  uint8_t *act = sc.take<uint8_t>((size_t)cap_t);
   // [0] error bits, [1] triangles, [2] flips wanted, [3] flips made, [4] points
   // pending, [5] segments pending
   int *ctr = sc.take<int>(8);
-  if (!sxy || !X || !Y || !R || !tri || !nbr || !cons || !vt || !cl || !cand || !ctr)
+  if (!sxy || !X || !Y || !R || !tri || !nbr || !cons || !vt || !cl || !cand || !act || !ctr)
     return GCVT_ERR_ALLOC;
   CCK(launch_extract(bits, fixed, n, colcnt, 1.0, 0.0, 0.0, sxy, F, colcnt + n, s));
   CCK(cudaMemsetAsync(ctr, 0, 8 * sizeof(int), s));
@@ -626,6 +661,7 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     if (!hk || !hv) return GCVT_ERR_ALLOC;
     CCK(cudaMemsetAsync(hk, 0xff, (size_t)hsize * sizeof(unsigned long long), s));
     CCK(cudaMemsetAsync(vt, 0, (size_t)V * sizeof(int), s));  // a vertex in no triangle: 0
+    CCK(cudaMemsetAsync(act, 0, (size_t)cap_t, s));           // the sites' triangulation is Delaunay
     k_edge_insert<<<nblk(3ll * T0, 256), 256, 0, s>>>(tri, (int)T0, hk, hv, hsize - 1, ctr);
     k_edge_link<<<nblk(3ll * T0, 256), 256, 0, s>>>(tri, (int)T0, hk, hv, hsize - 1, nbr, vt,
                                                     ctr);
@@ -639,18 +675,24 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     CCK(cudaStreamSynchronize(s));
     return GCVT_OK;
   };
-  // Delaunay flip rounds until none is left, read back every kFlipPoll
-  // rounds (a round that finds nothing to flip changes nothing)
+  // kFlipPoll Delaunay flip rounds over the changed triangles (their count
+  // read on the device: insertions of the same batch add triangles)
+  auto flip_rounds = [&]() -> int {
+    for (int i = 0; i < kFlipPoll; ++i) {
+      CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
+      CCK(cudaMemsetAsync(ctr + 2, 0, 2 * sizeof(int), s));
+      k_flip_mark<<<nblk(cap_t, 256), 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 2);
+      k_flip_apply<<<nblk(cap_t, 256), 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 3);
+    }
+    CCK(cudaGetLastError());
+    return GCVT_OK;
+  };
+  // flip rounds over every triangle until none is left, read back every
+  // kFlipPoll rounds (a round that finds nothing to flip changes nothing)
   auto flips = [&]() -> int {
+    CCK(cudaMemsetAsync(act, 1, (size_t)cap_t, s));
     for (int r = 0; r < kFlipRounds; r += kFlipPoll) {
-      for (int i = 0; i < kFlipPoll; ++i) {
-        CCK(cudaMemsetAsync(cl, 0xff, (size_t)T * sizeof(unsigned), s));
-        CCK(cudaMemsetAsync(ctr + 2, 0, 2 * sizeof(int), s));
-        k_flip_mark<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 2);
-        k_flip_apply<<<nblk(T, 256), 256, 0, s>>>(m, T, cand, cl, ctr + 3);
-      }
-      CCK(cudaGetLastError());
-      if ((rc = pull())) return rc;
+      if ((rc = flip_rounds()) || (rc = pull())) return rc;
       if (h[0] || h[2] == 0) return GCVT_OK;
     }
     h[0] |= kErrWalk;
@@ -675,17 +717,17 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
         CCK(cudaMemsetAsync(done, 0, (size_t)np * sizeof(int), s));
         k_ins_locate<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr);
         k_ins_apply<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr + 1, cap_t,
-                                                  done, ctr);
+                                                  done, act, ctr);
         k_compact<<<1, 1024, 0, s>>>(pend, start, done, np, pend2, start2, ctr + 4);
         CCK(cudaGetLastError());
-        if ((rc = pull())) return rc;
+        // a few flip rounds around the new points keep the mesh near Delaunay
+        // for the next walks; the final flips finish the job
+        if ((rc = flip_rounds()) || (rc = pull())) return rc;
         if (h[0]) break;
         np = h[4];
         std::swap(pend, pend2);
         std::swap(start, start2);
         T = h[1];
-        if ((rc = flips())) return rc;
-        if (h[0]) break;
       }
       if (!h[0] && np > 0) h[0] |= kErrWalk;
     }
