@@ -46,7 +46,10 @@ def mesh_case(gcvt_lib, nv, n, m, iters, seed=2):
 
 
 @pytest.mark.parametrize("nv,n,m,iters", [(24, 256, 500, 10), (64, 512, 3000, 20),
-                                          (128, 1024, 12000, 30)])
+                                          (128, 1024, 12000, 30),
+                                          # the mesh workload's size: a 256^2-vertex disk
+                                          # mesh on a 2048^2 grid, 65,536 sites
+                                          (256, 2048, 65536, 100)])
 def test_mesh_boundary_cdt_is_constrained_delaunay(gcvt_lib, cuda_device, nv, n, m, iters):
     ctx, cpts, be, bv, scale, left, lower = mesh_case(gcvt_lib, nv, n, m, iters)
     pts, R, F = exact_points(ctx, n, cpts, scale, left, lower)
