@@ -189,10 +189,10 @@ __device__ __forceinline__ void claim_nbrs(const Mesh &m, unsigned *cl, int t, u
 }
 
 // Locate every pending point and claim what its insertion changes.
-__global__ void k_ins_locate(Mesh m, const int *__restrict__ pend, int np, int *start, Loc *loc,
-                             unsigned *cl, int *err) {
+__global__ void k_ins_locate(Mesh m, const int *__restrict__ pend, const int *npp, int *start,
+                             Loc *loc, unsigned *cl, int *err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= np) return;
+  if (q >= *npp) return;
   const int p = pend[q];
   const unsigned pr = cdt::prio((unsigned)p);
   Loc L;
@@ -300,11 +300,11 @@ __device__ __forceinline__ void touch(const Mesh &m, uint8_t *act, int t) {
 
 // Insert the points that won every claim; the others stay pending (their
 // walk starts next round from the triangle they reached).
-__global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, int np, int *start,
+__global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, const int *npp, int *start,
                             const Loc *__restrict__ loc, const unsigned *cl, int *ntri, int cap,
                             int *done, uint8_t *act, int *err) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= np) return;
+  if (q >= *npp) return;
   const int p = pend[q];
   const unsigned pr = cdt::prio((unsigned)p);
   const Loc &L = loc[q];
@@ -543,18 +543,25 @@ __global__ void k_ins_start(const i64 *__restrict__ X, const i64 *__restrict__ Y
   if (j >= C) return;
   const int px = (int)(X[F + j] >> 15), py = (int)(Y[F + j] >> 15);
   int found = -1;
-  for (int r = 0; r < 64 && found < 0; ++r)
-    for (int dy = -r; dy <= r && found < 0; ++dy)
-      for (int dx = -r; dx <= r; ++dx) {
-        if (max(abs(dx), abs(dy)) != r) continue;
-        const int x = px + dx, y = py + dy;
-        if (x < 0 || y < 0 || x >= n || y >= n) continue;
-        const int v = site_at[(size_t)y * n + x];
-        if (v >= 0) {
-          found = v;
-          break;
-        }
+  for (int r = 0; r < 64 && found < 0; ++r) {
+    // the ring at Chebyshev distance r: its 8 r cells (1 for r = 0), side by side
+    const int cells = r ? 8 * r : 1;
+    for (int k = 0; k < cells; ++k) {
+      int dx, dy;
+      if (r == 0) dx = dy = 0;
+      else if (k < 2 * r) dx = -r + k, dy = -r;          // top, left to right
+      else if (k < 4 * r) dx = r, dy = -r + (k - 2 * r);  // right, top to bottom
+      else if (k < 6 * r) dx = r - (k - 4 * r), dy = r;   // bottom, right to left
+      else dx = -r, dy = r - (k - 6 * r);                 // left, bottom to top
+      const int x = px + dx, y = py + dy;
+      if (x < 0 || y < 0 || x >= n || y >= n) continue;
+      const int v = site_at[(size_t)y * n + x];
+      if (v >= 0) {
+        found = v;
+        break;
       }
+    }
+  }
   start[j] = found >= 0 ? vt[found] : 0;
 }
 
@@ -572,9 +579,10 @@ __global__ void k_iota(int *a, int count, int base) {
 
 // Drop the inserted points from the pending list (order kept).
 __global__ void k_compact(const int *__restrict__ pend, const int *__restrict__ start,
-                          const int *__restrict__ done, int np, int *pend2, int *start2,
+                          const int *__restrict__ done, const int *npp, int *pend2, int *start2,
                           int *count) {
   if (blockIdx.x != 0) return;
+  const int np = *npp;
   // one block: a running offset over chunks of blockDim.x
   __shared__ int base;
   __shared__ int wsum[32];
@@ -636,8 +644,8 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
   unsigned *cl = sc.take<unsigned>((size_t)cap_t);
   int *cand = sc.take<int>((size_t)cap_t);
   uint8_t *act = sc.take<uint8_t>((size_t)cap_t);
-  // [0] error bits, [1] triangles, [2] flips wanted, [3] flips made, [4] points
-  // pending, [5] segments pending
+  // [0] error bits, [1] triangles, [2] flips wanted, [3] flips made, [4] and
+  // [6] points pending (the two lists), [5] segments pending
   int *ctr = sc.take<int>(8);
   if (!sxy || !X || !Y || !R || !tri || !nbr || !cons || !vt || !cl || !cand || !act || !ctr)
     return GCVT_ERR_ALLOC;
@@ -710,27 +718,53 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     k_ins_start<<<nblk(C, 128), 128, 0, s>>>(X, Y, (int)F, C, site_at, n, vt, start);
     k_iota<<<nblk(C, 256), 256, 0, s>>>(pend, C, (int)F);  // point indices F + j
     CCK(cudaGetLastError());
-    {
-      int np = C;
-      for (int r = 0; r < kInsertRounds && np > 0; ++r) {
-        CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
-        CCK(cudaMemsetAsync(done, 0, (size_t)np * sizeof(int), s));
-        k_ins_locate<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr);
-        k_ins_apply<<<nblk(np, 128), 128, 0, s>>>(m, pend, np, start, loc, cl, ctr + 1, cap_t,
-                                                  done, act, ctr);
-        k_compact<<<1, 1024, 0, s>>>(pend, start, done, np, pend2, start2, ctr + 4);
-        CCK(cudaGetLastError());
-        // a few flip rounds around the new points keep the mesh near Delaunay
-        // for the next walks; the final flips finish the job
-        if ((rc = flip_rounds()) || (rc = pull())) return rc;
-        if (h[0]) break;
-        np = h[4];
-        std::swap(pend, pend2);
-        std::swap(start, start2);
-        T = h[1];
+    // one round: the points of list a (count *na) locate, claim and insert;
+    // those left go to list b (count *nb); then kFlipPoll flip rounds.  Every
+    // count is read on the device, so rounds queue without the host.
+    auto ins_round = [&](int *pa, int *sa, int *pb, int *sb, int *na, int *nb) -> int {
+      CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
+      CCK(cudaMemsetAsync(done, 0, (size_t)C * sizeof(int), s));
+      k_ins_locate<<<nblk(C, 128), 128, 0, s>>>(m, pa, na, sa, loc, cl, ctr);
+      k_ins_apply<<<nblk(C, 128), 128, 0, s>>>(m, pa, na, sa, loc, cl, ctr + 1, cap_t, done, act,
+                                               ctr);
+      k_compact<<<1, 1024, 0, s>>>(pa, sa, done, na, pb, sb, nb);
+      CCK(cudaGetLastError());
+      return flip_rounds();
+    };
+    // two rounds (list 1 -> 2 -> 1) per read-back, as one CUDA graph where the
+    // stream can be captured
+    auto ins_pair = [&]() -> int {
+      if ((rc = ins_round(pend, start, pend2, start2, ctr + 4, ctr + 6))) return rc;
+      return ins_round(pend2, start2, pend, start, ctr + 6, ctr + 4);
+    };
+    cudaGraphExec_t pair_exec = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int le = ins_pair();
+      cudaGraph_t g = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      const cudaError_t ie =
+          (le == GCVT_OK && ce == cudaSuccess) ? cudaGraphInstantiate(&pair_exec, g, 0) : ce;
+      if (g) cudaGraphDestroy(g);
+      if (le != GCVT_OK || ce != cudaSuccess || ie != cudaSuccess) {
+        if (pair_exec) cudaGraphExecDestroy(pair_exec);
+        return GCVT_ERR_CUDA;
       }
-      if (!h[0] && np > 0) h[0] |= kErrWalk;
+    } else {
+      cudaGetLastError();  // the legacy default stream: plain launches
     }
+    CCK(cudaMemcpyAsync(ctr + 4, &C, sizeof(int), cudaMemcpyHostToDevice, s));
+    int np = C;
+    for (int r = 0; r < kInsertRounds / 2 && np > 0; ++r) {
+      rc = pair_exec ? (cudaGraphLaunch(pair_exec, s) == cudaSuccess ? GCVT_OK : GCVT_ERR_CUDA)
+                     : ins_pair();
+      if (rc == GCVT_OK) rc = pull();
+      if (rc != GCVT_OK) break;
+      if (h[0]) break;
+      np = h[4];
+    }
+    if (pair_exec) cudaGraphExecDestroy(pair_exec);
+    if (rc != GCVT_OK) return rc;
+    if (!h[0] && np > 0) h[0] |= kErrWalk;
   }
   if ((rc = pull())) return rc;
   T = h[1];
