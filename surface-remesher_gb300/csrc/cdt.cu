@@ -10,9 +10,11 @@
 //   3. the constraint points inserted in rounds: every point locates itself
 //      by a walk, claims the triangles its split changes (atomicMin of a
 //      priority, a fixed bijective hash of its index: claims by plain index
-//      let only the first of a run of neighbours win each round), and the points that won all their claims split (1 -> 3 inside
-//      a triangle, 2 -> 4 on an edge, a fan over the visible hull edges
-//      outside the hull); after each round, Delaunay flip rounds;
+//      let only the first of a run of neighbours win each round), and the
+//      points that won all their claims split (1 -> 3 inside a triangle,
+//      2 -> 4 on an edge, a fan over the visible hull edges outside the
+//      hull); after each round, four flip rounds over the changed triangles
+//      (two rounds with their flips make one CUDA graph and one read-back);
 //   4. each segment made an edge by flipping the edges that cross it
 //      (Sloan's method, cdt_core.cuh recover_segment) and marked: segments
 //      already edges at once, the others in rounds where each claims the
@@ -25,12 +27,12 @@
 //   6. the triangles written in a fixed order (by their smallest vertex, then
 //      the next one), so the output does not depend on scheduling.
 //
-// A flip round: every triangle tests its edges towards higher-numbered
-// neighbours (cdt_core.cuh wants_flip); a flip claims its two triangles and
-// their four outer neighbours (whose back links it rewrites); the flips that
-// won all six claims are applied.  Lawson's flips end (each one lowers the
-// lifted surface), so the rounds end; a round limit turns a runaway into an
-// error instead of a hang.
+// A flip round: every changed triangle tests its edges towards
+// higher-numbered neighbours (cdt_core.cuh wants_flip); a flip claims its two
+// triangles and their four outer neighbours (whose back links it rewrites);
+// the flips that won all six claims are applied.  Lawson's flips end (each
+// one lowers the lifted surface), so the rounds end; a round limit turns a
+// runaway into an error instead of a hang.
 //
 // Coordinates: sites (x, y) on the pixel lattice scaled by 2^15; a
 // constraint point (px, py) maps to ((px - left) / scale, (py - lower) /
@@ -43,7 +45,6 @@
 #include "cdt_core.cuh"
 #include "../../include/gcvt_gb300.h"
 
-#include <climits>
 #include <cmath>
 #include <utility>
 
