@@ -391,6 +391,16 @@ __device__ __forceinline__ float cell_centroid(int base, float Sh, float Sl, flo
   return __fadd_rn(s, __fadd_rn(e, q2));
 }
 
+// Add one to *counter after every earlier write of this thread is visible
+// (an atomic with release semantics): the writer's half of a counter
+// handoff, where whoever brings the counter to its target fences and reads
+// the others' results.  Cheaper than a full fence before a plain atomic.
+__device__ __forceinline__ unsigned add_release(unsigned *counter) {
+  unsigned prev;
+  asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(prev) : "l"(counter) : "memory");
+  return prev;
+}
+
 __device__ __forceinline__ uint64_t *bits_at(const LevelBufs &a, int k) {
   return k == 0 ? a.bits[0] : (k == 1 ? a.bits[1] : a.bits[2]);
 }
@@ -590,8 +600,7 @@ __device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v
   const unsigned starget = min((unsigned)kGroupsPerSlot, v.ngroups - sbase);
   if (lane == 0) {
     a.gslot[g] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
-    __threadfence();
-    last = atomicAdd(a.scnt + sg, 1u) == starget - 1;
+    last = add_release(a.scnt + sg) == starget - 1;
   }
   if (!__shfl_sync(0xffffffffu, last, 0)) return;
   __threadfence();
@@ -609,8 +618,7 @@ __device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v
   if (lane == 0) {
     a.sslot[sg] = make_float4(eh, el, __uint_as_float(r2), __uint_as_float(mv));
     a.scnt[sg] = 0u;
-    __threadfence();
-    last = atomicAdd(&st->done_blocks, 1u) == nslots - 1;
+    last = add_release(&st->done_blocks) == nslots - 1;
   }
   if (!__shfl_sync(0xffffffffu, last, 0)) return;
   __threadfence();
@@ -878,9 +886,8 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
       }
       const unsigned mv = move_site(a, v, e, sx, sy, cs);
       a.sitev[idx] = make_float4(eh, el, __uint_as_float((unsigned)cs.r2), __uint_as_float(mv));
-      __threadfence();
       const unsigned gsize = min(32u, (unsigned)v.nsites - g * 32);
-      last = atomicAdd(a.gcnt + g, 1u) == gsize - 1;
+      last = add_release(a.gcnt + g) == gsize - 1;
     }
     if (!__shfl_sync(0xffffffffu, last, 0)) continue;
     // the group's last site: its values in lane order, then the usual tail
