@@ -15,7 +15,7 @@
 // sites S also writes their features, the MLP predicts, k_apply places the
 // jumped sites L, and the iteration of L decides: L stands if E(L) < E(S),
 // otherwise the plain step's sites are current again -- the plain method is
-// the fallback and the judge.
+// both the fallback and the test a jump must pass.
 #include "gcvt_internal.cuh"
 
 #include <cuda_bf16.h>
