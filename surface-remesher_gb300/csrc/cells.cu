@@ -555,9 +555,14 @@ __device__ __forceinline__ void site_features(const LevelBufs &a, const IterView
 // and zero-density targets stay.  The site goes into the next bitmap (the
 // first to set a bit counts it for the next list), leaves its window hint and
 // (learned steps) its move history and id at its new pixel.  Returns the
-// move's squared length.
+// move's squared length.  With centry, the count is left to the caller: the
+// list block to count in goes to *centry (-1: the bit was set already), so
+// that a warp adds its group's sites with one atomic per list block instead
+// of one per site (many sites land in one list block, and same-address
+// atomics serialise).
 __device__ __forceinline__ unsigned move_site(const LevelBufs &a, const IterView &v, uint32_t e,
-                                              int sx, int sy, const CellSums &cs) {
+                                              int sx, int sy, const CellSums &cs,
+                                              int *centry = nullptr) {
   const int n = a.n;
   const size_t pid = (size_t)sy * n + sx;
   const float cx = cell_centroid(sx, cs.xh, cs.xl, cs.wh, cs.wl);
@@ -572,7 +577,9 @@ __device__ __forceinline__ unsigned move_site(const LevelBufs &a, const IterView
   const unsigned long long bit = 1ull << (ny % kBand);
   const unsigned long long old =
       atomicOr(reinterpret_cast<unsigned long long *>(v.nxt + widx), bit);
-  if (!(old & bit)) atomicAdd(v.cnt_nxt + widx / kListWords, 1u);
+  const int entry = (old & bit) ? -1 : (int)(widx / kListWords);
+  if (centry) *centry = entry;
+  else if (entry >= 0) atomicAdd(v.cnt_nxt + entry, 1u);
   const size_t npid = (size_t)ny * n + nx;
   a.hint[npid] = (uint8_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
   if (a.hist[0]) {  // this move becomes the newest of the site's last four
@@ -643,12 +650,25 @@ __device__ __forceinline__ void group_tail(const LevelBufs &a, const IterView &v
 // planes).  MODE 2: the learned step's features of the sites (nothing
 // moves).  MODE 4: MODE 0 and the features, with each site's window in
 // jaux.  MODE 5: MODE 0 for the jumped sites (the pass then judges the jump).
+// The next work item of a persistent warp: its first is its block index (no
+// atomic), the rest come from the ticket, numbered after that first wave (a
+// ticket every warp takes at once is a burst of same-address atomics).
+__device__ __forceinline__ unsigned next_item(unsigned *ticket, bool first, int lane) {
+  unsigned g = blockIdx.x;
+  if (!first) {
+    if (lane == 0) g = gridDim.x + atomicAdd(ticket, 1u);
+    g = __shfl_sync(0xffffffffu, g, 0);
+  }
+  return g;
+}
+
 template <int MODE>
 __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, int lane,
                            double *out4) {
   const int n = a.n;
   float eh = 0.f, el = 0.f;
   unsigned r2 = 0, mv = 0;
+  int centry = -1;
   const int idx = (int)g * 32 + lane;
   if (idx < v.nsites) {
     const uint32_t e = a.list[idx];
@@ -668,10 +688,16 @@ __device__ void cell_group(const LevelBufs &a, const IterView &v, unsigned g, in
       r2 = (unsigned)cs.r2;
       if (MODE == 2 || MODE == 4) site_features(a, v, idx, sx, sy, cs);
       if (MODE == 4) a.jaux[idx] = (uint32_t)min(2 * isqrt_ceil(cs.r2) + v.slack, 255);
-      if (MODE != 2) mv = move_site(a, v, e, sx, sy, cs);
+      if (MODE != 2) mv = move_site(a, v, e, sx, sy, cs, &centry);
     }
   }
   __syncwarp();
+  // the group's new sites, counted per list block: one atomic per block
+  const unsigned want = __ballot_sync(0xffffffffu, centry >= 0);
+  if (centry >= 0) {
+    const unsigned peers = __match_any_sync(want, centry);
+    if (lane == __ffs(peers) - 1) atomicAdd(v.cnt_nxt + centry, (unsigned)__popc(peers));
+  }
   if (MODE == 1) return;
   group_tail<MODE>(a, v, g, lane, eh, el, r2, mv);
 }
@@ -857,19 +883,15 @@ __global__ void __launch_bounds__(32, 32) k_cell_warp(LevelBufs a) {
     return;
   }
   if (v.nsites > kWarpSites) {  // more sites than LevelBufs::sitev holds: per lane
-    for (;;) {
-      unsigned g = 0;
-      if (lane == 0) g = atomicAdd(&st->ticket, 1u);
-      g = __shfl_sync(0xffffffffu, g, 0);
+    for (bool first = true;; first = false) {
+      const unsigned g = next_item(&st->ticket, first, lane);
       if (g >= v.ngroups) return;
       cell_group<MODE>(a, v, g, lane, nullptr);
     }
   }
   const int n = a.n;
-  for (;;) {
-    unsigned idx = 0;
-    if (lane == 0) idx = atomicAdd(&st->ticket, 1u);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
+  for (bool first = true;; first = false) {
+    const unsigned idx = next_item(&st->ticket, first, lane);
     if (idx >= (unsigned)v.nsites) break;
     const uint32_t e = a.list[idx];
     const int sx = (int)(e & 0x7fffu), sy = (int)(e >> 16);
@@ -927,10 +949,8 @@ __global__ void __launch_bounds__(32, 32) k_cell(LevelBufs a, double *out4) {
     if (blockIdx.x == 0 && lane == 0) pass_done<MODE>(st, 0.0, 0u, 0u, a.n, v.cur);
     return;
   }
-  for (;;) {
-    unsigned g = 0;
-    if (lane == 0) g = atomicAdd(&st->ticket, 1u);
-    g = __shfl_sync(0xffffffffu, g, 0);
+  for (bool first = true;; first = false) {
+    const unsigned g = next_item(&st->ticket, first, lane);
     if (g >= v.ngroups) break;
     cell_group<MODE>(a, v, g, lane, out4);
   }
@@ -958,10 +978,8 @@ __global__ void __launch_bounds__(32, 32) k_cell_batch(const LevelBufs *__restri
       pass_done<MODE>(st, 0.0, 0u, 0u, a.n, cur);
   }
   const unsigned total = gofs[nchart];
-  for (;;) {
-    unsigned g = 0;
-    if (lane == 0) g = atomicAdd(ticket, 1u);
-    g = __shfl_sync(0xffffffffu, g, 0);
+  for (bool first = true;; first = false) {
+    const unsigned g = next_item(ticket, first, lane);
     if (g >= total) break;
     int lo = 0, hi = nchart - 1;  // the chart c with gofs[c] <= g < gofs[c + 1]
     while (lo < hi) {

@@ -19,7 +19,7 @@ constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 fo
                                     // every entry of gcvt.cu:842-847
 constexpr int kRowsPerBlock = 1;    // rows (one warp each) per row-pass block
 constexpr int kWarpSites = 8192;    // one site per warp up to this many sites
-constexpr int kListWords = 2048;   // bitmap words per site-list block
+constexpr int kListWords = 512;    // bitmap words per site-list block
 constexpr int kMinN = 256;   // n must be a multiple of 256 (S = n/32 >= 8)
 constexpr int kMaxN = 8192;  // row-pass shared memory: 4 rows x 32 KB at 8192
 

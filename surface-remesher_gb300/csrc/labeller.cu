@@ -60,7 +60,11 @@ __global__ void k_grid_to_bits(const uint32_t *__restrict__ grid, int n,
   }
   bits[(size_t)b * n + x] = w;
   if (bad) atomicOr(err, 1);
-  if (count && w) atomicAdd(count, __popcll(w));
+  if (count) {  // one atomic per warp: every thread adding to one counter serialises
+    const unsigned m = __activemask();
+    const unsigned c = __reduce_add_sync(m, (unsigned)__popcll(w));
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1 && c) atomicAdd(count, (int)c);
+  }
 }
 
 __global__ void k_bits_to_grid(const uint64_t *__restrict__ bits, int n,

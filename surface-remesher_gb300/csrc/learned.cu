@@ -136,7 +136,13 @@ __global__ void __launch_bounds__(256) k_apply(const LevelBufs *__restrict__ des
     const size_t widx = (size_t)(ny / kBand) * n + nx;
     const unsigned long long bit = 1ull << (ny % kBand);
     const unsigned long long was = atomicOr(reinterpret_cast<unsigned long long *>(dst + widx), bit);
-    if (!(was & bit)) atomicAdd(cdst + widx / kListWords, 1u);
+    // counted per list block, one atomic per block a warp's sites reached
+    const int entry = (was & bit) ? -1 : (int)(widx / kListWords);
+    const unsigned want = __ballot_sync(__activemask(), entry >= 0);
+    if (entry >= 0) {
+      const unsigned peers = __match_any_sync(want, entry);
+      if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(cdst + entry, (unsigned)__popc(peers));
+    }
     const size_t pid = (size_t)sy * n + sx, npid = (size_t)ny * n + nx;
     a.hist[lj][npid] = a.hist[cur][pid];
     if (a.ids[0]) a.ids[lj][npid] = a.ids[cur][pid];
