@@ -74,8 +74,8 @@ ALG_BYTES_PER_SITE = 24.0
 # dram__bytes_read.sum + dram__bytes_write.sum of k_list + k_cell<0> for one
 # iteration of this workload (iteration 31 of a graph-replayed run, warm L2),
 # from the ncu capture summarised in profiles/cell_kernel_plain_4096.md:
-# k_list 1,282,304 + 431,872, k_cell 22,419,712 + 7,846,912 bytes.
-NCU_TRAFFIC_BYTES = 31980800
+# k_list 789,248 + 264,448, k_cell 13,910,784 + 6,594,304 bytes.
+NCU_TRAFFIC_BYTES = 21558784
 # the same capture on the 8192^2 / 1,048,576-site workload (iteration 31,
 # profiles/cell_kernel_plain_8192.md): k_list 13,138,176 + 3,403,520, k_cell
 # 265,760,256 + 77,200,896 bytes
