@@ -13,7 +13,7 @@
 //      let only the first of a run of neighbours win each round), and the
 //      points that won all their claims split (1 -> 3 inside a triangle,
 //      2 -> 4 on an edge, a fan over the visible hull edges outside the
-//      hull); after each round, four flip rounds over the changed triangles
+//      hull); after each round, two flip rounds over the changed triangles
 //      (two rounds with their flips make one CUDA graph and one read-back);
 //   4. each segment made an edge by flipping the edges that cross it
 //      (Sloan's method, cdt_core.cuh recover_segment) and marked: segments
@@ -60,6 +60,8 @@ constexpr int kRotate = 4096;     // triangles around one vertex
 constexpr int kChain = 64;        // visible hull edges from one outside point
 constexpr int kFlipRounds = 1 << 16;
 constexpr int kFlipPoll = 4;      // flip rounds between read-backs
+constexpr int kInterimFlips = 2;  // flip rounds after each insertion round
+constexpr int kFlipBlocks = 304;  // grid of the grid-stride flip kernels (2 per SM)
 constexpr int kInsertRounds = 1 << 12;
 constexpr int kSegQueue = 4096;   // crossing edges of one segment
 constexpr int kSegStack = 256;    // pieces of one segment split by vertices inside it
@@ -363,10 +365,8 @@ __global__ void k_ins_apply(Mesh m, const int *__restrict__ pend, const int *npp
 // edges towards a higher-numbered neighbour that wants a flip; the flip
 // claims both triangles and the four outer neighbours with the priority of
 // 3 t + i.  A triangle with none is settled until a change touches it again.
-__global__ void k_flip_mark(Mesh m, const int *ntri, int *cand, unsigned *cl, uint8_t *act,
-                            int *found) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= *ntri) return;
+__device__ __forceinline__ void flip_mark_one(const Mesh &m, int t, int *cand, unsigned *cl,
+                                              uint8_t *act, int *found) {
   if (!act[t]) {
     cand[t] = 0;
     return;
@@ -393,18 +393,28 @@ __global__ void k_flip_mark(Mesh m, const int *ntri, int *cand, unsigned *cl, ui
   claim_nbrs(m, cl, t2, pr);
 }
 
+// (grid-stride: a round with few changed triangles costs few blocks)
+__global__ void k_flip_mark(Mesh m, const int *ntri, int *cand, unsigned *cl, uint8_t *act,
+                            int *found) {
+  const int T = *ntri;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x)
+    flip_mark_one(m, t, cand, cl, act, found);
+}
+
 __global__ void k_flip_apply(Mesh m, const int *ntri, const int *cand, const unsigned *cl,
                              uint8_t *act, int *flips) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= *ntri || !cand[t]) return;
-  const int i = cand[t] - 1;
-  const unsigned pr = cdt::prio((unsigned)(3 * t + i));
-  const int t2 = cdt::nb_tri(m.nbr[3 * t + i]);
-  if (!owns_nbrs(m, cl, t, pr) || !owns_nbrs(m, cl, t2, pr)) return;
-  cdt::flip(m, t, i);
-  touch(m, act, t);
-  touch(m, act, t2);
-  atomicAdd(flips, 1);
+  const int T = *ntri;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+    if (!cand[t]) continue;
+    const int i = cand[t] - 1;
+    const unsigned pr = cdt::prio((unsigned)(3 * t + i));
+    const int t2 = cdt::nb_tri(m.nbr[3 * t + i]);
+    if (!owns_nbrs(m, cl, t, pr) || !owns_nbrs(m, cl, t2, pr)) continue;
+    cdt::flip(m, t, i);
+    touch(m, act, t);
+    touch(m, act, t2);
+    atomicAdd(flips, 1);
+  }
 }
 
 // ---- segments --------------------------------------------------------------
@@ -684,14 +694,15 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     CCK(cudaStreamSynchronize(s));
     return GCVT_OK;
   };
-  // kFlipPoll Delaunay flip rounds over the changed triangles (their count
-  // read on the device: insertions of the same batch add triangles)
-  auto flip_rounds = [&]() -> int {
-    for (int i = 0; i < kFlipPoll; ++i) {
+  // Delaunay flip rounds over the changed triangles (their count read on the
+  // device: insertions of the same batch add triangles)
+  const int fgrid = nblk(cap_t, 256) < kFlipBlocks ? nblk(cap_t, 256) : kFlipBlocks;
+  auto flip_rounds = [&](int rounds) -> int {
+    for (int i = 0; i < rounds; ++i) {
       CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
       CCK(cudaMemsetAsync(ctr + 2, 0, 2 * sizeof(int), s));
-      k_flip_mark<<<nblk(cap_t, 256), 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 2);
-      k_flip_apply<<<nblk(cap_t, 256), 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 3);
+      k_flip_mark<<<fgrid, 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 2);
+      k_flip_apply<<<fgrid, 256, 0, s>>>(m, ctr + 1, cand, cl, act, ctr + 3);
     }
     CCK(cudaGetLastError());
     return GCVT_OK;
@@ -701,7 +712,7 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
   auto flips = [&]() -> int {
     CCK(cudaMemsetAsync(act, 1, (size_t)cap_t, s));
     for (int r = 0; r < kFlipRounds; r += kFlipPoll) {
-      if ((rc = flip_rounds()) || (rc = pull())) return rc;
+      if ((rc = flip_rounds(kFlipPoll)) || (rc = pull())) return rc;
       if (h[0] || h[2] == 0) return GCVT_OK;
     }
     h[0] |= kErrWalk;
@@ -720,7 +731,7 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
     k_iota<<<nblk(C, 256), 256, 0, s>>>(pend, C, (int)F);  // point indices F + j
     CCK(cudaGetLastError());
     // one round: the points of list a (count *na) locate, claim and insert;
-    // those left go to list b (count *nb); then kFlipPoll flip rounds.  Every
+    // those left go to list b (count *nb); then kInterimFlips flip rounds.  Every
     // count is read on the device, so rounds queue without the host.
     auto ins_round = [&](int *pa, int *sa, int *pb, int *sb, int *na, int *nb) -> int {
       CCK(cudaMemsetAsync(cl, 0xff, (size_t)cap_t * sizeof(unsigned), s));
@@ -730,7 +741,7 @@ int cdt_compute(const uint64_t *bits, const uint64_t *fixed, int n, unsigned *co
                                                ctr);
       k_compact<<<1, 1024, 0, s>>>(pa, sa, done, na, pb, sb, nb);
       CCK(cudaGetLastError());
-      return flip_rounds();
+      return flip_rounds(kInterimFlips);
     };
     // two rounds (list 1 -> 2 -> 1) per read-back, as one CUDA graph where the
     // stream can be captured
