@@ -1200,8 +1200,16 @@ __global__ void __launch_bounds__(256) k_cover(LevelBufs a) {
       }
     }
   }
+  // the block's maximum, then one atomic per block (one per warp onto the
+  // single accumulator serialised at the L2)
+  __shared__ unsigned wmax[8];
   m = __reduce_max_sync(0xffffffffu, m);
-  if (lane == 0 && m) atomicMax(&a.st->cover_acc, m);
+  if (lane == 0) wmax[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, wmax[w]);
+    if (m) atomicMax(&a.st->cover_acc, m);
+  }
 }
 __global__ void k_cover_finish(LevelBufs a) {
   DevState *st = a.st;

@@ -150,8 +150,15 @@ __global__ void __launch_bounds__(256) k_apply(const LevelBufs *__restrict__ des
     while (j * j < (int)j2) ++j;
     a.hint[npid] = (uint8_t)min((int)a.jaux[i] + 2 * j, 255);
   }
+  // the block's largest jump, one atomic per block onto the chart's maximum
+  __shared__ unsigned wmax[8];
   m2 = __reduce_max_sync(0xffffffffu, m2);
-  if ((threadIdx.x & 31) == 0 && m2) atomicMax(&st->gate_jump2, m2);
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) m2 = max(m2, wmax[w]);
+    if (m2) atomicMax(&st->gate_jump2, m2);
+  }
 }
 
 // One thread per chart: save the state after the plain iteration, make the
