@@ -17,11 +17,10 @@ constexpr int kNoneAbove = -32768;  // "no site above" in the column summaries
 constexpr int kNoneBelow = 32767;   // "no site below"
 constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 for
                                     // every entry of gcvt.cu:842-847
-constexpr int kRowsPerBlock = 1;    // rows (one warp each) per row-pass block
 constexpr int kWarpSites = 8192;    // one site per warp up to this many sites
 constexpr int kListWords = 512;    // bitmap words per site-list block
 constexpr int kMinN = 256;   // n must be a multiple of 256 (S = n/32 >= 8)
-constexpr int kMaxN = 8192;  // row-pass shared memory: 4 rows x 32 KB at 8192
+constexpr int kMaxN = 8192;  // largest grid (the row pass's whole-row buffer: 32 KB)
 
 __host__ __device__ inline uint32_t pack_xy(int x, int y) {
   return (uint32_t)(uint16_t)x | ((uint32_t)(uint16_t)y << 16);
@@ -68,6 +67,9 @@ struct DevState {
   int gate_tried, gate_kept;  // jumps proposed / kept
   double gate_e0;      // energy of the sites the jump starts from
   double gate_e1;      // energy of the jumped sites
+  // Labelling (labeller.cu): rows whose candidate hull did not fit the
+  // bounded buffer of k_rows, for k_rows_full (zero between labellings).
+  unsigned row_ovf[kMaxN / 32];
 };
 
 // Buffers of one resolution level, passed by value to every kernel.

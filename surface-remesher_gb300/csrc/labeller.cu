@@ -11,7 +11,7 @@
 //   * row pass (gcvt.cu:227-479): nearest of the column candidates, ties to
 //     the smaller column (kernelColor's '>' break at gcvt.cu:457).
 //
-// GB300 layout (two kernels instead of ~20 launches and ~60 B/px):
+// GB300 layout (three kernels instead of ~20 launches and ~60 B/px):
 //   * sites live in a bitmap of 64-row words, bits[band][column] -- one
 //     64-bit word per column and PBA band, so the band tie rule is "the lower
 //     site came from the same word";
@@ -21,12 +21,16 @@
 //     column candidates 32 columns at a time from the bitmap word and the
 //     summaries (no column-nearest grid is ever written); candidate (x, g)
 //     is the point (x, B = x^2 + g^2) and the pixels it wins lie under the
-//     lower convex hull of the points.  The hull is built in shared memory by
-//     rounds of simultaneous chord removal (every point strictly above the
-//     chord of its neighbours goes; the first round is fused into candidate
-//     generation; after 24 rounds a sequential monotone chain finishes any
-//     input), then the lanes write the row's label words from the hull's
-//     breakpoints.  The Lloyd iteration does not use this pass (cells.cu
+//     lower convex hull of the points.  Each chunk of 32 first drops, by two
+//     rounds of chord removal among its own points (every point strictly
+//     above the chord of its neighbours goes), points that cannot be on the
+//     hull; the survivors go to a half-row buffer in shared memory, where rounds
+//     of simultaneous chord removal over the whole row finish the hull (after
+//     24 rounds a sequential monotone chain finishes any input).  Then the
+//     lanes write the row's label words from the hull's breakpoints.  A row
+//     whose survivors do not fit the buffer is flagged and redone by
+//     k_rows_full with a whole-row buffer: the smaller buffer lets twice the
+//     rows share an SM.  The Lloyd iteration does not use this pass (cells.cu
 //     sums each site's cell directly); it gives the final label grid and the
 //     covering bound at a level's start.
 #include "gcvt_internal.cuh"
@@ -209,15 +213,19 @@ __device__ __forceinline__ int column_candidate(uint64_t w, int pv, int nx, uint
 
 // Lower envelope of the row's column candidates, left in C[0, K).
 // Candidates are generated 32 columns at a time (lane = column, coalesced
-// loads) and the first round of chord removal is applied on the fly; further
-// rounds remove, all at once, every point strictly above the chord of its
-// current neighbours, until a round removes nothing -- the surviving chain is
-// then convex, i.e. the lower hull (each removed point lies above a chord of
-// points on or above the hull).  After kMaxRounds the remaining points go
+// loads, the next chunk's loads in flight) and each chunk first drops, by
+// two rounds of chord removal among its own points, points strictly above
+// the chord of their neighbours there -- no such point is on the lower hull
+// of any superset.  The survivors are appended to C; further rounds over C
+// remove, all at once, every point strictly above the chord of its current
+// neighbours, until a round removes nothing -- the surviving chain is then
+// convex, i.e. the lower hull.  After kMaxRounds the remaining points go
 // through one sequential monotone-chain pass, so any input ends exactly.
+// cap: the entries C holds; -1 when the survivors do not fit.
 constexpr int kMaxRounds = 24;
+constexpr int kChunkRounds = 2;  // chord rounds within a chunk (about 40 % of a row survive two)
 
-__device__ int row_hull(const LevelBufs &a, int r, int *C) {
+__device__ int row_hull(const LevelBufs &a, int r, int *C, int cap) {
   const int n = a.n;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -234,32 +242,26 @@ __device__ int row_hull(const LevelBufs &a, int r, int *C) {
     return cr == kNoneAbove ? kNoEnt : pack_ent(x, cr - r);
   };
 
-  // ---- phase 1: candidates + fused first chord round ----------------------
+  // ---- phase 1: candidates, chunk-local chord rounds ------------------------
   const int nchunks = n >> 5;
   int K = 0;
-  int carry = kNoEnt;        // last valid candidate of earlier chunks
   int cur = cand(0);
   for (int c = 0; c < nchunks; ++c) {
     const int nxt = (c + 1 < nchunks) ? cand(c + 1) : kNoEnt;
-    const unsigned vcur = __ballot_sync(0xffffffffu, cur != kNoEnt);
-    const unsigned vnxt = __ballot_sync(0xffffffffu, nxt != kNoEnt);
-    // left neighbour: previous valid lane of this chunk, else the carry
-    const unsigned lower = vcur & lt;
-    const int lsrc = lower ? 31 - __clz(lower) : 0;
-    int left = __shfl_sync(0xffffffffu, cur, lsrc);
-    if (!lower) left = carry;
-    // right neighbour: next valid lane of this chunk, else next chunk's first
-    const unsigned upper = vcur & ~lt & ~(1u << lane);
-    const int rsrc = upper ? __ffs(upper) - 1 : (vnxt ? __ffs(vnxt) - 1 : 0);
-    const int r_in = __shfl_sync(0xffffffffu, cur, rsrc);
-    const int r_nx = __shfl_sync(0xffffffffu, nxt, rsrc);
-    int right = upper ? r_in : (vnxt ? r_nx : kNoEnt);  // unknown: keep (always safe)
-    bool keep = cur != kNoEnt &&
-                (left == kNoEnt || right == kNoEnt || below_chord(left, cur, right));
-    const unsigned km = __ballot_sync(0xffffffffu, keep);
-    if (keep) C[K + __popc(km & lt)] = cur;
-    K += __popc(km);
-    if (vcur) carry = __shfl_sync(0xffffffffu, cur, 31 - __clz(vcur));
+    unsigned vm = __ballot_sync(0xffffffffu, cur != kNoEnt);
+    for (int it = 0; it < kChunkRounds; ++it) {
+      const unsigned lower = vm & lt, upper = vm & ~lt & ~(1u << lane);
+      const int left = __shfl_sync(0xffffffffu, cur, lower ? 31 - __clz(lower) : lane);
+      const int right = __shfl_sync(0xffffffffu, cur, upper ? __ffs(upper) - 1 : lane);
+      const bool keep = cur != kNoEnt && (!lower || !upper || below_chord(left, cur, right));
+      const unsigned km = __ballot_sync(0xffffffffu, keep);
+      if (km == vm) break;
+      vm = km;
+      if (!keep) cur = kNoEnt;
+    }
+    if (K + __popc(vm) > cap) return -1;
+    if (cur != kNoEnt) C[K + __popc(vm & lt)] = cur;
+    K += __popc(vm);
     cur = nxt;
   }
   __syncwarp();
@@ -307,21 +309,9 @@ __device__ int row_hull(const LevelBufs &a, int r, int *C) {
   return K;
 }
 
-// Label pass: one warp per row writes the row's label words.  A row's hull
-// needs up to n entries of shared memory, so a block is one row (one warp):
-// blocks per SM then follow the shared memory exactly (7 at n = 8192, where
-// four-row blocks left one block of 4 warps per SM: 3.85 -> 2.19 ms; 0.39 ->
-// 0.34 ms at n = 4096).
-__global__ void __launch_bounds__(kRowsPerBlock * 32) k_rows(LevelBufs a, int respect_stop) {
-  extern __shared__ __align__(16) int smem[];
-  if (respect_stop && a.st->stopped) return;
-  const int n = a.n;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * kRowsPerBlock + warp;
-  if (r >= n) return;
-  int *C = smem + warp * n;
-  const int K = row_hull(a, r, C);
-  uint32_t *out = a.labels + (size_t)r * n;
+// The row's label words from its hull C[0, K).
+__device__ void write_row(uint32_t *out, int n, int r, const int *C, int K) {
+  const int lane = threadIdx.x & 31;
   if (K == 0) {  // no site anywhere
     for (int p = lane; p < n; p += 32) out[p] = kMarkerWord;
     return;
@@ -350,17 +340,52 @@ __global__ void __launch_bounds__(kRowsPerBlock * 32) k_rows(LevelBufs a, int re
   }
 }
 
-size_t rows_smem_bytes(int n) { return (size_t)kRowsPerBlock * n * sizeof(int); }
+// Label pass: one warp per row writes the row's label words.  A row's hull
+// buffer is half a row (the survivors of the chunk-local rounds of a typical
+// row fit): twice the rows per SM of a whole-row buffer.  A row whose survivors do
+// not fit (a row crowded with sites, where most columns' candidates stay on
+// the hull) is flagged in DevState::row_ovf and done by k_rows_full with a
+// whole-row buffer.
+constexpr int kRowCapDiv = 2;
+
+__global__ void __launch_bounds__(32) k_rows(LevelBufs a, int respect_stop) {
+  extern __shared__ __align__(16) int smem[];
+  if (respect_stop && a.st->stopped) return;
+  const int n = a.n, r = blockIdx.x;
+  if (r >= n) return;
+  const int K = row_hull(a, r, smem, n / kRowCapDiv);
+  if (K < 0) {
+    if ((threadIdx.x & 31) == 0) atomicOr(&a.st->row_ovf[r >> 5], 1u << (r & 31));
+    return;
+  }
+  write_row(a.labels + (size_t)r * n, n, r, smem, K);
+}
+
+// The flagged rows, with a whole-row buffer (a grid of a few blocks per SM
+// striding over the rows); clears their flags.
+__global__ void __launch_bounds__(32) k_rows_full(LevelBufs a, int respect_stop) {
+  extern __shared__ __align__(16) int smem[];
+  if (respect_stop && a.st->stopped) return;
+  const int n = a.n;
+  for (int r = blockIdx.x; r < n; r += gridDim.x) {
+    if (!((a.st->row_ovf[r >> 5] >> (r & 31)) & 1u)) continue;
+    const int K = row_hull(a, r, smem, n);
+    write_row(a.labels + (size_t)r * n, n, r, smem, K);
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) atomicAnd(&a.st->row_ovf[r >> 5], ~(1u << (r & 31)));
+  }
+}
+
+size_t rows_smem_bytes(int n) { return (size_t)n * sizeof(int); }
 
 cudaError_t rows_configure() {
-  return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_rows_full, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)rows_smem_bytes(kMaxN));
 }
 
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s) {
-  size_t smem = rows_smem_bytes(b.n);
-  dim3 blk(kRowsPerBlock * 32), grd((b.n + kRowsPerBlock - 1) / kRowsPerBlock);
-  k_rows<<<grd, blk, smem, s>>>(b, respect_stop);
+  k_rows<<<b.n, 32, rows_smem_bytes(b.n / kRowCapDiv), s>>>(b, respect_stop);
+  k_rows_full<<<b.n < 304 ? b.n : 304, 32, rows_smem_bytes(b.n), s>>>(b, respect_stop);
   return cudaGetLastError();
 }
 
