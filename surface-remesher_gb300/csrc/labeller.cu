@@ -21,16 +21,16 @@
 //     column candidates 32 columns at a time from the bitmap word and the
 //     summaries (no column-nearest grid is ever written); candidate (x, g)
 //     is the point (x, B = x^2 + g^2) and the pixels it wins lie under the
-//     lower convex hull of the points.  Each chunk of 32 first drops, by two
-//     rounds of chord removal among its own points (every point strictly
-//     above the chord of its neighbours goes), points that cannot be on the
-//     hull; the survivors go to a half-row buffer in shared memory, where rounds
+//     lower convex hull of the points.  Each chunk of 32 first drops, by
+//     three rounds of chord removal among its own points (every point
+//     strictly above the chord of its neighbours goes), points that cannot be
+//     on the hull; the survivors go to a 2/5-row buffer in shared memory, where rounds
 //     of simultaneous chord removal over the whole row finish the hull (after
 //     24 rounds a sequential monotone chain finishes any input).  Then the
 //     lanes write the row's label words from the hull's breakpoints.  A row
 //     whose survivors do not fit the buffer is flagged and redone by
-//     k_rows_full with a whole-row buffer: the smaller buffer lets twice the
-//     rows share an SM.  The Lloyd iteration does not use this pass (cells.cu
+//     k_rows_full with a whole-row buffer: the smaller buffer lets 2.5 times
+//     the rows share an SM.  The Lloyd iteration does not use this pass (cells.cu
 //     sums each site's cell directly); it gives the final label grid and the
 //     covering bound at a level's start.
 #include "gcvt_internal.cuh"
@@ -214,7 +214,7 @@ __device__ __forceinline__ int column_candidate(uint64_t w, int pv, int nx, uint
 // Lower envelope of the row's column candidates, left in C[0, K).
 // Candidates are generated 32 columns at a time (lane = column, coalesced
 // loads, the next chunk's loads in flight) and each chunk first drops, by
-// two rounds of chord removal among its own points, points strictly above
+// three rounds of chord removal among its own points, points strictly above
 // the chord of their neighbours there -- no such point is on the lower hull
 // of any superset.  The survivors are appended to C; further rounds over C
 // remove, all at once, every point strictly above the chord of its current
@@ -223,7 +223,7 @@ __device__ __forceinline__ int column_candidate(uint64_t w, int pv, int nx, uint
 // through one sequential monotone-chain pass, so any input ends exactly.
 // cap: the entries C holds; -1 when the survivors do not fit.
 constexpr int kMaxRounds = 24;
-constexpr int kChunkRounds = 2;  // chord rounds within a chunk (about 40 % of a row survive two)
+constexpr int kChunkRounds = 3;  // chord rounds within a chunk (28-31 % of a row survive three)
 
 __device__ int row_hull(const LevelBufs &a, int r, int *C, int cap) {
   const int n = a.n;
@@ -341,19 +341,19 @@ __device__ void write_row(uint32_t *out, int n, int r, const int *C, int K) {
 }
 
 // Label pass: one warp per row writes the row's label words.  A row's hull
-// buffer is half a row (the survivors of the chunk-local rounds of a typical
-// row fit): twice the rows per SM of a whole-row buffer.  A row whose survivors do
+// buffer holds 2/5 of a row (the survivors of the chunk-local rounds of a
+// typical row fit): 2.5 times the rows per SM of a whole-row buffer.  A row whose survivors do
 // not fit (a row crowded with sites, where most columns' candidates stay on
 // the hull) is flagged in DevState::row_ovf and done by k_rows_full with a
 // whole-row buffer.
-constexpr int kRowCapDiv = 2;
+constexpr int row_cap(int n) { return n * 2 / 5; }
 
 __global__ void __launch_bounds__(32) k_rows(LevelBufs a, int respect_stop) {
   extern __shared__ __align__(16) int smem[];
   if (respect_stop && a.st->stopped) return;
   const int n = a.n, r = blockIdx.x;
   if (r >= n) return;
-  const int K = row_hull(a, r, smem, n / kRowCapDiv);
+  const int K = row_hull(a, r, smem, row_cap(n));
   if (K < 0) {
     if ((threadIdx.x & 31) == 0) atomicOr(&a.st->row_ovf[r >> 5], 1u << (r & 31));
     return;
@@ -384,7 +384,7 @@ cudaError_t rows_configure() {
 }
 
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s) {
-  k_rows<<<b.n, 32, rows_smem_bytes(b.n / kRowCapDiv), s>>>(b, respect_stop);
+  k_rows<<<b.n, 32, rows_smem_bytes(row_cap(b.n)), s>>>(b, respect_stop);
   k_rows_full<<<b.n < 304 ? b.n : 304, 32, rows_smem_bytes(b.n), s>>>(b, respect_stop);
   return cudaGetLastError();
 }
