@@ -55,7 +55,8 @@ typedef struct {
 typedef struct {
     int cell_blocks_per_sm; /* persistent Lloyd grid: blocks (warps) per SM, 0 = all that fit */
     int hint_slack;         /* a site's next window: 2 R + hint_slack pixels              */
-    int jfa_tail_halo;      /* jump flooding: steps <= halo/2 fused in one launch (8/16/32) */
+    int jfa_tail_halo;      /* jump flooding: steps <= halo/2 fused in one launch (8/16/32;
+                               0, the default: every step its own launch) */
     float lloyd_ms;         /* autotune: best time of one Lloyd iteration (ms)           */
     float jfa_ms;           /* autotune: best time of one jump-flooding labelling (ms)   */
     int cell_mode;          /* Lloyd cells: 0 = one site per warp up to 8192 sites, else

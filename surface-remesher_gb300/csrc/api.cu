@@ -53,7 +53,7 @@ struct gcvt_ctx {
   // fit), window hint slack, jump-flooding fusion depth (tail halo)
   int cell_grid = 0;
   int hint_slack = 2;
-  int jfa_halo = 16;
+  int jfa_halo = 0;             // jump flooding: 0 = every step its own launch
   int cell_mode = 0;            // 0 auto, 1 one site per lane, 2 one site per warp
   float4 *sitev = nullptr;      // one site per warp: kWarpSites site values
   unsigned *gcnt = nullptr;     //   and kWarpSites / 32 group counters
@@ -741,7 +741,7 @@ int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, 
   uint32_t *a = c->jfa, *b = c->jfa + nmax2;
   unsigned long long *counts = reinterpret_cast<unsigned long long *>(c->jfa + 2 * nmax2);
   CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-  CK(launch_bits_to_grid(c->bits[c->st_host->cur], n, a, c->stream));
+  CK(launch_jfa_seed(c->bits[c->st_host->cur], n, a, c->stream));
   uint32_t *res = nullptr;
   CK(launch_jfa(a, b, n, c->err, &res, c->stream, c->jfa_halo));
   if (stats) {
@@ -768,8 +768,8 @@ int gcvt_ctx_jfa_label(gcvt_ctx *c, int16_t *labels, unsigned long long *stats, 
 int gcvt_ctx_set_tuning(gcvt_ctx *c, const gcvt_tuning *t) {
   if (!c || !t) return GCVT_ERR_ARGUMENT;
   if (t->cell_blocks_per_sm < 0 || t->cell_blocks_per_sm > 32 || t->hint_slack < 0 ||
-      t->hint_slack > 64 || (t->jfa_tail_halo != 8 && t->jfa_tail_halo != 16 &&
-                             t->jfa_tail_halo != 32) ||
+      t->hint_slack > 64 || (t->jfa_tail_halo != 0 && t->jfa_tail_halo != 8 &&
+                             t->jfa_tail_halo != 16 && t->jfa_tail_halo != 32) ||
       t->cell_mode < 0 || t->cell_mode > 2)
     return GCVT_ERR_ARGUMENT;
   int sms = 0;
@@ -894,13 +894,13 @@ int gcvt_ctx_autotune(gcvt_ctx *c, gcvt_tuning *out) {
     rc = GCVT_ERR_ALLOC;
   slot = 0;
   if (!rc) rc = copy_state(false);
-  const int halos[3] = {8, 16, 32};
-  for (int hi = 0; hi < 3 && !rc; ++hi) {
+  const int halos[4] = {0, 8, 16, 32};
+  for (int hi = 0; hi < 4 && !rc; ++hi) {
     uint32_t *ja = c->jfa, *jb = c->jfa + (size_t)c->n_max * c->n_max, *res = nullptr;
     float ms = 0.f;
     for (int it = 0; it < 3 && !rc; ++it) {
       float one = 0.f;
-      if (launch_bits_to_grid(c->bits[saved_host.cur], n, ja, c->stream) != cudaSuccess ||
+      if (launch_jfa_seed(c->bits[saved_host.cur], n, ja, c->stream) != cudaSuccess ||
           cudaEventRecord(e0, c->stream) != cudaSuccess ||
           launch_jfa(ja, jb, n, c->err, &res, c->stream, halos[hi]) != cudaSuccess ||
           cudaEventRecord(e1, c->stream) != cudaSuccess ||
@@ -1300,7 +1300,7 @@ int gcvt_ctx_time_kernels(gcvt_ctx *c, int iterations, float *ms3) {
     uint32_t *ja = c->jfa, *jb = c->jfa + nmax2, *res = nullptr;
     for (int it = 0; it < iterations && status == GCVT_OK; ++it) {
       float ms = 0.f;
-      if (launch_bits_to_grid(c->bits[c->st_host->cur], c->n, ja, c->stream) != cudaSuccess ||
+      if (launch_jfa_seed(c->bits[c->st_host->cur], c->n, ja, c->stream) != cudaSuccess ||
           cudaEventRecord(ev[0], c->stream) != cudaSuccess ||
           launch_jfa(ja, jb, c->n, c->err, &res, c->stream, c->jfa_halo) != cudaSuccess ||
           cudaEventRecord(ev[1], c->stream) != cudaSuccess ||

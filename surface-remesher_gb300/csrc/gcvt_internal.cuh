@@ -13,6 +13,9 @@ namespace cvtgb {
 
 constexpr int kMarker = -32768;
 constexpr uint32_t kMarkerWord = 0x80008000u;
+// "no label" inside jump flooding: the point (16383, 16383), farther from
+// every pixel of a grid of side <= 8192 than any site
+constexpr uint32_t kJfaNone = 0x3fff3fffu;
 constexpr int kNoneAbove = -32768;  // "no site above" in the column summaries
 constexpr int kNoneBelow = 32767;   // "no site below"
 constexpr int kBand = 64;           // PBA+ phase-1 band height: n / m1 == 64 for
@@ -120,7 +123,14 @@ __device__ __forceinline__ const uint64_t *cur_bits(const LevelBufs &a) {
 // Kernels (launch helpers in labeller.cu / lloyd.cu / cells.cu).
 cudaError_t launch_grid_to_bits(const uint32_t *grid, int n, uint64_t *bits, int *err,
                                 int *count, cudaStream_t s);
-cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s);
+// the site grid of a bitmap: pack_xy(x, y) per site (pack_xy(y, x) with
+// swap), `empty` elsewhere
+cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s,
+                                uint32_t empty = kMarkerWord, bool swap = false);
+// jump flooding's seeding: (x << 16) | y per site, kJfaNone elsewhere
+inline cudaError_t launch_jfa_seed(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s) {
+  return launch_bits_to_grid(bits, n, grid, s, kJfaNone, true);
+}
 cudaError_t launch_summary(const LevelBufs &b, int respect_stop, cudaStream_t s);
 cudaError_t launch_fixed_bits(const uint8_t *mask, int n, uint64_t *fixed_bits, cudaStream_t s);
 cudaError_t launch_rows(const LevelBufs &b, int respect_stop, cudaStream_t s);

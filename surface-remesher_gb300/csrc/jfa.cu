@@ -1,26 +1,43 @@
 // jfa.cu -- jump-flooding Voronoi labelling: an approximate labeller beside
 // the exact one (labeller.cu), with its error measured against it.
 //
-// The label grid holds one int32 per pixel (x in the low, y in the high 16
-// bits, MARKER for none), the same words as the reference's short2 grids.
-// A step of offset k gives pixel p the nearest of the nine labels at
-// p + (dx, dy) k, dx, dy in {-1, 0, 1} (ties: smaller x, then smaller y).
-// The schedule is k = n/2, n/4, ..., 1 and one more step of 1 (for a side
-// that is not a power of two, from the largest power of two <= n/2).
+// The result is a label grid of one int32 per pixel (x in the low, y in the
+// high 16 bits), the same words as the reference's short2 grids; the grids
+// between launches hold (x << 16) | y instead, the order of the tie rule, and
+// the last launch swaps the halves back.  A step of offset k gives pixel p
+// the nearest of the nine labels at p + (dx, dy) k, dx, dy in {-1, 0, 1};
+// ties go to the smaller x, then the smaller y (the exact labeller's column
+// order).  The schedule is k = n/2, n/4, ..., 1 and one more step of 1 (for a
+// side that is not a power of two, from the largest power of two <= n/2).
+// Between launches "no label" is kJfaNone, the point (16383, 16383): farther
+// from every pixel than any site, so it needs no test of its own; the
+// seeding writes it and the last launch turns it into MARKER.
 //
-//   * k > H/2: k_jfa_step, one launch per step, sixteen pixels per thread:
-//     four groups of four at (x0 + a k, y + b k), whose neighbours are 4 x 4
-//     aligned 16-byte words (k is a multiple of 4) -- 16 loads for 16
-//     pixels, every load and store 128-bit, a warp reading 512 contiguous
-//     bytes per row.  The nearest label is the smallest 64-bit key
-//     (distance, then x, then y).
-//   * k = H/2, ..., 1, 1: k_jfa_tail<H>, one launch (H = 8, 16 or 32, the
-//     fusion depth; 16 by default, the autotuner picks).  A block loads its
-//     64 x 64 tile with an H-pixel halo (96 x 96 labels, 36 KB, for H = 16)
+// All kernels work on units of 16 pixels: (a, b, i) at column x0 + a cs + i,
+// row y + b k (a, b in {0, 1}, i < 4), whose candidates lie in 16 aligned
+// 16-byte words (r, s) at column x0 + (s - 1) cs, row y + (r - 1) k.  For k a
+// multiple of 4, cs = k and a pixel's candidates are component i of nine of
+// the words; for k = 1 or 2, cs = 4 (eight adjacent columns).  The unit walks
+// its 64 labels once: each is unpacked once, and its key for a pixel p,
+//   e = |c|^2 - 2 c.p + bias  (= |c - p|^2 - |p|^2 + bias),
+// costs one multiply-add per further pixel that uses it; |p|^2 is the same for
+// all nine candidates of p, so (e, x, y) orders them as (distance, x, y) does.
+// A pixel's first candidate initialises its key; the other eight compare.
+// The compare and select of the 64-bit keys (four integer-ALU instructions
+// per candidate) bound the kernels: the integer ALU pipe runs at ~85 %.
+//
+//   * k > H/2: k_jfa_step, one launch per step, one unit per thread, every
+//     load and store 128-bit (a warp reads 512 contiguous bytes per row).
+//   * H = 0 (the fastest on GB300, as the autotuner finds): every step its
+//     own launch, k_jfa_step down to k = 4, k_jfa_step_small for 2, 1, 1.
+//   * H = 8, 16 or 32: k = H/2, ..., 1, 1 in one k_jfa_tail<H> launch.  A
+//     block loads its 64 x 64 tile with an H-pixel halo ((64 + 2H)^2 labels)
 //     into shared memory with one TMA tile copy, runs the steps there on a
-//     region that shrinks by each step's offset (8 + 4 + 2 + 1 + 1 = 16),
-//     ping-ponging between two shared buffers, and writes the tile back with
-//     128-bit stores: five passes over the grid for one read and one write.
+//     region that shrinks by each step's offset, ping-ponging between two
+//     shared buffers, and writes the tile back with 128-bit stores.  It saves
+//     DRAM traffic, which is not the limit, and costs halo work, barriers and
+//     instruction-cache misses (five unrolled steps), so it runs slower than
+//     separate launches.
 #include "gcvt_internal.cuh"
 
 #include <cuda.h>
@@ -29,6 +46,10 @@
 namespace cvtgb {
 
 constexpr int kTile = 64;
+constexpr int kTailThreads = 128;
+// keeps e = |c - p|^2 - |p|^2 + kJfaBias in [0, 2^31) for pixels and labels of
+// a grid of side <= 8192 (|p|^2 < 2^27; |c - p|^2 < 2^30 with kJfaNone)
+constexpr unsigned kJfaBias = 1u << 27;
 // Tail of halo H: steps H/2, H/4, ..., 1 and the extra 1 (they sum to H) on
 // a (64 + 2H)^2 region; H = 8, 16 or 32 (the fusion depth the autotuner picks).
 template <int H> __host__ __device__ constexpr int tail_reg() { return kTile + 2 * H; }
@@ -39,21 +60,6 @@ template <int H> constexpr unsigned tail_bytes() {
 __device__ __forceinline__ int lab_x(uint32_t v) { return (int)(int16_t)(v & 0xffffu); }
 __device__ __forceinline__ int lab_y(uint32_t v) { return (int)(int16_t)(v >> 16); }
 
-// Comparison key of label c for pixel (x, y): squared distance in the high
-// word, the site's (x, y) in the low word (so ties go to the smaller x, then
-// y).  The nearest label is the smallest key.  "No label" (MARKER, -32768 in
-// both halves) needs no special case: its squared distance from a pixel of a
-// grid of side <= 8192 lies in [2^31, 3.4e9], no overflow of 32 bits, and is
-// larger than any site's (< 2 * 8192^2).
-__device__ __forceinline__ unsigned long long jkey(uint32_t c, int x, int y) {
-  const unsigned dx = (unsigned)(lab_x(c) - x), dy = (unsigned)(lab_y(c) - y);
-  return ((unsigned long long)(dx * dx + dy * dy) << 32) | __byte_perm(c, 0, 0x1032);
-}
-
-__device__ __forceinline__ uint32_t jlabel(unsigned long long k) {
-  return __byte_perm((uint32_t)k, 0, 0x1032);
-}
-
 __device__ __forceinline__ unsigned long long kmin(unsigned long long a, unsigned long long b) {
   return b < a ? b : a;
 }
@@ -62,10 +68,87 @@ __device__ __forceinline__ uint32_t comp(const uint4 &v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// One step of offset k (a multiple of 4).  A thread takes the 2 x 2 groups of
-// four pixels at (x0 + a k, y + b k), a, b in {0, 1}, (x0, y) in the even
-// k-blocks: their nine neighbours each are 4 x 4 aligned 16-byte words, 16
-// loads for 16 pixels.
+// the words of four keys, as they are between launches
+__device__ __forceinline__ uint4 words(const unsigned long long (&k)[4]) {
+  return make_uint4((uint32_t)k[0], (uint32_t)k[1], (uint32_t)k[2], (uint32_t)k[3]);
+}
+
+// a word between launches -> the label of the result (MARKER for none)
+__device__ __forceinline__ uint32_t final_label(uint32_t w) {
+  return w == kJfaNone ? kMarkerWord : __byte_perm(w, 0, 0x1032);
+}
+
+__device__ __forceinline__ uint4 final_labels(uint4 v) {
+  return make_uint4(final_label(v.x), final_label(v.y), final_label(v.z), final_label(v.w));
+}
+
+// The 16 words (r, s) of a unit at column x0 + (s - 1) cs, row y + (r - 1) k;
+// outside the grid kJfaNone.  (A separate untested path for units wholly
+// inside the grid measured slower: it raised the kernel's registers.)
+__device__ __forceinline__ void unit_load(const uint32_t *__restrict__ in, int n, int x0, int y,
+                                          int k, int cs, uint4 (&w)[4][4]) {
+  const uint4 none = make_uint4(kJfaNone, kJfaNone, kJfaNone, kJfaNone);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int yy = y + (r - 1) * k;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int xx = x0 + (s - 1) * cs;
+      w[r][s] = (yy >= 0 && yy < n && xx >= 0 && xx < n)
+                    ? __ldg(reinterpret_cast<const uint4 *>(in + (size_t)yy * n + xx))
+                    : none;
+    }
+  }
+}
+
+// The nearest label of each pixel of a unit (see the file comment) among its
+// nine candidates, words (x << 16) | y: best[a][b][i] = (e << 32) | word,
+// smallest first.
+// KS = 0: cs = k, k a multiple of 4 (any value); KS = 1 or 2: k = KS, cs = 4.
+template <int KS>
+__device__ __forceinline__ void unit_best(const uint4 (&w)[4][4], int x0, int y, int k,
+                                          unsigned long long (&best)[2][2][4]) {
+  const unsigned m2x = 0u - 2u * (unsigned)x0, m2y = 0u - 2u * (unsigned)y;
+  const unsigned m2k = 0u - 2u * (unsigned)(KS ? KS : k);
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t c = comp(w[r][s], j);
+        const unsigned cx = c >> 16, cy = c & 0xffffu;
+        // e for the pixel at (x0, y)
+        const unsigned base = cx * cx + cy * cy + kJfaBias + cx * m2x + cy * m2y;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          if (r - 1 - b < -1 || r - 1 - b > 1) continue;
+          const unsigned eb = b ? base + cy * m2k : base;
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              unsigned e;
+              bool first;  // the pixel's first candidate in this loop order
+              if (KS == 0) {
+                if (i != j || s - 1 - a < -1 || s - 1 - a > 1) continue;
+                e = eb + cx * (0u - 2u * (unsigned)i) + (a ? cx * m2k : 0u);
+                first = r - 1 - b == -1 && s - 1 - a == -1;
+              } else {
+                const int off = 4 * (s - 1) + j - 4 * a - i;
+                if (off != -KS && off != 0 && off != KS) continue;
+                e = eb + cx * (0u - 2u * (unsigned)(4 * a + i));
+                first = r - 1 - b == -1 && off == -KS;
+              }
+              const unsigned long long key = ((unsigned long long)e << 32) | c;
+              best[a][b][i] = first ? key : kmin(best[a][b][i], key);
+            }
+        }
+      }
+}
+
+// One step of offset k (a multiple of 4): thread qi of row yi takes the unit
+// with cs = k at x0 = (qi / (k/4)) 2k + 4 (qi % (k/4)), y = (yi / k) 2k + yi % k.
 __global__ void __launch_bounds__(256) k_jfa_step(const uint32_t *__restrict__ in,
                                                   uint32_t *__restrict__ out, int n, int k) {
   const int kq = k / 4;
@@ -75,19 +158,10 @@ __global__ void __launch_bounds__(256) k_jfa_step(const uint32_t *__restrict__ i
   const int yi = blockIdx.y;
   const int x0 = (qi / kq) * 2 * k + (qi % kq) * 4;
   const int y = (yi / k) * 2 * k + (yi % k);
-  const uint4 none = make_uint4(kMarkerWord, kMarkerWord, kMarkerWord, kMarkerWord);
-  uint4 c[4][4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const int yy = y + (r - 1) * k;
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      const int xx = x0 + (s - 1) * k;
-      c[r][s] = (yy >= 0 && yy < n && xx >= 0 && xx < n)
-                    ? __ldg(reinterpret_cast<const uint4 *>(in + (size_t)yy * n + xx))
-                    : none;
-    }
-  }
+  uint4 w[4][4];
+  unit_load(in, n, x0, y, k, k, w);
+  unsigned long long best[2][2][4];
+  unit_best<0>(w, x0, y, k, best);
 #pragma unroll
   for (int b = 0; b < 2; ++b) {
     const int py = y + b * k;
@@ -96,32 +170,112 @@ __global__ void __launch_bounds__(256) k_jfa_step(const uint32_t *__restrict__ i
     for (int a = 0; a < 2; ++a) {
       const int px = x0 + a * k;
       if (px >= n) continue;
-      uint32_t res[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        unsigned long long best = ~0ull;
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int s = 0; s < 3; ++s) best = kmin(best, jkey(comp(c[b + r][a + s], i), px + i, py));
-        res[i] = jlabel(best);
-      }
-      *reinterpret_cast<uint4 *>(out + (size_t)py * n + px) =
-          make_uint4(res[0], res[1], res[2], res[3]);
+      *reinterpret_cast<uint4 *>(out + (size_t)py * n + px) = words(best[a][b]);
     }
   }
+}
+
+// A step of offset KS = 2 or 1 (on the last step, "no label" becomes MARKER):
+// thread qi of row pair yi takes the unit with cs = 4 at x0 = 8 qi,
+// y = (yi / KS) 2 KS + yi % KS.
+template <int KS, bool LAST>
+__global__ void __launch_bounds__(256) k_jfa_step_small(const uint32_t *__restrict__ in,
+                                                        uint32_t *__restrict__ out, int n) {
+  const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= n / 8) return;
+  const int yi = blockIdx.y;
+  const int x0 = 8 * qi, y = (yi / KS) * 2 * KS + yi % KS;
+  uint4 w[4][4];
+  unit_load(in, n, x0, y, KS, 4, w);
+  unsigned long long best[2][2][4];
+  unit_best<KS>(w, x0, y, KS, best);
+#pragma unroll
+  for (int b = 0; b < 2; ++b)
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      const uint4 v = words(best[a][b]);
+      *reinterpret_cast<uint4 *>(out + (size_t)(y + b * KS) * n + x0 + 4 * a) =
+          LAST ? final_labels(v) : v;
+    }
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// One step of offset K inside the tail's shared buffers (side R = 64 + 2H,
+// grid position of [0][0] = (ox, oy)): pixels of rows and columns [HH, R - HH)
+// (HH = the halo left after the step) from `cur` into `nxt`.  Units of cs = K
+// for K >= 4, cs = 4 for K < 4 (their columns rounded out to whole units;
+// the extra pixels lie outside the region and are never read as valid).
+// Pixels outside the grid stay kJfaNone.
+template <int K, int HH, int R>
+__device__ __forceinline__ void tail_step(const uint32_t *__restrict__ cur,
+                                          uint32_t *__restrict__ nxt, int ox, int oy, int n,
+                                          bool inner) {
+  constexpr int KS = K >= 4 ? 0 : K;
+  constexpr int CS = K >= 4 ? K : 4;
+  constexpr int W = R - 2 * HH;               // the region's side
+  constexpr int PAIRS = W / 2;                // row pairs (y, y + K)
+  constexpr int X0 = KS ? (HH / 4) * 4 : HH;  // first unit's column
+  constexpr int UNITS = KS ? (R - HH - X0 + 7) / 8 : W / 8;
+  static_assert(W % (2 * K) == 0, "rows pair up");
+  static_assert(KS || (W % (2 * K) == 0 && HH % 4 == 0), "units tile the region");
+  static_assert(X0 - CS >= 0 && HH >= K, "reads stay in the buffer");
+  static_assert(KS ? X0 + 8 * UNITS + 4 <= R : HH + W + K <= R, "reads stay in the buffer");
+  for (int u = threadIdx.x; u < PAIRS * UNITS; u += kTailThreads) {
+    const int p = u / UNITS, q = u % UNITS;
+    const int y = HH + (p / K) * 2 * K + p % K;
+    const int x0 = KS ? X0 + 8 * q : HH + (q / (K / 4)) * 2 * K + 4 * (q % (K / 4));
+    uint4 w[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        w[r][s] = *reinterpret_cast<const uint4 *>(cur + (y + (r - 1) * K) * R + x0 + (s - 1) * CS);
+    unsigned long long best[2][2][4];
+    unit_best<KS>(w, ox + x0, oy + y, K, best);
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const int row = y + b * K, col = x0 + a * CS;
+        uint4 v = words(best[a][b]);
+        if (!inner) {
+          const int gy = oy + row, gx = ox + col;
+          const bool rin = gy >= 0 && gy < n;
+          if (!rin || gx < 0 || gx >= n) v.x = kJfaNone;
+          if (!rin || gx + 1 < 0 || gx + 1 >= n) v.y = kJfaNone;
+          if (!rin || gx + 2 < 0 || gx + 2 >= n) v.z = kJfaNone;
+          if (!rin || gx + 3 < 0 || gx + 3 >= n) v.w = kJfaNone;
+        }
+        *reinterpret_cast<uint4 *>(nxt + row * R + col) = v;
+      }
+  }
+}
+
+// Steps K, K/2, ..., 1 and the extra 1; HH is the halo left after step K.
+template <int K, int HH, int R>
+__device__ __forceinline__ uint32_t *tail_steps(uint32_t *cur, uint32_t *nxt, int ox, int oy,
+                                                int n, bool inner) {
+  tail_step<K, HH, R>(cur, nxt, ox, oy, n, inner);
+  __syncthreads();
+  if constexpr (K > 1) {
+    return tail_steps<K / 2, HH + K / 2, R>(nxt, cur, ox, oy, n, inner);
+  } else if constexpr (HH < (R - kTile) / 2) {
+    return tail_steps<1, HH + 1, R>(nxt, cur, ox, oy, n, inner);  // the extra step of 1
+  } else {
+    return nxt;
+  }
+}
+
 // Steps H/2 .. 1, 1 on one 64 x 64 tile; `tm` maps the input label grid
 // (n x n uint32, box (64 + 2H)^2).  err[0] is set if the tile copy does not
 // arrive within the wait limit (the block then writes nothing).
 template <int H>
-__global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtensorMap tm,
-                                                  uint32_t *__restrict__ out, int n, int *err) {
+__global__ void __launch_bounds__(kTailThreads) k_jfa_tail(const __grid_constant__ CUtensorMap tm,
+                                                           uint32_t *__restrict__ out, int n,
+                                                           int *err) {
   constexpr int kHalo = H, kReg = tail_reg<H>();
   extern __shared__ __align__(1024) uint32_t smem[];
   uint32_t *buf0 = smem, *buf1 = smem + kReg * kReg;
@@ -157,43 +311,21 @@ __global__ void __launch_bounds__(256) k_jfa_tail(const __grid_constant__ CUtens
     return;
   }
   // the copy fills positions outside the grid with zeros: no label there
-  for (int p = tid; p < kReg * kReg; p += blockDim.x) {
-    const int gx = ox + p % kReg, gy = oy + p / kReg;
-    if (gx < 0 || gy < 0 || gx >= n || gy >= n) buf0[p] = kMarkerWord;
+  const bool inner = ox >= 0 && oy >= 0 && ox + kReg <= n && oy + kReg <= n;
+  if (!inner) {
+    for (int p = tid; p < kReg * kReg; p += kTailThreads) {
+      const int gx = ox + p % kReg, gy = oy + p / kReg;
+      if (gx < 0 || gy < 0 || gx >= n || gy >= n) buf0[p] = kJfaNone;
+    }
   }
   __syncthreads();
-  uint32_t *cur = buf0, *nxt = buf1;
-  int h = 0;  // rows / columns of the region already out of date
-#pragma unroll
-  for (int k2 = H; k2 >= 1; k2 >>= 1) {  // k = H/2, ..., 1, then 1 again
-    const int k = k2 > 1 ? k2 / 2 : 1;
-    h += k;
-    const int w = kReg - 2 * h;
-    for (int p = tid; p < w * w; p += blockDim.x) {
-      const int i = h + p / w, j = h + p % w;  // buffer row, column
-      const int gx = ox + j, gy = oy + i;
-      unsigned long long best = ~0ull;  // outside the grid: no label
-      if (gx >= 0 && gy >= 0 && gx < n && gy < n) {
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-          for (int dx = -1; dx <= 1; ++dx)
-            best = kmin(best, jkey(cur[(i + dy * k) * kReg + j + dx * k], gx, gy));
-      }
-      nxt[i * kReg + j] = best == ~0ull ? kMarkerWord : jlabel(best);
-    }
-    __syncthreads();
-    uint32_t *t = cur;
-    cur = nxt;
-    nxt = t;
-  }
-  // the tile: buffer rows / columns [16, 80), 16-byte stores
-  for (int p = tid; p < kTile * kTile / 4; p += blockDim.x) {
+  const uint32_t *res = tail_steps<H / 2, H / 2, kReg>(buf0, buf1, ox, oy, n, inner);
+  // the tile: buffer rows / columns [H, H + 64), 16-byte stores, as labels
+  for (int p = tid; p < kTile * kTile / 4; p += kTailThreads) {
     const int i = p / (kTile / 4), j = 4 * (p % (kTile / 4));
-    const uint32_t *src = cur + (kHalo + i) * kReg + kHalo + j;
+    const uint4 v = *reinterpret_cast<const uint4 *>(res + (kHalo + i) * kReg + kHalo + j);
     if (ty + i < n && tx + j < n)
-      *reinterpret_cast<uint4 *>(out + (size_t)(ty + i) * n + tx + j) =
-          *reinterpret_cast<const uint4 *>(src);
+      *reinterpret_cast<uint4 *>(out + (size_t)(ty + i) * n + tx + j) = final_labels(v);
   }
 }
 
@@ -246,7 +378,7 @@ cudaError_t launch_tail(uint32_t *in, uint32_t *out, int n, int *err, cudaStream
       CUDA_SUCCESS)
     return cudaErrorInvalidValue;
   const dim3 grid((unsigned)(n / kTile), (unsigned)(n / kTile));
-  k_jfa_tail<H><<<grid, 256, tail_bytes<H>(), s>>>(tm, out, n, err);
+  k_jfa_tail<H><<<grid, kTailThreads, tail_bytes<H>(), s>>>(tm, out, n, err);
   return cudaGetLastError();
 }
 }  // namespace
@@ -273,27 +405,36 @@ cudaError_t jfa_configure() {
   return cudaSuccess;
 }
 
-// Jump flooding of the label grid `a` (seeded: every site labels itself,
-// MARKER elsewhere) for a grid of side n (a multiple of 64 >= 128); `b` is
+// Jump flooding of the grid `a` (seeded: every site holds its word
+// (x << 16) | y, kJfaNone elsewhere) for a grid of side n (a multiple of 64 >= 128); `b` is
 // the ping-pong partner; steps above tail_halo / 2 run one launch each, the
-// rest in one fused tail launch (tail_halo = 8, 16 or 32).  Returns the
-// buffer holding the result in *result.
+// rest in one fused tail launch (tail_halo = 8, 16 or 32); tail_halo = 0:
+// every step its own launch.  Returns the buffer holding the result in
+// *result.
 cudaError_t launch_jfa(uint32_t *a, uint32_t *b, int n, int *err, uint32_t **result,
                        cudaStream_t s, int tail_halo) {
   cudaError_t e = jfa_configure();
   if (e != cudaSuccess) return e;
-  if (tail_halo != 8 && tail_halo != 32) tail_halo = 16;
+  if (tail_halo != 0 && tail_halo != 8 && tail_halo != 32) tail_halo = 16;
   while (tail_halo > 8 && tail_halo > n / 4) tail_halo /= 2;  // the steps start at <= n/2
   uint32_t *in = a, *out = b;
   int k = 1;
   while (2 * k <= n / 2) k *= 2;  // the largest power of two <= n/2
-  for (; k > tail_halo / 2; k /= 2) {
+  for (; k > (tail_halo ? tail_halo / 2 : 2); k /= 2) {
     const int blocks = (n + 2 * k - 1) / (2 * k);
     const dim3 grid((unsigned)((blocks * (k / 4) + 255) / 256), (unsigned)(blocks * k));
     k_jfa_step<<<grid, 256, 0, s>>>(in, out, n, k);
     uint32_t *t = in;
     in = out;
     out = t;
+  }
+  if (!tail_halo) {  // k = 2, 1 and the extra 1
+    const dim3 grid((unsigned)((n / 8 + 255) / 256), (unsigned)(n / 2));
+    k_jfa_step_small<2, false><<<grid, 256, 0, s>>>(in, out, n);
+    k_jfa_step_small<1, false><<<grid, 256, 0, s>>>(out, in, n);
+    k_jfa_step_small<1, true><<<grid, 256, 0, s>>>(in, out, n);
+    *result = out;
+    return cudaGetLastError();
   }
   if (tail_halo == 8) e = launch_tail<8>(in, out, n, err, s);
   else if (tail_halo == 32) e = launch_tail<32>(in, out, n, err, s);

@@ -72,7 +72,7 @@ __global__ void k_grid_to_bits(const uint32_t *__restrict__ grid, int n,
 }
 
 __global__ void k_bits_to_grid(const uint64_t *__restrict__ bits, int n,
-                               uint32_t *__restrict__ grid) {
+                               uint32_t *__restrict__ grid, uint32_t empty, bool swap) {
   int x = blockIdx.x * blockDim.x + threadIdx.x;
   int b = blockIdx.y;
   if (x >= n) return;
@@ -80,7 +80,9 @@ __global__ void k_bits_to_grid(const uint64_t *__restrict__ bits, int n,
   uint32_t *p = grid + (size_t)(b * kBand) * n + x;
 #pragma unroll 8
   for (int i = 0; i < kBand; ++i)
-    p[(size_t)i * n] = ((w >> i) & 1ull) ? pack_xy(x, b * kBand + i) : kMarkerWord;
+    p[(size_t)i * n] = !((w >> i) & 1ull) ? empty
+                       : swap                ? pack_xy(b * kBand + i, x)
+                                             : pack_xy(x, b * kBand + i);
 }
 
 cudaError_t launch_grid_to_bits(const uint32_t *grid, int n, uint64_t *bits, int *err,
@@ -90,9 +92,10 @@ cudaError_t launch_grid_to_bits(const uint32_t *grid, int n, uint64_t *bits, int
   return cudaGetLastError();
 }
 
-cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s) {
+cudaError_t launch_bits_to_grid(const uint64_t *bits, int n, uint32_t *grid, cudaStream_t s,
+                                uint32_t empty, bool swap) {
   dim3 blk(128), grd((n + 127) / 128, n / kBand);
-  k_bits_to_grid<<<grd, blk, 0, s>>>(bits, n, grid);
+  k_bits_to_grid<<<grd, blk, 0, s>>>(bits, n, grid, empty, swap);
   return cudaGetLastError();
 }
 

@@ -289,7 +289,7 @@ class Context:
         _check(self.lib.gcvt_ctx_autotune(self.h, ctypes.byref(t)), "gcvt_ctx_autotune")
         return t.as_dict()
 
-    def set_tuning(self, cell_blocks_per_sm=0, hint_slack=2, jfa_tail_halo=16, cell_mode=0):
+    def set_tuning(self, cell_blocks_per_sm=0, hint_slack=2, jfa_tail_halo=0, cell_mode=0):
         t = Tuning(int(cell_blocks_per_sm), int(hint_slack), int(jfa_tail_halo), 0.0, 0.0,
                    int(cell_mode))
         _check(self.lib.gcvt_ctx_set_tuning(self.h, ctypes.byref(t)), "gcvt_ctx_set_tuning")

@@ -36,7 +36,7 @@ def test_tuning_changes_nothing(gcvt_lib, cuda_device, case):
     tuned, t = run(gcvt_lib, sites, rho, mask, 15, "auto")
     assert t["cell_blocks_per_sm"] in (16, 24, 32)
     assert t["hint_slack"] in (1, 2, 3)
-    assert t["jfa_tail_halo"] in (8, 16, 32)
+    assert t["jfa_tail_halo"] in (0, 8, 16, 32)
     assert t["lloyd_ms"] > 0 and t["jfa_ms"] > 0
     assert t["cell_mode"] in (1, 2)
     for a, b in zip(base, tuned):
@@ -47,6 +47,8 @@ def test_tuning_changes_nothing(gcvt_lib, cuda_device, case):
                    {"cell_blocks_per_sm": 32, "hint_slack": 3, "jfa_tail_halo": 32,
                     "cell_mode": 1},
                    {"cell_blocks_per_sm": 24, "hint_slack": 2, "jfa_tail_halo": 16,
+                    "cell_mode": 2},
+                   {"cell_blocks_per_sm": 24, "hint_slack": 2, "jfa_tail_halo": 0,
                     "cell_mode": 2}):
         other, _ = run(gcvt_lib, sites, rho, mask, 15, choice)
         for a, b in zip(base, other):

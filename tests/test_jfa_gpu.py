@@ -72,6 +72,23 @@ def test_jfa_matches_numpy(gcvt_lib, cuda_device, n, m, seed):
     ctx.close()
 
 
+@pytest.mark.parametrize("halo", [0, 8, 32])
+@pytest.mark.parametrize("n,m,seed", [(512, 4000, 6), (768, 1500, 7)])
+def test_every_fusion_depth_matches_numpy(gcvt_lib, cuda_device, halo, n, m, seed):
+    # the fused tail (halo 8 / 32) and one launch per step (halo 0) give the same labels
+    rng = np.random.default_rng(seed)
+    sites = np.full((n, n, 2), MARKER, np.int16)
+    pick = rng.choice(n * n, m, replace=False)
+    ys, xs = np.divmod(pick, n)
+    sites[ys, xs, 0], sites[ys, xs, 1] = xs, ys
+    ctx = gcvt_lib.Context(n)
+    ctx.load(sites, np.ones((n, n), np.float32), np.zeros((n, n), np.uint8))
+    ctx.set_tuning(jfa_tail_halo=halo)
+    got, _ = ctx.jfa_label()
+    assert np.array_equal(got, jfa_numpy(sites))
+    ctx.close()
+
+
 def test_jfa_error_on_clustered_sites(gcvt_lib, cuda_device):
     # dense clusters are where jump flooding errs; the count stays small
     n = 512
