@@ -382,10 +382,11 @@ int gcvt_vertex_weights(const double *uv, const double *xyz, int num_vertex,
  * the current device; `stream` is a cudaStream_t (NULL: the legacy default
  * stream).  Nothing is allocated: the scratch lives in one static device
  * array sized for n <= 2048 (about 0.8 MB, held by every device that loads the
- * library until exit); larger n returns GCVT_ERR_SIZE.  The first call on a
- * device looks up that array's device address -- make it before any stream
- * capture.  Every call waits for `stream` to finish its work before it
- * returns.  Calls share the array, so calls that overlap on the GPU race.
+ * library until exit); larger n returns GCVT_ERR_SIZE.  Every call is
+ * synchronous: it reads back an error flag and waits for `stream` before it
+ * returns, so it cannot be captured into a CUDA graph, and it fails while
+ * another thread captures in global mode.  Calls share the array, so calls
+ * that overlap on the GPU race.
  * A site pixel that does not hold its own (x, y) is detected on the GPU while
  * the labelling runs: the call then returns GCVT_ERR_INPUT and the contents
  * of `labels` are unspecified (gcvt_label_grid returns before writing). */

@@ -17,9 +17,8 @@
 // Host code may not use the array's name as a device address (in host code it
 // names a host-side stand-in).  The first call on a device takes the array's
 // device address with cudaGetSymbolAddress, with that device current, and
-// caches it for the device; make that first call before any stream capture.
-// A call waits for its stream before it returns (its one readback is the
-// error flag).  A malformed site grid is found by the GPU while the labelling
+// caches it for the device.  A call is synchronous -- it reads back the error
+// flag and waits for its stream -- so it cannot be captured into a graph.  A malformed site grid is found by the GPU while the labelling
 // runs, so on GCVT_ERR_INPUT the label grid has been written with unspecified
 // contents.
 #include "gcvt_internal.cuh"
