@@ -94,15 +94,16 @@ def support_pixels(rho):
 def jfa_line(n, ms, stats, peak, halo=16):
     """Jump-flooding labelling of the workload's sites: logical passes n/2 ..
     1 plus 1; launches = one per step above halo/2 plus one fused tail (halo/2
-    .. 1, 1); algorithmic 8 B per pixel per launch (labels in and out)."""
+    .. 1, 1), or one per pass for halo 0; algorithmic 8 B per pixel per launch
+    (labels in and out)."""
     k, passes = 1, 1
     while 2 * k <= n // 2:
         k *= 2
     while k >= 1:
         passes += 1
         k //= 2
-    tail = 1
-    while (1 << (tail - 1)) < halo:
+    tail = 1  # passes in the fused tail (halo 0: none, every pass its own launch)
+    while halo and (1 << (tail - 1)) < halo:
         tail += 1
     launches = passes - tail + 1
     alg = 8.0 * n * n * launches
