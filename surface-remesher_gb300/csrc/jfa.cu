@@ -51,7 +51,7 @@ constexpr int kTailThreads = 128;
 // a grid of side <= 8192 (|p|^2 < 2^27; |c - p|^2 < 2^30 with kJfaNone)
 constexpr unsigned kJfaBias = 1u << 27;
 // Tail of halo H: steps H/2, H/4, ..., 1 and the extra 1 (they sum to H) on
-// a (64 + 2H)^2 region; H = 8, 16 or 32 (the fusion depth the autotuner picks).
+// a (64 + 2H)^2 region; H = 8, 16 or 32 (fusion depths the autotuner tries).
 template <int H> __host__ __device__ constexpr int tail_reg() { return kTile + 2 * H; }
 template <int H> constexpr unsigned tail_bytes() {
   return 2u * tail_reg<H>() * tail_reg<H>() * 4u + 64u;  // two buffers + mbarrier
@@ -83,8 +83,8 @@ __device__ __forceinline__ uint4 final_labels(uint4 v) {
 }
 
 // The 16 words (r, s) of a unit at column x0 + (s - 1) cs, row y + (r - 1) k;
-// outside the grid kJfaNone.  (A separate untested path for units wholly
-// inside the grid measured slower: it raised the kernel's registers.)
+// outside the grid kJfaNone.  (A second path without the bounds tests, for
+// units wholly inside the grid, measured slower: it raised the registers.)
 __device__ __forceinline__ void unit_load(const uint32_t *__restrict__ in, int n, int x0, int y,
                                           int k, int cs, uint4 (&w)[4][4]) {
   const uint4 none = make_uint4(kJfaNone, kJfaNone, kJfaNone, kJfaNone);
